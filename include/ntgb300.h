@@ -1,0 +1,253 @@
+/*
+ * ntgb300.h - C ABI of the GB300-native spectral-element Helmholtz/Poisson
+ * hot path (ax_helm, gather-scatter, Jacobi-PCG, residual projection,
+ * mixed-precision flexible CG, learned initial guess, RAMP/Brinkman
+ * coefficient kernels and the masked vector kernels of neko-top).
+ *
+ * Conventions (the same as the reference's own C ABI in
+ * sources/neko_ext/math/bcknd/device/cuda/math_ext.cu:41-108 and its
+ * Fortran bind(c) blocks in sources/neko_ext/math/bcknd/device_math_ext.f90:43-103):
+ *   - plain C types only; field arrays are DEVICE pointers (Neko's x_d),
+ *     laid out as x(lx,ly,lz,nelv) with i fastest;
+ *   - real = double unless a function says float;
+ *   - every function returns an int status (NTG_OK = 0) instead of
+ *     aborting; the reference's cuda_* masked kernels keep their void
+ *     signature and report through ntg_last_error();
+ *   - masks are index lists with an explicit base (Neko masks are 1-based);
+ *   - a plan owns every buffer it allocates and frees it in *_destroy;
+ *     caller pointers are never freed by the library;
+ *   - all kernels of a plan run on the plan's stream (default: the legacy
+ *     default stream); calls on one plan are not re-entrant.
+ */
+#ifndef NTGB300_H
+#define NTGB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+  NTG_OK = 0,
+  NTG_ERR_INVALID = 1,     /* bad argument or handle */
+  NTG_ERR_CUDA = 2,        /* a CUDA call failed */
+  NTG_ERR_ALLOC = 3,       /* device allocation failed */
+  NTG_ERR_UNSUPPORTED = 4, /* polynomial order not compiled in */
+  NTG_MAXITER = 10,        /* solve stopped at max_iter before the tolerance */
+  NTG_BREAKDOWN = 11,      /* p.Ap <= 0 (operator not SPD) */
+  NTG_NONFINITE = 12,      /* NaN/Inf met in a residual or a dot product */
+  NTG_GUESS_REJECTED = 13  /* learned guess worse than the fallback; fallback used */
+};
+
+/* gather-scatter operations (Neko GS_OP_ADD/MUL/MIN/MAX) */
+enum { NTG_GS_ADD = 1, NTG_GS_MUL = 2, NTG_GS_MIN = 3, NTG_GS_MAX = 4 };
+
+/* precision selector for operator applications */
+enum { NTG_FP64 = 0, NTG_FP32 = 1 };
+
+/* Krylov solver types */
+enum {
+  NTG_KSP_CG = 0,        /* Jacobi-PCG, FP64 throughout (the plain drop-in) */
+  NTG_KSP_FCG_MIXED = 1  /* FP64 flexible CG whose preconditioner is an FP32
+                            Jacobi-PCG inner solve (FP32 Ax, FP32 Jacobi, FP32
+                            geometric factors); FP64 residuals and dots */
+};
+
+typedef struct ntg_plan ntg_plan; /* mesh + coef_t + gs_t + Jacobi state */
+typedef struct ntg_ksp ntg_ksp;   /* Krylov solver workspace */
+typedef struct ntg_proj ntg_proj; /* residual projection space */
+typedef struct ntg_guess ntg_guess; /* learned initial-guess network */
+
+/* ksp_monitor_t of the reference (iter, res_start, res_final;
+   sources/mapping_functions/PDE_filter_mapping.f90:265-272), plus the
+   status, the outer/inner split of the mixed solver and device time. */
+typedef struct ntg_monitor {
+  int iter;          /* outer iterations (CG: all iterations) */
+  int inner_iter;    /* total inner FP32 iterations (mixed solver) */
+  double res_start;  /* ||r0|| (mult-weighted, i.e. over unique nodes) */
+  double res_final;  /* ||r|| at exit, recomputed in FP64 */
+  double rhs_norm;   /* ||f|| */
+  int status;        /* NTG_OK, NTG_MAXITER, NTG_BREAKDOWN, NTG_NONFINITE */
+  int fp64_ax;       /* FP64 operator applications performed */
+} ntg_monitor;
+
+/* ---------------------------------------------------------------------- */
+/* library                                                                */
+/* ---------------------------------------------------------------------- */
+const char* ntg_version(void);
+/* message of the last error on this host thread ("" if none) */
+const char* ntg_last_error(void);
+/* compiled polynomial orders: writes up to cap values of lx, returns count */
+int ntg_supported_lx(int* lx, int cap);
+
+/* ---------------------------------------------------------------------- */
+/* mesh / coef_t / gs_t plan                                               */
+/* Replaces: coef_t init + gs_t init (Neko; called at                      */
+/* sources/adjoint/adjoint_scheme.f90:341-343) and dofmap_t's global ids.  */
+/* ---------------------------------------------------------------------- */
+/* Build a plan from node coordinates x_d,y_d,z_d (device, n = nelv*lx^3
+   doubles each) and global node ids glb_d (device, n int64; equal ids are
+   the same mesh node).  Computes G11..G33, B, mult and the gs maps on the
+   device. */
+int ntg_plan_create(ntg_plan** plan, int64_t nelv, int lx, const double* x_d, const double* y_d,
+                    const double* z_d, const int64_t* glb_d);
+int ntg_plan_destroy(ntg_plan* plan);
+/* stream: a cudaStream_t cast to void* (NULL = legacy default stream) */
+int ntg_plan_set_stream(ntg_plan* plan, void* stream);
+/* sizes: n local DOFs, nu unique nodes, nshared segments with > 1 copy */
+int ntg_plan_info(const ntg_plan* plan, int64_t* nelv, int* lx, int64_t* n, int64_t* nu, int64_t* nshared);
+/* copy the geometric factors / mass / multiplicity into caller device
+   arrays (any pointer may be NULL) */
+int ntg_coef_get(const ntg_plan* plan, double* g11_d, double* g12_d, double* g13_d, double* g22_d,
+                 double* g23_d, double* g33_d, double* B_d, double* mult_d);
+/* Helmholtz coefficients (coef%h1, coef%h2, coef%ifh2).  h1_d == NULL ->
+   constant h1c; h2_d == NULL with ifh2 -> constant h2c; ifh2 == 0 -> no
+   mass term.  Values are copied (FP64 and FP32); h2*B is precombined. */
+int ntg_coef_set(ntg_plan* plan, const double* h1_d, double h1c, const double* h2_d, double h2c, int ifh2);
+/* Dirichlet mask (bc_list): index list mask_d (device int32, nmask
+   entries) in base `base` (1 for Neko masks).  nmask == 0 clears it. */
+int ntg_plan_set_mask(ntg_plan* plan, const int32_t* mask_d, int64_t nmask, int base);
+/* gs maps: perm (n int32: local indices sorted by global id, stable) and
+   offs (nu+1 int64 segment offsets), device arrays */
+int ntg_gs_export(const ntg_plan* plan, int32_t* perm_d, int64_t* offs_d);
+
+/* ---------------------------------------------------------------------- */
+/* synthetic mesh generator (replaces Neko's genmeshbox for the tests and  */
+/* benchmark; examples/rugby_ball/prepare.sh uses genmeshbox)             */
+/* ---------------------------------------------------------------------- */
+/* Box of ex*ey*ez hexes on [lo,hi]^3 with GLL nodes of order lx-1 and a
+   seeded sinusoidal deformation of amplitude amp*h per axis. Writes
+   coordinates and global ids (device arrays of n entries). */
+int ntg_mesh_box(int ex, int ey, int ez, int lx, const double* lo3, const double* hi3, double amp,
+                 uint64_t seed, double* x_d, double* y_d, double* z_d, int64_t* glb_d, void* stream);
+/* 1-based local indices of the x = hi face (nmask = ex*ey*ez/ex * lx^2
+   entries when mask_d != NULL).  Returns the count in *nmask. */
+int ntg_mask_face_xmax(int ex, int ey, int ez, int lx, int32_t* mask_d, int64_t* nmask, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* ax_t (ax_helm): w = h1 (D^T G D) u + h2 B u, element-local.            */
+/* Replaces: ax_helm_factory(Ax, full_formulation=.false.)%compute (Neko; */
+/* sources/mapping_functions/PDE_filter_mapping.f90:177,256,               */
+/* sources/adjoint/adjoint_pnpn.f90:207,217).                              */
+/* ---------------------------------------------------------------------- */
+int ntg_ax_helm(ntg_plan* plan, double* w_d, const double* u_d);
+int ntg_ax_helm_f32(ntg_plan* plan, float* w_d, const float* u_d);
+
+/* ---------------------------------------------------------------------- */
+/* gs_t%op(u, n, op) (Neko; sources/adjoint/adjoint_pnpn.f90:725,755-757, */
+/* sources/mapping_functions/PDE_filter_mapping.f90:249)                  */
+/* ---------------------------------------------------------------------- */
+int ntg_gs_op(ntg_plan* plan, double* u_d, int op);
+int ntg_gs_op_f32(ntg_plan* plan, float* u_d, int op);
+
+/* bc_list_apply_scalar(bclst, x, n): zero the masked entries
+   (sources/adjoint/adjoint_pnpn.f90:726) */
+int ntg_bc_apply_scalar(ntg_plan* plan, double* x_d);
+
+/* ---------------------------------------------------------------------- */
+/* pc_t (Jacobi): update() builds 1/gs(diag A) in FP64 and FP32;          */
+/* solve(z, r) applies it.  (sources/adjoint/adjoint_pnpn.f90:732,781,     */
+/* sources/mapping_functions/PDE_filter_mapping.f90:262,365-400)          */
+/* ---------------------------------------------------------------------- */
+int ntg_pc_jacobi_update(ntg_plan* plan);
+int ntg_pc_jacobi_solve(ntg_plan* plan, double* z_d, const double* r_d);
+/* copy the FP64 inverse diagonal into dinv_d */
+int ntg_pc_jacobi_get(const ntg_plan* plan, double* dinv_d);
+
+/* ---------------------------------------------------------------------- */
+/* ksp_t: krylov_solver_factory(ksp, n, type, max_iter, abstol) / solve /  */
+/* krylov_solver_destroy (sources/adjoint/adjoint_scheme.f90:1046-1055,    */
+/* sources/mapping_functions/PDE_filter_mapping.f90:180-181,197,255-257). */
+/* Stopping test: ||r|| <= max(abstol, rtol*||f||), norms weighted by     */
+/* mult (unique-node Euclidean norm of the assembled residual).           */
+/* ---------------------------------------------------------------------- */
+int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double abstol, ntg_ksp** ksp);
+int ntg_ksp_destroy(ntg_ksp* ksp);
+/* mixed solver: inner relative tolerance and inner iteration cap */
+int ntg_ksp_set_inner(ntg_ksp* ksp, double inner_rtol, int inner_max_iter);
+/* how many iterations run between host convergence checks (default 16) */
+int ntg_ksp_set_check_every(ntg_ksp* ksp, int every);
+/* x_d: initial guess in, solution out.  f_d: assembled, masked RHS. */
+int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon);
+/* solve_coupled for three components with one operator
+   (sources/adjoint/adjoint_pnpn.f90:784-786) */
+int ntg_ksp_solve_coupled(ntg_ksp* ksp, double* x_d, double* y_d, double* z_d, const double* fx_d,
+                          const double* fy_d, const double* fz_d, ntg_monitor* mon3);
+
+/* ---------------------------------------------------------------------- */
+/* projection_t (Fischer residual projection): init(n, L) / pre_solving / */
+/* post_solving / free (sources/adjoint/adjoint_pnpn.f90:365-374,729-741) */
+/* ---------------------------------------------------------------------- */
+int ntg_proj_create(ntg_plan* plan, int L, ntg_proj** proj);
+int ntg_proj_destroy(ntg_proj* proj);
+/* b_d (assembled, masked) is replaced by b - A xbar; xbar is kept */
+int ntg_proj_pre_solving(ntg_proj* proj, double* b_d);
+/* x_d: the correction solved for on entry, the full solution on exit;
+   one FP64 operator application updates the basis */
+int ntg_proj_post_solving(ntg_proj* proj, double* x_d);
+int ntg_proj_size(const ntg_proj* proj);
+
+/* ---------------------------------------------------------------------- */
+/* dot products (FP64 accumulation, deterministic order)                   */
+/* ---------------------------------------------------------------------- */
+/* glsc3(a, b, c) = sum a*b*c over n entries */
+int ntg_glsc3(ntg_plan* plan, const double* a_d, const double* b_d, const double* c_d, int64_t n, double* out);
+
+/* ---------------------------------------------------------------------- */
+/* coefficient path                                                        */
+/* ---------------------------------------------------------------------- */
+/* RAMP mapping (sources/mapping_functions/RAMP_mapping.f90:182-267) */
+int ntg_ramp_forward(double* xout_d, const double* xin_d, int64_t n, double fmin, double fmax, double q,
+                     int convex_up, void* stream);
+int ntg_ramp_backward(double* dF_din_d, const double* dF_dout_d, const double* xin_d, int64_t n, double fmin,
+                      double fmax, double q, int convex_up, void* stream);
+/* simple_brinkman_source_term compute: f_c -= u_c * chi
+   (sources/source_terms/simple_brinkman_source_term.f90:139-153);
+   mask_d == NULL -> all n entries, else the masked entries (base `base`) */
+int ntg_brinkman_compute(double* fx_d, double* fy_d, double* fz_d, const double* u_d, const double* v_d,
+                         const double* w_d, const double* chi_d, int64_t n, const int32_t* mask_d,
+                         int64_t nmask, int base, void* stream);
+/* permeability kappa(phi), negated (sources/topology_optimization/design.f90:316-348) */
+int ntg_permeability(double* kappa_d, const double* phi_d, int64_t n, double perm0, double perm1,
+                     double penalty, void* stream);
+/* minimum-dissipation sensitivity -u.u_adj (+ K|u|^2), FP64
+   (sources/objectives/minimum_dissipation_objective_function.f90:260-301) */
+int ntg_sens_min_dissipation(double* s_d, const double* u_d, const double* v_d, const double* w_d,
+                             const double* ua_d, const double* va_d, const double* wa_d, int64_t n,
+                             int if_lube, double K_scale, void* stream);
+/* PDE filter (r^2 K + B) X_out = B X_in, all-Neumann, guess = X_in
+   (sources/mapping_functions/PDE_filter_mapping.f90:212-278 forward,
+   :298-363 backward).  Overwrites the plan's h1/h2. */
+int ntg_filter_apply(ntg_plan* plan, ntg_ksp* ksp, double* X_out_d, const double* X_in_d, double r,
+                     ntg_monitor* mon);
+
+/* ---------------------------------------------------------------------- */
+/* masked vector kernels of neko-top, same names and signatures as the     */
+/* reference's extern "C" wrappers (math_ext.cu:49-108): device arrays by  */
+/* value, sizes and scalars by pointer, 1-based masks, real = double.      */
+/* They run on the stream set with ntg_set_glb_queue (default stream 0).  */
+/* ---------------------------------------------------------------------- */
+void cuda_cadd_mask(void* a, double* c, int* size, int* mask, int* mask_size);
+void cuda_invcol1_mask(void* a, int* size, int* mask, int* mask_size);
+void cuda_col2_mask(void* a, void* b, int* size, int* mask, int* mask_size);
+void cuda_col3_mask(void* a, void* b, void* c, int* size, int* mask, int* mask_size);
+void cuda_sub3_mask(void* a, void* b, void* c, int* size, int* mask, int* mask_size);
+/* cmult_mask and glsc2_mask exist on the CPU only in the reference
+   (math_ext.f90:40-52,99-116); these are their device versions. */
+void cuda_cmult_mask(void* a, double* c, int* size, int* mask, int* mask_size);
+double cuda_glsc2_mask(void* a, void* b, int* size, int* mask, int* mask_size);
+/* the stream the cuda_* kernels use (Neko's glb_cmd_queue) */
+void ntg_set_glb_queue(void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#endif /* NTGB300_H */

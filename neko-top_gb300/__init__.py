@@ -1,0 +1,38 @@
+"""GB300-native spectral-element Helmholtz/Poisson hot path.
+
+Python host side over the C ABI (include/ntgb300.h) of ``lib/libntgb300.so``.
+The classes mirror the Neko/neko-top interfaces the reference drives on this
+path, with the same names and argument meaning:
+
+    coef_t / dofmap      mesh, geometric factors, mult, gs maps   (Neko coef_t, gs_t%init)
+    gs_t.op              direct stiffness summation              (gs_t%op(u, n, GS_OP_ADD))
+    ax_helm_t.compute    w = h1 K u + h2 B u                     (ax_helm)
+    jacobi_t             update / solve                          (pc_t, jacobi)
+    krylov_solver_factory -> ksp.solve / solve_coupled           (ksp_t, ksp_monitor_t)
+    projection_t         pre_solving / post_solving              (projection_t)
+    RAMP_mapping_t       apply_forward / apply_backward          (sources/mapping_functions/RAMP_mapping.f90)
+    PDE_filter_t         apply_forward / apply_backward          (sources/mapping_functions/PDE_filter_mapping.f90)
+    simple_brinkman_source_term_t.compute                        (sources/source_terms/simple_brinkman_source_term.f90)
+    cadd_mask ... glsc2_mask                                     (sources/neko_ext/math/math_ext.f90)
+
+Field arguments are CUDA tensors (torch) laid out like Neko's x(lx,ly,lz,nelv):
+contiguous, i fastest.  Only their device pointers cross the boundary.  There
+is no CPU fallback: if the CUDA library is missing, importing the native
+module raises.
+"""
+from __future__ import annotations
+
+from ._native import (GS_OP_ADD, GS_OP_MAX, GS_OP_MIN, GS_OP_MUL, KSP_CG, KSP_FCG_MIXED, NTG_BREAKDOWN,
+                      NTG_MAXITER, NTG_NONFINITE, NTG_OK, NtgError, library_path, lib)
+from .api import (PDE_filter_t, RAMP_mapping_t, ax_helm_t, build_box, cadd_mask, cmult_mask, coef_t, col2_mask,
+                  col3_mask, glsc2_mask, glsc3, gs_t, invcol1_mask, jacobi_t, krylov_solver_factory, ksp_monitor_t,
+                  mask_face_xmax, permeability, projection_t, sens_min_dissipation, simple_brinkman_source_term_t,
+                  sub3_mask)
+
+__all__ = [
+    "GS_OP_ADD", "GS_OP_MUL", "GS_OP_MIN", "GS_OP_MAX", "KSP_CG", "KSP_FCG_MIXED", "NTG_OK", "NTG_MAXITER",
+    "NTG_BREAKDOWN", "NTG_NONFINITE", "NtgError", "library_path", "lib", "coef_t", "gs_t", "ax_helm_t", "jacobi_t",
+    "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
+    "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
+    "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
+]

@@ -1,0 +1,120 @@
+"""ctypes binding of the C ABI in include/ntgb300.h (no torch types cross it)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "lib", "libntgb300.so")
+
+NTG_OK, NTG_ERR_INVALID, NTG_ERR_CUDA, NTG_ERR_ALLOC, NTG_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
+NTG_MAXITER, NTG_BREAKDOWN, NTG_NONFINITE, NTG_GUESS_REJECTED = 10, 11, 12, 13
+GS_OP_ADD, GS_OP_MUL, GS_OP_MIN, GS_OP_MAX = 1, 2, 3, 4
+KSP_CG, KSP_FCG_MIXED = 0, 1
+
+_vp = C.c_void_p
+_i = C.c_int
+_i64 = C.c_int64
+_d = C.c_double
+_pi64 = C.POINTER(C.c_int64)
+_pi = C.POINTER(C.c_int)
+_pd = C.POINTER(C.c_double)
+
+
+class ntg_monitor(C.Structure):
+    _fields_ = [("iter", C.c_int), ("inner_iter", C.c_int), ("res_start", C.c_double),
+                ("res_final", C.c_double), ("rhs_norm", C.c_double), ("status", C.c_int),
+                ("fp64_ax", C.c_int)]
+
+
+class NtgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"ntgb300 status {status}: {msg}")
+        self.status = status
+
+
+# name -> (restype, argtypes); every symbol include/ntgb300.h declares
+SIGNATURES = {
+    "ntg_version": (C.c_char_p, []),
+    "ntg_last_error": (C.c_char_p, []),
+    "ntg_supported_lx": (_i, [_pi, _i]),
+    "ntg_plan_create": (_i, [C.POINTER(_vp), _i64, _i, _vp, _vp, _vp, _vp]),
+    "ntg_plan_destroy": (_i, [_vp]),
+    "ntg_plan_set_stream": (_i, [_vp, _vp]),
+    "ntg_plan_info": (_i, [_vp, _pi64, _pi, _pi64, _pi64, _pi64]),
+    "ntg_coef_get": (_i, [_vp] + [_vp] * 8),
+    "ntg_coef_set": (_i, [_vp, _vp, _d, _vp, _d, _i]),
+    "ntg_plan_set_mask": (_i, [_vp, _vp, _i64, _i]),
+    "ntg_gs_export": (_i, [_vp, _vp, _vp]),
+    "ntg_mesh_box": (_i, [_i, _i, _i, _i, _pd, _pd, _d, C.c_uint64, _vp, _vp, _vp, _vp, _vp]),
+    "ntg_mask_face_xmax": (_i, [_i, _i, _i, _i, _vp, _pi64, _vp]),
+    "ntg_ax_helm": (_i, [_vp, _vp, _vp]),
+    "ntg_ax_helm_f32": (_i, [_vp, _vp, _vp]),
+    "ntg_gs_op": (_i, [_vp, _vp, _i]),
+    "ntg_gs_op_f32": (_i, [_vp, _vp, _i]),
+    "ntg_bc_apply_scalar": (_i, [_vp, _vp]),
+    "ntg_pc_jacobi_update": (_i, [_vp]),
+    "ntg_pc_jacobi_solve": (_i, [_vp, _vp, _vp]),
+    "ntg_pc_jacobi_get": (_i, [_vp, _vp]),
+    "ntg_ksp_create": (_i, [_vp, _i, _i, _d, _d, C.POINTER(_vp)]),
+    "ntg_ksp_destroy": (_i, [_vp]),
+    "ntg_ksp_set_inner": (_i, [_vp, _d, _i]),
+    "ntg_ksp_set_check_every": (_i, [_vp, _i]),
+    "ntg_ksp_solve": (_i, [_vp, _vp, _vp, C.POINTER(ntg_monitor)]),
+    "ntg_ksp_solve_coupled": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(ntg_monitor)]),
+    "ntg_proj_create": (_i, [_vp, _i, C.POINTER(_vp)]),
+    "ntg_proj_destroy": (_i, [_vp]),
+    "ntg_proj_pre_solving": (_i, [_vp, _vp]),
+    "ntg_proj_post_solving": (_i, [_vp, _vp]),
+    "ntg_proj_size": (_i, [_vp]),
+    "ntg_glsc3": (_i, [_vp, _vp, _vp, _vp, _i64, _pd]),
+    "ntg_ramp_forward": (_i, [_vp, _vp, _i64, _d, _d, _d, _i, _vp]),
+    "ntg_ramp_backward": (_i, [_vp, _vp, _vp, _i64, _d, _d, _d, _i, _vp]),
+    "ntg_brinkman_compute": (_i, [_vp] * 7 + [_i64, _vp, _i64, _i, _vp]),
+    "ntg_permeability": (_i, [_vp, _vp, _i64, _d, _d, _d, _vp]),
+    "ntg_sens_min_dissipation": (_i, [_vp] * 7 + [_i64, _i, _d, _vp]),
+    "ntg_filter_apply": (_i, [_vp, _vp, _vp, _vp, _d, C.POINTER(ntg_monitor)]),
+    "cuda_cadd_mask": (None, [_vp, _pd, _pi, _vp, _pi]),
+    "cuda_invcol1_mask": (None, [_vp, _pi, _vp, _pi]),
+    "cuda_col2_mask": (None, [_vp, _vp, _pi, _vp, _pi]),
+    "cuda_col3_mask": (None, [_vp, _vp, _vp, _pi, _vp, _pi]),
+    "cuda_sub3_mask": (None, [_vp, _vp, _vp, _pi, _vp, _pi]),
+    "cuda_cmult_mask": (None, [_vp, _pd, _pi, _vp, _pi]),
+    "cuda_glsc2_mask": (_d, [_vp, _vp, _pi, _vp, _pi]),
+    "ntg_set_glb_queue": (None, [_vp]),
+}
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            raise NtgError(-1, f"CUDA library missing: {_LIB} (run build() first); there is no CPU fallback")
+        L = C.CDLL(_LIB)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> int:
+    """Raise NtgError for hard errors; solver statuses (>= 10) are returned."""
+    if status != NTG_OK and status < 10:
+        raise NtgError(status, lib().ntg_last_error().decode())
+    return status
+
+
+def check_last(name: str) -> None:
+    """For the void cuda_* kernels: raise if they recorded an error."""
+    msg = lib().ntg_last_error().decode()
+    if msg:
+        raise NtgError(NTG_ERR_CUDA, f"{name}: {msg}")

@@ -1,0 +1,417 @@
+"""Neko-shaped host interface over the C ABI.
+
+Argument meaning, order and error behaviour follow the reference's call
+sites (file:line given per class).  Device memory comes from torch CUDA
+tensors; the library sees raw pointers only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import torch
+
+from ._native import (GS_OP_ADD, KSP_CG, KSP_FCG_MIXED, NtgError, check, check_last, lib, ntg_monitor)
+
+_DT = {torch.float64: "f64", torch.float32: "f32", torch.int32: "i32", torch.int64: "i64"}
+
+
+def _ptr(t, dtype=torch.float64, n=None, name="array"):
+    if t is None:
+        return None
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name}: expected a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name}: expected {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name}: must be contiguous")
+    if n is not None and t.numel() != n:
+        raise ValueError(f"{name}: expected {n} entries, got {t.numel()}")
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@dataclass
+class ksp_monitor_t:
+    """Neko's ksp_monitor_t (iter, res_start, res_final;
+    sources/mapping_functions/PDE_filter_mapping.f90:265-272) plus the
+    status and the mixed solver's inner/FP64 counts."""
+    iter: int
+    res_start: float
+    res_final: float
+    rhs_norm: float
+    status: int
+    inner_iter: int = 0
+    fp64_ax: int = 0
+
+    @classmethod
+    def from_c(cls, m: ntg_monitor):
+        return cls(m.iter, m.res_start, m.res_final, m.rhs_norm, m.status, m.inner_iter, m.fp64_ax)
+
+
+def mask_face_xmax(ex, ey, ez, lx, device="cuda"):
+    """1-based local indices of the x = max face (a Dirichlet mask)."""
+    n = C.c_int64(0)
+    check(lib().ntg_mask_face_xmax(ex, ey, ez, lx, None, C.byref(n), None))
+    m = torch.empty(n.value, dtype=torch.int32, device=device)
+    check(lib().ntg_mask_face_xmax(ex, ey, ez, lx, _ptr(m, torch.int32), C.byref(n), _stream()))
+    return m
+
+
+def build_box(ex, ey, ez, lx=8, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.0, seed=0, device="cuda"):
+    """Synthetic box mesh (coordinates and global ids) on the device."""
+    n = ex * ey * ez * lx ** 3
+    x = torch.empty(n, dtype=torch.float64, device=device)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    gid = torch.empty(n, dtype=torch.int64, device=device)
+    lo3 = (C.c_double * 3)(*lo)
+    hi3 = (C.c_double * 3)(*hi)
+    check(lib().ntg_mesh_box(ex, ey, ez, lx, lo3, hi3, float(amp), int(seed), _ptr(x), _ptr(y), _ptr(z),
+                             _ptr(gid, torch.int64), _stream()))
+    return x, y, z, gid
+
+
+class coef_t:
+    """Mesh + geometric factors + gather-scatter plan (Neko's coef_t and
+    gs_t, built at sources/adjoint/adjoint_scheme.f90:341-343)."""
+
+    def __init__(self, nelv, lx, x, y, z, glb_ids):
+        n = nelv * lx ** 3
+        h = C.c_void_p()
+        check(lib().ntg_plan_create(C.byref(h), int(nelv), int(lx), _ptr(x, n=n, name="x"), _ptr(y, n=n, name="y"),
+                                    _ptr(z, n=n, name="z"), _ptr(glb_ids, torch.int64, n, "glb_ids")))
+        self._h = h
+        check(lib().ntg_plan_set_stream(h, _stream()))
+        ne, l, nn, nu, nsh = C.c_int64(), C.c_int(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().ntg_plan_info(h, C.byref(ne), C.byref(l), C.byref(nn), C.byref(nu), C.byref(nsh)))
+        self.nelv, self.lx, self.n, self.nu, self.nshared = ne.value, l.value, nn.value, nu.value, nsh.value
+        self.device = x.device
+        self.mask = None
+
+    @classmethod
+    def box(cls, ex, ey, ez, lx=8, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.0, seed=0, device="cuda"):
+        x, y, z, gid = build_box(ex, ey, ez, lx, lo, hi, amp, seed, device)
+        c = cls(ex * ey * ez, lx, x, y, z, gid)
+        c.x, c.y, c.z, c.gid = x, y, z, gid
+        c.box_dims = (ex, ey, ez)
+        c.lo, c.hi = tuple(lo), tuple(hi)
+        return c
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise NtgError(1, "coef_t used after free()")
+        return self._h
+
+    def set_coefs(self, h1=None, h1c=1.0, h2=None, h2c=0.0, ifh2=False):
+        """coef%h1, coef%h2, coef%ifh2 (sources/mapping_functions/PDE_filter_mapping.f90:225-241)."""
+        check(lib().ntg_coef_set(self.handle, _ptr(h1, n=self.n, name="h1"), float(h1c), _ptr(h2, n=self.n, name="h2"),
+                                 float(h2c), int(bool(ifh2))))
+
+    def set_mask(self, mask, base=1):
+        """Dirichlet index list (bc_list); Neko masks are 1-based."""
+        if mask is None or mask.numel() == 0:
+            check(lib().ntg_plan_set_mask(self.handle, None, 0, int(base)))
+            self.mask = None
+            return
+        check(lib().ntg_plan_set_mask(self.handle, _ptr(mask, torch.int32, name="mask"), mask.numel(), int(base)))
+        self.mask = mask
+
+    def geometry(self):
+        out = {k: torch.empty(self.n, dtype=torch.float64, device=self.device)
+               for k in ("g11", "g12", "g13", "g22", "g23", "g33", "B", "mult")}
+        check(lib().ntg_coef_get(self.handle, *[_ptr(out[k]) for k in ("g11", "g12", "g13", "g22", "g23", "g33", "B",
+                                                                         "mult")]))
+        torch.cuda.synchronize()
+        return out
+
+    def gs_maps(self):
+        perm = torch.empty(self.n, dtype=torch.int32, device=self.device)
+        offs = torch.empty(self.nu + 1, dtype=torch.int64, device=self.device)
+        check(lib().ntg_gs_export(self.handle, _ptr(perm, torch.int32), _ptr(offs, torch.int64)))
+        torch.cuda.synchronize()
+        return perm, offs
+
+    def free(self):
+        if self._h is not None:
+            check(lib().ntg_plan_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class gs_t:
+    """gs_t%op(u, n, op) (sources/adjoint/adjoint_pnpn.f90:725)."""
+
+    def __init__(self, coef: coef_t):
+        self.coef = coef
+
+    def op(self, u, op=GS_OP_ADD):
+        if u.dtype == torch.float32:
+            check(lib().ntg_gs_op_f32(self.coef.handle, _ptr(u, torch.float32, self.coef.n, "u"), int(op)))
+        else:
+            check(lib().ntg_gs_op(self.coef.handle, _ptr(u, n=self.coef.n, name="u"), int(op)))
+
+
+class ax_helm_t:
+    """Ax%compute(w, u, coef, msh, Xh) of ax_helm
+    (sources/mapping_functions/PDE_filter_mapping.f90:177,256)."""
+
+    def compute(self, w, u, coef: coef_t):
+        if u.dtype == torch.float32:
+            check(lib().ntg_ax_helm_f32(coef.handle, _ptr(w, torch.float32, coef.n, "w"),
+                                        _ptr(u, torch.float32, coef.n, "u")))
+        else:
+            check(lib().ntg_ax_helm(coef.handle, _ptr(w, n=coef.n, name="w"), _ptr(u, n=coef.n, name="u")))
+
+
+def bc_list_apply_scalar(coef: coef_t, x):
+    check(lib().ntg_bc_apply_scalar(coef.handle, _ptr(x, n=coef.n, name="x")))
+
+
+class jacobi_t:
+    """Jacobi pc_t: init(coef, dof, gs), update(), solve(z, r)
+    (sources/mapping_functions/PDE_filter_mapping.f90:365-400)."""
+
+    def __init__(self, coef: coef_t):
+        self.coef = coef
+
+    def update(self):
+        check(lib().ntg_pc_jacobi_update(self.coef.handle))
+
+    def solve(self, z, r):
+        check(lib().ntg_pc_jacobi_solve(self.coef.handle, _ptr(z, n=self.coef.n, name="z"),
+                                        _ptr(r, n=self.coef.n, name="r")))
+
+    def dinv(self):
+        d = torch.empty(self.coef.n, dtype=torch.float64, device=self.coef.device)
+        check(lib().ntg_pc_jacobi_get(self.coef.handle, _ptr(d)))
+        torch.cuda.synchronize()
+        return d
+
+
+class _ksp:
+    def __init__(self, coef: coef_t, type_: int, max_iter: int, rtol: float, abstol: float):
+        self.coef = coef
+        h = C.c_void_p()
+        check(lib().ntg_ksp_create(coef.handle, int(type_), int(max_iter), float(rtol), float(abstol), C.byref(h)))
+        self._h = h
+        self.type = type_
+        self.max_iter = max_iter
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_inner(self, inner_rtol=1e-4, inner_max_iter=400):
+        check(lib().ntg_ksp_set_inner(self._h, float(inner_rtol), int(inner_max_iter)))
+
+    def set_check_every(self, k):
+        check(lib().ntg_ksp_set_check_every(self._h, int(k)))
+
+    def solve(self, x, f) -> ksp_monitor_t:
+        """ksp%solve(Ax, x, f, n, coef, blst, gs): x = guess in, solution out;
+        f = assembled, masked RHS."""
+        mon = ntg_monitor()
+        check(lib().ntg_ksp_solve(self._h, _ptr(x, n=self.coef.n, name="x"), _ptr(f, n=self.coef.n, name="f"),
+                                  C.byref(mon)))
+        return ksp_monitor_t.from_c(mon)
+
+    def solve_coupled(self, x, y, z, fx, fy, fz):
+        mons = (ntg_monitor * 3)()
+        n = self.coef.n
+        check(lib().ntg_ksp_solve_coupled(self._h, _ptr(x, n=n), _ptr(y, n=n), _ptr(z, n=n), _ptr(fx, n=n),
+                                          _ptr(fy, n=n), _ptr(fz, n=n), mons))
+        return [ksp_monitor_t.from_c(m) for m in mons]
+
+    def free(self):
+        if self._h is not None:
+            check(lib().ntg_ksp_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def krylov_solver_factory(coef: coef_t, type_: str = "cg", max_iter: int = 800, rtol: float = 1e-10,
+                          abstol: float = 0.0) -> _ksp:
+    """krylov_solver_factory(ksp, n, type, max_iter, abstol)
+    (sources/adjoint/adjoint_scheme.f90:1046-1055).  type: 'cg' (FP64
+    Jacobi-PCG) or 'fcg_mixed' (FP32 inner PCG in an FP64 flexible CG)."""
+    t = {"cg": KSP_CG, "fcg_mixed": KSP_FCG_MIXED}.get(type_)
+    if t is None:
+        raise ValueError(f"unknown solver type {type_!r}")
+    return _ksp(coef, t, max_iter, rtol, abstol)
+
+
+class projection_t:
+    """Residual projection: init(n, L), pre_solving(b), post_solving(x)
+    (sources/adjoint/adjoint_pnpn.f90:365-374,729-741)."""
+
+    def __init__(self, coef: coef_t, L: int = 20):
+        self.coef = coef
+        h = C.c_void_p()
+        check(lib().ntg_proj_create(coef.handle, int(L), C.byref(h)))
+        self._h = h
+        self.L = L
+
+    def pre_solving(self, b):
+        check(lib().ntg_proj_pre_solving(self._h, _ptr(b, n=self.coef.n, name="b")))
+
+    def post_solving(self, x):
+        check(lib().ntg_proj_post_solving(self._h, _ptr(x, n=self.coef.n, name="x")))
+
+    @property
+    def size(self):
+        return int(lib().ntg_proj_size(self._h))
+
+    def free(self):
+        if self._h is not None:
+            check(lib().ntg_proj_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def glsc3(coef: coef_t, a, b, c=None) -> float:
+    out = C.c_double()
+    n = a.numel()
+    check(lib().ntg_glsc3(coef.handle, _ptr(a, n=n), _ptr(b, n=n), _ptr(c, n=n) if c is not None else None, n,
+                          C.byref(out)))
+    return out.value
+
+
+class RAMP_mapping_t:
+    """RAMP mapping (sources/mapping_functions/RAMP_mapping.f90:101-267);
+    defaults of RAMP_mapping_init_from_json (f_min 0, f_max 1000, q 1,
+    convex_up)."""
+
+    def __init__(self, f_min=0.0, f_max=1000.0, q=1.0, convex_up=True):
+        self.f_min, self.f_max, self.q, self.convex_up = f_min, f_max, q, convex_up
+
+    def apply_forward(self, X_out, X_in):
+        check(lib().ntg_ramp_forward(_ptr(X_out), _ptr(X_in), X_in.numel(), self.f_min, self.f_max, self.q,
+                                     int(self.convex_up), _stream()))
+
+    def apply_backward(self, dF_dX_in, dF_dX_out, X_in):
+        check(lib().ntg_ramp_backward(_ptr(dF_dX_in), _ptr(dF_dX_out), _ptr(X_in), X_in.numel(), self.f_min,
+                                      self.f_max, self.q, int(self.convex_up), _stream()))
+
+
+class PDE_filter_t:
+    """PDE density filter (sources/mapping_functions/PDE_filter_mapping.f90:126-363):
+    (r^2 K + B) X_out = B X_in, all-Neumann, initial guess X_in; r = 0.01,
+    abstol 1e-10, 200 iterations by default."""
+
+    def __init__(self, coef: coef_t, r=0.01, abstol=1e-10, max_iter=200):
+        self.coef, self.r = coef, r
+        self.ksp = krylov_solver_factory(coef, "cg", max_iter, 0.0, abstol)
+        self.ksp_results = None
+
+    def _apply(self, X_out, X_in):
+        mon = ntg_monitor()
+        check(lib().ntg_filter_apply(self.coef.handle, self.ksp.handle, _ptr(X_out, n=self.coef.n),
+                                     _ptr(X_in, n=self.coef.n), float(self.r), C.byref(mon)))
+        self.ksp_results = ksp_monitor_t.from_c(mon)
+        return self.ksp_results
+
+    def apply_forward(self, X_out, X_in):
+        return self._apply(X_out, X_in)
+
+    def apply_backward(self, dF_dX_in, dF_dX_out, X_in=None):
+        return self._apply(dF_dX_in, dF_dX_out)
+
+
+class simple_brinkman_source_term_t:
+    """f -= chi * u per component
+    (sources/source_terms/simple_brinkman_source_term.f90:139-153)."""
+
+    def __init__(self, fx, fy, fz, u, v, w, chi):
+        self.fields = (fx, fy, fz)
+        self.u, self.v, self.w, self.chi = u, v, w, chi
+
+    def compute(self, t=0.0, tstep=0, mask=None, base=1):
+        fx, fy, fz = self.fields
+        check(lib().ntg_brinkman_compute(_ptr(fx), _ptr(fy), _ptr(fz), _ptr(self.u), _ptr(self.v), _ptr(self.w),
+                                         _ptr(self.chi), fx.numel(), _ptr(mask, torch.int32) if mask is not None
+                                         else None, 0 if mask is None else mask.numel(), int(base), _stream()))
+
+
+def permeability(kappa, phi, perm0, perm1, penalty):
+    """design_t%update_permeability (sources/topology_optimization/design.f90:316-348)."""
+    check(lib().ntg_permeability(_ptr(kappa), _ptr(phi), phi.numel(), float(perm0), float(perm1), float(penalty),
+                                 _stream()))
+
+
+def sens_min_dissipation(s, u, v, w, ua, va, wa, if_lube=False, K_scale=0.0):
+    check(lib().ntg_sens_min_dissipation(_ptr(s), _ptr(u), _ptr(v), _ptr(w), _ptr(ua), _ptr(va), _ptr(wa), u.numel(),
+                                         int(bool(if_lube)), float(K_scale), _stream()))
+
+
+# masked ops: the reference's cuda_* entry points (math_ext.cu:49-108)
+def _mi(mask):
+    return C.byref(C.c_int(int(mask.numel())))
+
+
+def _queue():
+    lib().ntg_set_glb_queue(_stream())
+
+
+def cadd_mask(a, c, mask):
+    _queue()
+    lib().cuda_cadd_mask(_ptr(a), C.byref(C.c_double(c)), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32),
+                         _mi(mask))
+    check_last("cuda_cadd_mask")
+
+
+def invcol1_mask(a, mask):
+    _queue()
+    lib().cuda_invcol1_mask(_ptr(a), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32), _mi(mask))
+    check_last("cuda_invcol1_mask")
+
+
+def cmult_mask(a, c, mask):
+    _queue()
+    lib().cuda_cmult_mask(_ptr(a), C.byref(C.c_double(c)), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32),
+                          _mi(mask))
+    check_last("cuda_cmult_mask")
+
+
+def col2_mask(a, b, mask):
+    _queue()
+    lib().cuda_col2_mask(_ptr(a), _ptr(b), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32), _mi(mask))
+    check_last("cuda_col2_mask")
+
+
+def col3_mask(a, b, c, mask):
+    _queue()
+    lib().cuda_col3_mask(_ptr(a), _ptr(b), _ptr(c), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32), _mi(mask))
+    check_last("cuda_col3_mask")
+
+
+def sub3_mask(a, b, c, mask):
+    _queue()
+    lib().cuda_sub3_mask(_ptr(a), _ptr(b), _ptr(c), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32), _mi(mask))
+    check_last("cuda_sub3_mask")
+
+
+def glsc2_mask(a, b, mask) -> float:
+    _queue()
+    v = lib().cuda_glsc2_mask(_ptr(a), _ptr(b), C.byref(C.c_int(a.numel())), _ptr(mask, torch.int32), _mi(mask))
+    check_last("cuda_glsc2_mask")
+    return float(v)

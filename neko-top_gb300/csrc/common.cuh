@@ -1,0 +1,152 @@
+// Shared definitions of the GB300 SEM library: error handling, the plan
+// structure, device scalar block and deterministic reductions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/ntgb300.h"
+
+#define NTG_LXMAX 12
+
+namespace ntg {
+
+void set_error(const char* fmt, ...);
+void clear_error();
+
+// Returns NTG_ERR_CUDA (and records the message) if a CUDA call failed.
+#define NTG_CUDA_TRY(call)                                                             \
+  do {                                                                                 \
+    cudaError_t _e = (call);                                                           \
+    if (_e != cudaSuccess) {                                                           \
+      ::ntg::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(_e)); \
+      return NTG_ERR_CUDA;                                                             \
+    }                                                                                  \
+  } while (0)
+
+#define NTG_CHECK_ARG(cond, msg)            \
+  do {                                      \
+    if (!(cond)) {                          \
+      ::ntg::set_error("%s", msg);          \
+      return NTG_ERR_INVALID;               \
+    }                                       \
+  } while (0)
+
+#define NTG_TRY(expr)              \
+  do {                             \
+    int _s = (expr);               \
+    if (_s != NTG_OK) return _s;   \
+  } while (0)
+
+template <typename T>
+int dev_alloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return NTG_OK;
+  cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(e));
+    *p = nullptr;
+    return NTG_ERR_ALLOC;
+  }
+  return NTG_OK;
+}
+template <typename T>
+void dev_free(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// Partial-sum slots of the deterministic two-level reductions: each block
+// writes its partial to part[blockIdx.x]; the last block to finish (found
+// with an atomic ticket) sums part[0..gridDim.x) in index order.
+constexpr int kRedSlots = 4096;   // max blocks of a reducing kernel
+constexpr int kRedLanes = 32;     // up to 32 simultaneous sums per kernel
+
+// Device-resident solver scalars (one block per solve, FP64).
+struct Scalars {
+  double rz;       // (r, z) of the current iteration
+  double rz_new;
+  double pap;      // (p, Ap)
+  double alpha, beta;
+  double rr;       // (r, r) mult-weighted
+  double tol2;     // squared stopping threshold
+  double ff;       // (f, f)
+  double rtol, abstol;
+  double pap_prev; // (p_{k-1}, A p_{k-1}) of the flexible CG
+  double gamma;    // flexible-CG orthogonalisation coefficient
+  double rr0;      // (r0, r0) at the start of the solve
+  double red[8];   // scratch results of generic reductions
+  int iter;        // iterations performed
+  int done;        // 1 = converged or stopped: later kernels are no-ops
+  int status;      // NTG_OK / NTG_MAXITER / NTG_BREAKDOWN / NTG_NONFINITE
+  int max_iter;
+  unsigned ticket; // last-block ticket of the reducing kernels
+  unsigned pad;
+};
+
+}  // namespace ntg
+
+// The plan: mesh, coef_t, gs_t, Jacobi.
+struct ntg_plan {
+  int lx = 0;
+  int64_t nelv = 0, n = 0, nu = 0, nshared = 0, nshared_idx = 0;
+  cudaStream_t stream = 0;
+  double D[NTG_LXMAX * NTG_LXMAX];
+  double wq[NTG_LXMAX];
+  float Df[NTG_LXMAX * NTG_LXMAX];
+  // geometry (FP64 + FP32 copies)
+  double* g[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  float* gf[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double* B = nullptr;
+  double* mult = nullptr;
+  float* multf = nullptr;
+  // gather-scatter: full map (perm sorted by global id, offsets) and the
+  // shared-node subset the hot kernels use
+  int32_t* perm = nullptr;
+  int64_t* offs = nullptr;
+  int32_t* sh_idx = nullptr;  // local indices of nodes with > 1 copy, grouped
+  int32_t* sh_off = nullptr;  // nshared + 1 offsets into sh_idx
+  // coefficients
+  int h1_const = 1;
+  double h1c = 1.0;
+  double* h1 = nullptr;   // n (when !h1_const)
+  float* h1f = nullptr;
+  int ifh2 = 0;
+  double* hB = nullptr;   // h2*B (when ifh2)
+  float* hBf = nullptr;
+  // Dirichlet mask (0-based)
+  int32_t* mask = nullptr;
+  int64_t nmask = 0;
+  // Jacobi
+  double* dinv = nullptr;
+  float* dinvf = nullptr;
+  int jacobi_ready = 0;
+  // reductions
+  double* red_part = nullptr;    // kRedSlots * kRedLanes
+  ntg::Scalars* scal = nullptr;  // generic scalars for standalone dots
+  double* host_red = nullptr;    // pinned
+};
+
+namespace ntg {
+// launch helpers implemented in the .cu files
+int ax_launch(ntg_plan* p, double* w, const double* u, Scalars* dot_scal, int dot_slot, cudaStream_t s);
+int ax_launch_f32(ntg_plan* p, float* w, const float* u, Scalars* dot_scal, int dot_slot, cudaStream_t s);
+int gs_launch(ntg_plan* p, double* u, int op, cudaStream_t s);
+int gs_launch_f32(ntg_plan* p, float* u, int op, cudaStream_t s);
+int mask_launch(ntg_plan* p, double* u, cudaStream_t s);
+int mask_launch_f32(ntg_plan* p, float* u, cudaStream_t s);
+// assembled masked operator w = mask(gs(A u)); optional fused (u, Au_local)
+int op_apply(ntg_plan* p, double* w, const double* u, cudaStream_t s);
+int op_apply_f32(ntg_plan* p, float* w, const float* u, cudaStream_t s);
+// generic deterministic weighted dot: sum a*b*c (c may be null -> 1)
+int wdot(ntg_plan* p, const double* a, const double* b, const double* c, int64_t n, double* host_out,
+         cudaStream_t s);
+int gs_add_guarded(ntg_plan* p, double* u, cudaStream_t s, const Scalars* sc);
+int gs_add_guarded_f32(ntg_plan* p, float* u, cudaStream_t s, const Scalars* sc);
+int mask_guarded(ntg_plan* p, double* u, cudaStream_t s, const Scalars* sc);
+int mask_guarded_f32(ntg_plan* p, float* u, cudaStream_t s, const Scalars* sc);
+int ensure_fp32(ntg_plan* p);
+int grid_for(int64_t work, int threads);
+int num_sms();
+}  // namespace ntg

@@ -1,0 +1,682 @@
+// Jacobi preconditioner, Jacobi-PCG (FP64 drop-in), the mixed-precision
+// flexible CG (FP32 inner PCG, FP64 outer residuals and dots), Fischer
+// residual projection, the PDE filter driver and generic dot products.
+//
+// Replaces Neko's pc_t (jacobi), ksp_t (cg) and projection_t, used by the
+// reference at sources/adjoint/adjoint_pnpn.f90:729-741,781-794 and
+// sources/mapping_functions/PDE_filter_mapping.f90:180-184,246-262.
+//
+// Solver state lives on the device (Scalars); every iteration is a fixed
+// sequence of kernels (Ax with the fused (p, Ap) dot, gather-scatter, mask,
+// update with fused (r, z) and (r, r) dots, direction update), each of which
+// returns at once after the device-side convergence flag is set.  The host
+// reads the flag every `check_every` iterations, so the iteration count is
+// exact and no per-iteration host round trip is needed.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "reduce.cuh"
+
+namespace ntg {
+
+// ---------------------------------------------------------------------------
+// Jacobi diagonal of the element operator (see the derivation in the oracle):
+//   sum_l D_li^2 G11(l,j,k) h1 + D_lj^2 G22(i,l,k) h1 + D_lk^2 G33(i,j,l) h1
+//   + 2 h1 (D_ii D_jj G12 + D_ii D_kk G13 + D_jj D_kk G23) + h2 B
+// ---------------------------------------------------------------------------
+struct DBig {
+  double d[NTG_LXMAX * NTG_LXMAX];
+};
+
+__global__ void k_helm_diag(int64_t nelv, int lx, const __grid_constant__ DBig D, const double* __restrict__ g11,
+                            const double* __restrict__ g12, const double* __restrict__ g13,
+                            const double* __restrict__ g22, const double* __restrict__ g23,
+                            const double* __restrict__ g33, const double* __restrict__ h1, double h1c,
+                            const double* __restrict__ hB, double* __restrict__ d) {
+  const int64_t lx3 = (int64_t)lx * lx * lx;
+  const int64_t n = nelv * lx3;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n; m += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = m / lx3;
+    const int r = (int)(m - e * lx3);
+    const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+    const int64_t base = e * lx3;
+    double acc = 0.0;
+    for (int l = 0; l < lx; ++l) {
+      int64_t qr = base + l + lx * (j + lx * k);
+      int64_t qs = base + i + lx * (l + lx * k);
+      int64_t qt = base + i + lx * (j + lx * l);
+      double hr = h1 ? h1[qr] : h1c, hs = h1 ? h1[qs] : h1c, ht = h1 ? h1[qt] : h1c;
+      double a = D.d[l * lx + i], b = D.d[l * lx + j], c = D.d[l * lx + k];
+      acc += a * a * g11[qr] * hr;
+      acc += b * b * g22[qs] * hs;
+      acc += c * c * g33[qt] * ht;
+    }
+    double hm = h1 ? h1[m] : h1c;
+    double di = D.d[i * lx + i], dj = D.d[j * lx + j], dk = D.d[k * lx + k];
+    acc += 2.0 * hm * (di * dj * g12[m] + di * dk * g13[m] + dj * dk * g23[m]);
+    if (hB) acc += hB[m];
+    d[m] = acc;
+  }
+}
+
+__global__ void k_set_masked(double* __restrict__ u, const int32_t* __restrict__ mask, int64_t m, double v) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < m; q += (int64_t)gridDim.x * blockDim.x)
+    u[mask[q]] = v;
+}
+__global__ void k_invert(double* __restrict__ d, float* __restrict__ df, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double v = 1.0 / d[i];
+    d[i] = v;
+    df[i] = (float)v;
+  }
+}
+__global__ void k_col3(double* __restrict__ z, const double* __restrict__ a, const double* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    z[i] = a[i] * b[i];
+}
+
+int jacobi_update(ntg_plan* p) {
+  cudaStream_t s = p->stream;
+  if (!p->dinv) NTG_TRY(dev_alloc(&p->dinv, p->n));
+  if (!p->dinvf) NTG_TRY(dev_alloc(&p->dinvf, p->n));
+  DBig D;
+  memcpy(D.d, p->D, sizeof(double) * p->lx * p->lx);
+  k_helm_diag<<<grid_for(p->n, 256), 256, 0, s>>>(p->nelv, p->lx, D, p->g[0], p->g[1], p->g[2], p->g[3], p->g[4],
+                                                    p->g[5], p->h1_const ? nullptr : p->h1, p->h1c,
+                                                    p->ifh2 ? p->hB : nullptr, p->dinv);
+  NTG_CUDA_TRY(cudaGetLastError());
+  NTG_TRY(gs_launch(p, p->dinv, NTG_GS_ADD, s));
+  if (p->nmask) k_set_masked<<<grid_for(p->nmask, 256), 256, 0, s>>>(p->dinv, p->mask, p->nmask, 1.0);
+  k_invert<<<grid_for(p->n, 256), 256, 0, s>>>(p->dinv, p->dinvf, p->n);
+  NTG_CUDA_TRY(cudaGetLastError());
+  p->jacobi_ready = 1;
+  return NTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Generic reductions
+// ---------------------------------------------------------------------------
+struct FinStore {
+  int slot;
+  __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[slot] = acc[0]; }
+};
+
+__global__ void k_wdot(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                       int64_t n, double* __restrict__ part, Scalars* sc) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += c ? a[i] * b[i] * c[i] : a[i] * b[i];
+  double v[1] = {s};
+  grid_reduce<1>(v, part, sc, FinStore{0});
+}
+
+int wdot(ntg_plan* p, const double* a, const double* b, const double* c, int64_t n, double* host_out,
+         cudaStream_t s) {
+  k_wdot<<<grid_for(n, 256), 256, 0, s>>>(a, b, c, n, p->red_part, p->scal);
+  NTG_CUDA_TRY(cudaGetLastError());
+  NTG_CUDA_TRY(cudaMemcpyAsync(p->host_red, &p->scal->red[0], sizeof(double), cudaMemcpyDeviceToHost, s));
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  *host_out = p->host_red[0];
+  return NTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// PCG kernels (T = double for the FP64 solver, float for the inner solve;
+// reductions always accumulate in FP64).
+// ---------------------------------------------------------------------------
+struct FinInit {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    // acc: ff, rr, rz
+    sc->ff = acc[0];
+    sc->rr = acc[1];
+    sc->rr0 = acc[1];
+    sc->rz = acc[2];
+    double t = sc->rtol * sqrt(acc[0]);
+    if (sc->abstol > t) t = sc->abstol;
+    sc->tol2 = t * t;
+    sc->iter = 0;
+    sc->status = NTG_OK;
+    sc->done = 0;
+    if (!isfinite(acc[0]) || !isfinite(acc[1]) || !isfinite(acc[2])) {
+      sc->status = NTG_NONFINITE;
+      sc->done = 1;
+    } else if (acc[1] <= sc->tol2) {
+      sc->done = 1;
+    } else if (sc->max_iter <= 0) {
+      sc->status = NTG_MAXITER;
+      sc->done = 1;
+    }
+  }
+};
+
+// r = f - w (w == null: r = f); z = dinv r; p = z; sums ff, rr, rz
+template <typename T>
+__global__ void k_cg_init(const T* __restrict__ f, const T* __restrict__ w, const T* __restrict__ dinv,
+                          const T* __restrict__ mult, T* __restrict__ r, T* __restrict__ p, int64_t n,
+                          double* __restrict__ part, Scalars* sc) {
+  double ff = 0, rr = 0, rz = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T fi = f[i];
+    T ri = w ? fi - w[i] : fi;
+    T zi = dinv[i] * ri;
+    r[i] = ri;
+    p[i] = zi;
+    double m = (double)mult[i];
+    ff += m * (double)fi * (double)fi;
+    rr += m * (double)ri * (double)ri;
+    rz += m * (double)ri * (double)zi;
+  }
+  double v[3] = {ff, rr, rz};
+  grid_reduce<3>(v, part, sc, FinInit());
+}
+
+struct FinUpd {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    // acc: rz_new, rr
+    sc->iter += 1;
+    sc->rr = acc[1];
+    if (!isfinite(acc[0]) || !isfinite(acc[1])) {
+      sc->status = NTG_NONFINITE;
+      sc->done = 1;
+      return;
+    }
+    if (acc[1] <= sc->tol2) {
+      sc->done = 1;
+      return;
+    }
+    if (sc->iter >= sc->max_iter) {
+      sc->status = NTG_MAXITER;
+      sc->done = 1;
+      return;
+    }
+    sc->beta = acc[0] / sc->rz;
+    sc->rz = acc[0];
+  }
+};
+
+// x += alpha p; r -= alpha w; sums (r, dinv r), (r, r)
+template <typename T>
+__global__ void k_cg_update(T* __restrict__ x, const T* __restrict__ p, T* __restrict__ r, const T* __restrict__ w,
+                            const T* __restrict__ dinv, const T* __restrict__ mult, int64_t n,
+                            double* __restrict__ part, Scalars* sc) {
+  if (sc->done) return;
+  const T alpha = (T)sc->alpha;
+  double rz = 0, rr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T xi = x[i] + alpha * p[i];
+    T ri = r[i] - alpha * w[i];
+    x[i] = xi;
+    r[i] = ri;
+    double m = (double)mult[i];
+    double rd = (double)ri;
+    rz += m * rd * (double)(dinv[i] * ri);
+    rr += m * rd * rd;
+  }
+  double v[2] = {rz, rr};
+  grid_reduce<2>(v, part, sc, FinUpd());
+}
+
+// p = dinv r + beta p
+template <typename T>
+__global__ void k_cg_dir(T* __restrict__ p, const T* __restrict__ r, const T* __restrict__ dinv, int64_t n,
+                         const Scalars* sc) {
+  if (sc->done) return;
+  const T beta = (T)sc->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = dinv[i] * r[i] + beta * p[i];
+}
+
+template <typename T>
+struct PcgVecs {
+  T *r = nullptr, *p = nullptr, *w = nullptr;
+};
+
+// Runs Jacobi-PCG on x (guess in, solution out) for rhs f.  `zero_guess`
+// skips the initial operator application.  Returns the final host copy of
+// the scalars in *hs.
+template <typename T>
+static int run_pcg(ntg_plan* pl, Scalars* sc, Scalars* hs_pinned, PcgVecs<T>& v, T* x, const T* f,
+                   const T* dinv, const T* mult, double rtol, double abstol, int max_iter, bool zero_guess,
+                   int check_every, cudaStream_t s, int* fp_ax) {
+  const int64_t n = pl->n;
+  const int TPB = 256;
+  const int G = grid_for(n, TPB);
+  // reset the scalar block
+  memset(hs_pinned, 0, sizeof(Scalars));
+  hs_pinned->rtol = rtol;
+  hs_pinned->abstol = abstol;
+  hs_pinned->max_iter = max_iter;
+  NTG_CUDA_TRY(cudaMemcpyAsync(sc, hs_pinned, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+  if (!zero_guess) {
+    if (sizeof(T) == 8) NTG_TRY(op_apply(pl, (double*)v.w, (const double*)x, s));
+    else NTG_TRY(op_apply_f32(pl, (float*)v.w, (const float*)x, s));
+    if (fp_ax && sizeof(T) == 8) (*fp_ax)++;
+  }
+  k_cg_init<T><<<G, TPB, 0, s>>>(f, zero_guess ? nullptr : v.w, dinv, mult, v.r, v.p, n, pl->red_part, sc);
+  NTG_CUDA_TRY(cudaGetLastError());
+  int launched = 0;
+  for (;;) {
+    NTG_CUDA_TRY(cudaMemcpyAsync(hs_pinned, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    NTG_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs_pinned->done) break;
+    if (launched >= max_iter + check_every) break;  // defensive: device cap reached
+    for (int c = 0; c < check_every; ++c) {
+      if (sizeof(T) == 8) {
+        NTG_TRY(ax_launch(pl, (double*)v.w, (const double*)v.p, sc, 0, s));
+        NTG_TRY(gs_add_guarded(pl, (double*)v.w, s, sc));
+        NTG_TRY(mask_guarded(pl, (double*)v.w, s, sc));
+      } else {
+        NTG_TRY(ax_launch_f32(pl, (float*)v.w, (const float*)v.p, sc, 0, s));
+        NTG_TRY(gs_add_guarded_f32(pl, (float*)v.w, s, sc));
+        NTG_TRY(mask_guarded_f32(pl, (float*)v.w, s, sc));
+      }
+      k_cg_update<T><<<G, TPB, 0, s>>>(x, v.p, v.r, v.w, dinv, mult, n, pl->red_part, sc);
+      k_cg_dir<T><<<G, TPB, 0, s>>>(v.p, v.r, dinv, n, sc);
+      NTG_CUDA_TRY(cudaGetLastError());
+      ++launched;
+    }
+  }
+  // each iteration that ran did exactly one FP64 Ax when T == double
+  if (fp_ax && sizeof(T) == 8) *fp_ax += hs_pinned->iter;
+  return NTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision flexible CG kernels
+// ---------------------------------------------------------------------------
+struct FinResid {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    // acc: ff, rr
+    sc->ff = acc[0];
+    sc->rr = acc[1];
+    sc->rr0 = acc[1];
+    double t = sc->rtol * sqrt(acc[0]);
+    if (sc->abstol > t) t = sc->abstol;
+    sc->tol2 = t * t;
+    sc->iter = 0;
+    sc->status = NTG_OK;
+    sc->done = 0;
+    sc->pap_prev = 0.0;
+    if (!isfinite(acc[0]) || !isfinite(acc[1])) {
+      sc->status = NTG_NONFINITE;
+      sc->done = 1;
+    } else if (acc[1] <= sc->tol2) {
+      sc->done = 1;
+    }
+  }
+};
+
+// r = f - w; sums ff, rr
+__global__ void k_resid(const double* __restrict__ f, const double* __restrict__ w, const double* __restrict__ mult,
+                        double* __restrict__ r, int64_t n, double* __restrict__ part, Scalars* sc) {
+  double ff = 0, rr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double fi = f[i];
+    double ri = w ? fi - w[i] : fi;
+    r[i] = ri;
+    ff += mult[i] * fi * fi;
+    rr += mult[i] * ri * ri;
+  }
+  double v[2] = {ff, rr};
+  grid_reduce<2>(v, part, sc, FinResid());
+}
+
+// inner right-hand side: rin = (float)(r / ||r||)
+__global__ void k_to_f32_scaled(const double* __restrict__ r, float* __restrict__ rin, int64_t n, const Scalars* sc) {
+  const double s = 1.0 / sqrt(sc->rr);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    rin[i] = (float)(r[i] * s);
+}
+
+struct FinGamma {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    sc->gamma = sc->pap_prev > 0.0 ? acc[0] / sc->pap_prev : 0.0;
+  }
+};
+// z = ||r|| * (double)din; sums (z, qprev)_mult.  z is continuous and q
+// assembled, so the mult-weighted local sum is the unique-node product.
+__global__ void k_from_f32(const float* __restrict__ din, double* __restrict__ z, const double* __restrict__ qprev,
+                           const double* __restrict__ mult, int64_t n, double* __restrict__ part, Scalars* sc) {
+  const double s = sqrt(sc->rr);
+  double zq = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double zi = s * (double)din[i];
+    z[i] = zi;
+    if (qprev) zq += mult[i] * zi * qprev[i];
+  }
+  double v[1] = {zq};
+  grid_reduce<1>(v, part, sc, FinGamma());
+}
+struct FinPr {
+  __device__ void operator()(const double* acc, Scalars* sc) const { sc->rz = acc[0]; }
+};
+// p = z - gamma pprev; sums (p, r)_mult
+__global__ void k_fcg_orth(double* __restrict__ p, const double* __restrict__ pprev, const double* __restrict__ r,
+                           const double* __restrict__ mult, int64_t n, double* __restrict__ part, Scalars* sc) {
+  const double g = sc->gamma;
+  double pr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double pi = p[i];
+    if (pprev) pi -= g * pprev[i];
+    p[i] = pi;
+    pr += mult[i] * pi * r[i];
+  }
+  double v[1] = {pr};
+  grid_reduce<1>(v, part, sc, FinPr());
+}
+struct FinOuter {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    sc->iter += 1;
+    sc->rr = acc[0];
+    sc->pap_prev = sc->pap;
+    if (!isfinite(acc[0])) {
+      sc->status = NTG_NONFINITE;
+      sc->done = 1;
+    } else if (acc[0] <= sc->tol2) {
+      sc->done = 1;
+    } else if (sc->iter >= sc->max_iter) {
+      sc->status = NTG_MAXITER;
+      sc->done = 1;
+    }
+  }
+};
+// x += alpha p; r -= alpha q; sums (r, r)_mult
+__global__ void k_fcg_update(double* __restrict__ x, const double* __restrict__ p, double* __restrict__ r,
+                             const double* __restrict__ q, const double* __restrict__ mult, int64_t n,
+                             double* __restrict__ part, Scalars* sc) {
+  const double a = sc->alpha;
+  double rr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += a * p[i];
+    double ri = r[i] - a * q[i];
+    r[i] = ri;
+    rr += mult[i] * ri * ri;
+  }
+  double v[1] = {rr};
+  grid_reduce<1>(v, part, sc, FinOuter());
+}
+
+__global__ void k_zero_f(float* __restrict__ a, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = 0.f;
+}
+
+}  // namespace ntg
+
+// ---------------------------------------------------------------------------
+// ksp object
+// ---------------------------------------------------------------------------
+struct ntg_ksp {
+  ntg_plan* plan = nullptr;
+  int type = NTG_KSP_CG;
+  int max_iter = 800;
+  double rtol = 1e-10, abstol = 0.0;
+  double inner_rtol = 1e-4;
+  int inner_max_iter = 400;
+  int check_every = 16;
+  // FP64 workspace
+  ntg::PcgVecs<double> v64;
+  double *pd = nullptr, *qd = nullptr, *pprev = nullptr, *qprev = nullptr;
+  // FP32 workspace
+  ntg::PcgVecs<float> v32;
+  float *rin = nullptr, *din = nullptr;
+  ntg::Scalars* sc = nullptr;      // outer / plain solve
+  ntg::Scalars* sc_in = nullptr;   // inner solve
+  ntg::Scalars* hs = nullptr;      // pinned host mirror (outer)
+  ntg::Scalars* hs_in = nullptr;   // pinned host mirror (inner)
+};
+
+using namespace ntg;
+
+static void ksp_free(ntg_ksp* k) {
+  dev_free(k->v64.r); dev_free(k->v64.p); dev_free(k->v64.w);
+  dev_free(k->pd); dev_free(k->qd); dev_free(k->pprev); dev_free(k->qprev);
+  dev_free(k->v32.r); dev_free(k->v32.p); dev_free(k->v32.w);
+  dev_free(k->rin); dev_free(k->din);
+  dev_free(k->sc); dev_free(k->sc_in);
+  if (k->hs) cudaFreeHost(k->hs);
+  if (k->hs_in) cudaFreeHost(k->hs_in);
+  k->hs = nullptr;
+  k->hs_in = nullptr;
+}
+
+static int ksp_solve_cg(ntg_ksp* k, double* x, const double* f, ntg_monitor* mon) {
+  ntg_plan* p = k->plan;
+  cudaStream_t s = p->stream;
+  if (!p->jacobi_ready) NTG_TRY(jacobi_update(p));
+  // a zero initial guess skips one operator application
+  double xx = 0.0;
+  NTG_TRY(wdot(p, x, x, nullptr, p->n, &xx, s));
+  int fpax = 0;
+  NTG_TRY(run_pcg<double>(p, k->sc, k->hs, k->v64, x, f, p->dinv, p->mult, k->rtol, k->abstol, k->max_iter,
+                          xx == 0.0, k->check_every, s, &fpax));
+  if (mon) {
+    mon->iter = k->hs->iter;
+    mon->inner_iter = 0;
+    mon->res_start = sqrt(k->hs->rr0);
+    mon->res_final = sqrt(k->hs->rr);
+    mon->rhs_norm = sqrt(k->hs->ff);
+    mon->status = k->hs->status;
+    mon->fp64_ax = fpax;
+  }
+  return NTG_OK;
+}
+
+static int ksp_solve_mixed(ntg_ksp* k, double* x, const double* f, ntg_monitor* mon) {
+  ntg_plan* p = k->plan;
+  cudaStream_t s = p->stream;
+  const int64_t n = p->n;
+  const int TPB = 256;
+  const int G = grid_for(n, TPB);
+  NTG_TRY(ensure_fp32(p));
+  if (!p->jacobi_ready) NTG_TRY(jacobi_update(p));
+  double xx = 0.0;
+  NTG_TRY(wdot(p, x, x, nullptr, n, &xx, s));
+  int fpax = 0, inner_total = 0;
+  // outer residual r = f - A x (FP64)
+  Scalars* hs = k->hs;
+  memset(hs, 0, sizeof(Scalars));
+  hs->rtol = k->rtol;
+  hs->abstol = k->abstol;
+  hs->max_iter = k->max_iter;
+  NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+  if (xx != 0.0) {
+    NTG_TRY(op_apply(p, k->qd, x, s));
+    fpax++;
+  }
+  k_resid<<<G, TPB, 0, s>>>(f, xx != 0.0 ? k->qd : nullptr, p->mult, k->v64.r, n, p->red_part, k->sc);
+  NTG_CUDA_TRY(cudaGetLastError());
+  NTG_CUDA_TRY(cudaMemcpyAsync(hs, k->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  const double rr0 = hs->rr0, ff = hs->ff;
+  double* pd = k->pd;
+  double* qd = k->qd;
+  double* pprev = k->pprev;
+  double* qprev = k->qprev;
+  bool have_prev = false;
+  Scalars& hin = *k->hs_in;
+  double last_rr = hs->rr;
+  int stagnant = 0;
+  int outer_status = hs->status;
+  bool fallback = false;
+  while (!hs->done) {
+    // inner FP32 Jacobi-PCG on the normalised residual, zero guess
+    k_to_f32_scaled<<<G, TPB, 0, s>>>(k->v64.r, k->rin, n, k->sc);
+    k_zero_f<<<G, TPB, 0, s>>>(k->din, n);
+    NTG_CUDA_TRY(cudaGetLastError());
+    NTG_TRY(run_pcg<float>(p, k->sc_in, &hin, k->v32, k->din, k->rin, p->dinvf, p->multf, k->inner_rtol, 0.0,
+                           k->inner_max_iter, true, k->check_every, s, nullptr));
+    inner_total += hin.iter;
+    // direction: z = ||r|| din, FCG(1) orthogonalisation against pprev
+    k_from_f32<<<G, TPB, 0, s>>>(k->din, pd, have_prev ? qprev : nullptr, p->mult, n, p->red_part, k->sc);
+    k_fcg_orth<<<G, TPB, 0, s>>>(pd, have_prev ? pprev : nullptr, k->v64.r, p->mult, n, p->red_part, k->sc);
+    // q = A p (FP64) with fused (p, Ap) -> alpha = (p, r) / (p, Ap)
+    NTG_TRY(ax_launch(p, qd, pd, k->sc, 0, s));
+    NTG_TRY(gs_launch(p, qd, NTG_GS_ADD, s));
+    NTG_TRY(mask_launch(p, qd, s));
+    fpax++;
+    k_fcg_update<<<G, TPB, 0, s>>>(x, pd, k->v64.r, qd, p->mult, n, p->red_part, k->sc);
+    NTG_CUDA_TRY(cudaGetLastError());
+    NTG_CUDA_TRY(cudaMemcpyAsync(hs, k->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    NTG_CUDA_TRY(cudaStreamSynchronize(s));
+    // swap direction buffers
+    double* t = pprev; pprev = pd; pd = t;
+    t = qprev; qprev = qd; qd = t;
+    have_prev = true;
+    // stagnation guard: two outer steps that each fail to halve the
+    // residual hand the rest of the solve to the FP64 PCG
+    if (!hs->done) {
+      if (hs->rr > 0.25 * last_rr) ++stagnant;
+      else stagnant = 0;
+      last_rr = hs->rr;
+      if (stagnant >= 2) {
+        fallback = true;
+        break;
+      }
+    }
+  }
+  outer_status = hs->status;
+  int outer_iter = hs->iter;
+  double rr_final = hs->rr;
+  if (fallback) {
+    int fp2 = 0;
+    NTG_TRY(run_pcg<double>(p, k->sc, k->hs, k->v64, x, f, p->dinv, p->mult, k->rtol, k->abstol,
+                            k->max_iter, false, k->check_every, s, &fp2));
+    fpax += fp2;
+    outer_iter += k->hs->iter;
+    rr_final = k->hs->rr;
+    outer_status = k->hs->status;
+  }
+  k->pd = pd; k->qd = qd; k->pprev = pprev; k->qprev = qprev;
+  if (mon) {
+    mon->iter = outer_iter;
+    mon->inner_iter = inner_total;
+    mon->res_start = sqrt(rr0);
+    mon->res_final = sqrt(rr_final);
+    mon->rhs_norm = sqrt(ff);
+    mon->status = outer_status;
+    mon->fp64_ax = fpax;
+  }
+  return NTG_OK;
+}
+
+extern "C" {
+
+int ntg_pc_jacobi_update(ntg_plan* plan) {
+  clear_error();
+  NTG_CHECK_ARG(plan, "ntg_pc_jacobi_update: null plan");
+  return jacobi_update(plan);
+}
+
+int ntg_pc_jacobi_solve(ntg_plan* plan, double* z_d, const double* r_d) {
+  clear_error();
+  NTG_CHECK_ARG(plan && z_d && r_d, "ntg_pc_jacobi_solve: null argument");
+  if (!plan->jacobi_ready) NTG_TRY(jacobi_update(plan));
+  k_col3<<<grid_for(plan->n, 256), 256, 0, plan->stream>>>(z_d, plan->dinv, r_d, plan->n);
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+int ntg_pc_jacobi_get(const ntg_plan* plan, double* dinv_d) {
+  clear_error();
+  NTG_CHECK_ARG(plan && dinv_d, "ntg_pc_jacobi_get: null argument");
+  NTG_CHECK_ARG(plan->jacobi_ready, "ntg_pc_jacobi_get: call ntg_pc_jacobi_update first");
+  NTG_CUDA_TRY(cudaMemcpyAsync(dinv_d, plan->dinv, sizeof(double) * plan->n, cudaMemcpyDeviceToDevice, plan->stream));
+  return NTG_OK;
+}
+
+int ntg_glsc3(ntg_plan* plan, const double* a_d, const double* b_d, const double* c_d, int64_t n, double* out) {
+  clear_error();
+  NTG_CHECK_ARG(plan && a_d && b_d && out && n >= 0, "ntg_glsc3: bad argument");
+  return wdot(plan, a_d, b_d, c_d, n, out, plan->stream);
+}
+
+int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double abstol, ntg_ksp** ksp) {
+  clear_error();
+  NTG_CHECK_ARG(plan && ksp, "ntg_ksp_create: null argument");
+  NTG_CHECK_ARG(type == NTG_KSP_CG || type == NTG_KSP_FCG_MIXED, "ntg_ksp_create: unknown solver type");
+  NTG_CHECK_ARG(max_iter >= 0 && rtol >= 0 && abstol >= 0, "ntg_ksp_create: bad tolerance or iteration cap");
+  *ksp = nullptr;
+  ntg_ksp* k = new ntg_ksp();
+  k->plan = plan;
+  k->type = type;
+  k->max_iter = max_iter;
+  k->rtol = rtol;
+  k->abstol = abstol;
+  const int64_t n = plan->n;
+  int st = NTG_OK;
+  do {
+    if ((st = dev_alloc(&k->v64.r, n))) break;
+    if ((st = dev_alloc(&k->v64.p, n))) break;
+    if ((st = dev_alloc(&k->v64.w, n))) break;
+    if ((st = dev_alloc(&k->sc, 1))) break;
+    if ((st = dev_alloc(&k->sc_in, 1))) break;
+    if (cudaMallocHost(&k->hs, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
+    if (cudaMallocHost(&k->hs_in, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
+    if (cudaMemset(k->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    if (cudaMemset(k->sc_in, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    if (type == NTG_KSP_FCG_MIXED) {
+      if ((st = dev_alloc(&k->pd, n))) break;
+      if ((st = dev_alloc(&k->qd, n))) break;
+      if ((st = dev_alloc(&k->pprev, n))) break;
+      if ((st = dev_alloc(&k->qprev, n))) break;
+      if ((st = dev_alloc(&k->v32.r, n))) break;
+      if ((st = dev_alloc(&k->v32.p, n))) break;
+      if ((st = dev_alloc(&k->v32.w, n))) break;
+      if ((st = dev_alloc(&k->rin, n))) break;
+      if ((st = dev_alloc(&k->din, n))) break;
+    }
+  } while (0);
+  if (st) {
+    ksp_free(k);
+    delete k;
+    return st;
+  }
+  *ksp = k;
+  return NTG_OK;
+}
+
+int ntg_ksp_destroy(ntg_ksp* ksp) {
+  clear_error();
+  if (!ksp) return NTG_OK;
+  cudaStreamSynchronize(ksp->plan->stream);
+  ksp_free(ksp);
+  delete ksp;
+  return NTG_OK;
+}
+
+int ntg_ksp_set_inner(ntg_ksp* ksp, double inner_rtol, int inner_max_iter) {
+  clear_error();
+  NTG_CHECK_ARG(ksp && inner_rtol > 0 && inner_rtol < 1 && inner_max_iter > 0, "ntg_ksp_set_inner: bad argument");
+  ksp->inner_rtol = inner_rtol;
+  ksp->inner_max_iter = inner_max_iter;
+  return NTG_OK;
+}
+
+int ntg_ksp_set_check_every(ntg_ksp* ksp, int every) {
+  clear_error();
+  NTG_CHECK_ARG(ksp && every > 0 && every <= 1024, "ntg_ksp_set_check_every: bad argument");
+  ksp->check_every = every;
+  return NTG_OK;
+}
+
+int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon) {
+  clear_error();
+  NTG_CHECK_ARG(ksp && x_d && f_d, "ntg_ksp_solve: null argument");
+  if (mon) memset(mon, 0, sizeof(*mon));
+  if (ksp->type == NTG_KSP_FCG_MIXED) return ksp_solve_mixed(ksp, x_d, f_d, mon);
+  return ksp_solve_cg(ksp, x_d, f_d, mon);
+}
+
+int ntg_ksp_solve_coupled(ntg_ksp* ksp, double* x_d, double* y_d, double* z_d, const double* fx_d,
+                          const double* fy_d, const double* fz_d, ntg_monitor* mon3) {
+  clear_error();
+  NTG_CHECK_ARG(ksp && x_d && y_d && z_d && fx_d && fy_d && fz_d, "ntg_ksp_solve_coupled: null argument");
+  double* xs[3] = {x_d, y_d, z_d};
+  const double* fs[3] = {fx_d, fy_d, fz_d};
+  for (int c = 0; c < 3; ++c) NTG_TRY(ntg_ksp_solve(ksp, xs[c], fs[c], mon3 ? mon3 + c : nullptr));
+  return NTG_OK;
+}
+
+}  // extern "C"

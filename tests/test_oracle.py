@@ -1,0 +1,193 @@
+"""CPU tests of the oracle (the checker): known answers, an independent
+numpy/scipy assembly, and the coefficient kernels of neko-top.
+
+The reference tree holds no golden vector or test for this path (its only
+tests are MMA toy programs), so the oracle is pinned by known answers and by
+the independent restatement in oracle/numpy_ref.py.
+"""
+import numpy as np
+import pytest
+
+
+def test_gll_basis(orc):
+    from oracle import numpy_ref
+    for lx in (3, 4, 6, 8, 10):
+        xi, w, D = orc.gll(lx)
+        assert abs(w.sum() - 2.0) < 1e-14
+        # D differentiates polynomials of degree <= N exactly
+        for p in range(lx):
+            assert np.allclose(D @ xi ** p, p * xi ** max(p - 1, 0) * (p > 0), atol=1e-11)
+        xi2, w2, D2 = numpy_ref.gll(lx)
+        assert np.allclose(xi, xi2, atol=1e-14) and np.allclose(w, w2, atol=1e-14)
+        assert np.allclose(D, D2, atol=1e-11)
+
+
+def test_mesh_ids_and_shared_coordinates(orc):
+    m = orc.build_mesh(3, 2, 2, 5, amp=0.05, seed=3)
+    N = m.lx - 1
+    assert m.nu == (3 * N + 1) * (2 * N + 1) * (2 * N + 1)
+    # every copy of a global node has identical coordinates (bit for bit)
+    for s in range(m.nu):
+        idx = m.perm[m.offs[s]:m.offs[s + 1]]
+        for arr in (m.x, m.y, m.z):
+            assert np.all(arr[idx] == arr[idx[0]])
+    # multiplicity: gs(1) = copies, sum of mult = unique count
+    ones = orc.gs_op(m, np.ones(m.n))
+    assert np.allclose(ones * m.mult, 1.0)
+    assert abs(m.mult.sum() - m.nu) < 1e-9
+
+
+def test_affine_geometry(orc):
+    m = orc.build_mesh(2, 3, 2, 6, lo=(0, 0, 0), hi=(2.0, 3.0, 1.0))
+    for k in ("g12", "g13", "g23"):
+        assert np.abs(m.G[k]).max() < 1e-13
+    assert abs(m.B.sum() - 6.0) < 1e-12
+    assert np.all(m.jac > 0)
+
+
+def test_deformed_geometry_nonuniform(orc):
+    m = orc.build_mesh(4, 4, 4, 8, amp=0.05, seed=11)
+    assert np.all(m.jac > 0)
+    for k in ("g11", "g12", "g13", "g22", "g23", "g33"):
+        v = m.G[k] / m.B
+        assert np.std(v) > 1e-3 * (np.abs(v).mean() + 1e-3), k
+
+
+def test_ax_constant_null_space_and_symmetry(orc):
+    m = orc.build_mesh(3, 2, 2, 7, amp=0.05, seed=5)
+    w = orc.ax_helm(m, np.ones(m.n))
+    assert np.abs(w).max() < 1e-11 * np.abs(m.G["g11"]).max() * 100
+    rng = np.random.default_rng(1)
+    u = orc.gs_op(m, rng.standard_normal(m.n)) * m.mult  # continuous fields
+    v = orc.gs_op(m, rng.standard_normal(m.n)) * m.mult
+    Au = orc.gs_op(m, orc.ax_helm(m, u))
+    Av = orc.gs_op(m, orc.ax_helm(m, v))
+    a = orc.glsc3(v, Au, m.mult)
+    b = orc.glsc3(u, Av, m.mult)
+    assert abs(a - b) < 1e-12 * max(abs(a), 1.0)
+    assert orc.glsc3(u, Au, m.mult) > 0
+
+
+def test_exact_weak_forms(orc):
+    # affine unit cube: sum_l u_l (A u)_l = int |grad u|^2, and the mass term
+    m = orc.build_mesh(2, 2, 2, 8)
+    u = m.x ** 2
+    assert abs(np.dot(u, orc.ax_helm(m, u)) - 4.0 / 3.0) < 1e-12
+    u = m.x + 2 * m.y + 3 * m.z
+    assert abs(np.dot(u, orc.ax_helm(m, u)) - 14.0) < 1e-11
+    u = m.x ** 2
+    w = orc.ax_helm(m, u, h1c=0.0, h2=np.ones(m.n))
+    assert abs(np.dot(u, w) - 0.2) < 1e-13
+
+
+def test_against_scipy_assembly(orc):
+    from oracle import numpy_ref
+    m = orc.build_mesh(2, 2, 1, 4, amp=0.05, seed=9)
+    rng = np.random.default_rng(2)
+    h2 = orc.field_uniform(m, 4, 2, 0.5, 2.0)
+    A, uidx = numpy_ref.assembled_operator(m.x, m.y, m.z, m.gid, m.lx, h2)
+    ug = rng.standard_normal(A.shape[0])
+    u = ug[uidx]
+    w = orc.gs_op(m, orc.ax_helm(m, u, h2=h2))
+    wg = A @ ug
+    assert np.allclose(w, wg[uidx], rtol=1e-11, atol=1e-11 * np.abs(wg).max())
+    # gs maps sorted by global id, stable
+    uniq = np.unique(m.gid)
+    assert len(uniq) == m.nu
+    for s in range(m.nu):
+        idx = m.perm[m.offs[s]:m.offs[s + 1]]
+        assert np.all(m.gid[idx] == uniq[s]) and np.all(np.diff(idx) > 0)
+    # Jacobi diagonal equals the assembled matrix diagonal
+    d = 1.0 / orc.jacobi(m, h2=h2)
+    assert np.allclose(d, A.diagonal()[uidx], rtol=1e-11)
+
+
+def test_cg_against_direct_solve(orc):
+    import scipy.sparse.linalg as spla
+    from oracle import numpy_ref
+    m = orc.build_mesh(2, 2, 2, 5, amp=0.05, seed=13)
+    mask = orc.mask_face_xmax(2, 2, 2, 5)
+    A, uidx = numpy_ref.assembled_operator(m.x, m.y, m.z, m.gid, m.lx)
+    rng = np.random.default_rng(3)
+    f = orc.assemble_rhs(m, rng.uniform(-1, 1, m.n), mask)
+    x, it, r0, r1 = orc.cg(m, f, mask=mask, rtol=1e-12)
+    assert r1 <= 1e-12 * r0 * 1.0001
+    # direct solve with Dirichlet rows removed
+    dir_u = np.unique(uidx[mask - 1])
+    free = np.setdiff1d(np.arange(A.shape[0]), dir_u)
+    fg = np.zeros(A.shape[0])
+    fg[uidx] = f
+    xg = np.zeros(A.shape[0])
+    xg[free] = spla.spsolve(A[free][:, free].tocsc(), fg[free])
+    assert np.linalg.norm(x - xg[uidx]) <= 1e-9 * np.linalg.norm(xg)
+
+
+def test_ramp_derivatives(orc):
+    x = np.linspace(0.01, 0.99, 101)
+    h = 1e-6
+    for up, q in ((0, 8.0), (0, 1.0), (1, 1.0), (1, 8.0)):
+        d = orc.ramp_backward(x, np.ones_like(x), 0.0, 1e4, q, up)
+        fd = (orc.ramp_forward(x + h, 0.0, 1e4, q, up) - orc.ramp_forward(x - h, 0.0, 1e4, q, up)) / (2 * h)
+        if up and q != 1.0:
+            # RAMP_mapping.f90:250-267 writes d/dx = (fmax-fmin)(q+1)/(x+q)^2,
+            # which is the true derivative divided by q; exact for the
+            # default q = 1.  The restatement keeps the reference's formula.
+            assert np.allclose(d * q, fd, rtol=1e-6)
+        else:
+            assert np.allclose(d, fd, rtol=1e-6)
+    # BASELINE chi(rho) = chimax (1-rho)/(1+q rho) is the convex-down map at 1-rho
+    rho = np.linspace(0, 1, 11)
+    chi = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
+    assert np.allclose(chi, 1e4 * (1 - rho) / (1 + 8 * rho))
+
+
+def test_masked_ops(orc):
+    rng = np.random.default_rng(4)
+    a, b, c = (rng.uniform(1, 2, 50) for _ in range(3))
+    mask = np.array([1, 5, 9, 50, 17], dtype=np.int32)
+    mi = mask - 1
+    r = orc.masked("cadd_mask", a, 2.5, mask, len(mask)); e = a.copy(); e[mi] += 2.5; assert np.array_equal(r, e)
+    r = orc.masked("invcol1_mask", a, mask, len(mask)); e = a.copy(); e[mi] = 1 / e[mi]; assert np.array_equal(r, e)
+    r = orc.masked("cmult_mask", a, 3.0, mask, len(mask)); e = a.copy(); e[mi] *= 3; assert np.array_equal(r, e)
+    r = orc.masked("col2_mask", a, b, mask, len(mask)); e = a.copy(); e[mi] *= b[mi]; assert np.array_equal(r, e)
+    r = orc.masked("col3_mask", a, b, c, mask, len(mask)); e = a.copy(); e[mi] = b[mi] * c[mi]; assert np.array_equal(r, e)
+    r = orc.masked("sub3_mask", a, b, c, mask, len(mask)); e = a.copy(); e[mi] = b[mi] - c[mi]; assert np.array_equal(r, e)
+    assert abs(orc.glsc2_mask(a, b, mask) - np.dot(a[mi], b[mi])) < 1e-13
+
+
+def test_brinkman_permeability_sensitivity(orc):
+    rng = np.random.default_rng(5)
+    n = 40
+    fx, fy, fz, u, v, w, chi = (rng.standard_normal(n) for _ in range(7))
+    gx, gy, gz = orc.brinkman(fx, fy, fz, u, v, w, chi)
+    assert np.allclose(gx, fx - u * chi) and np.allclose(gz, fz - w * chi)
+    phi = rng.uniform(0, 1, n)
+    k = orc.permeability(phi, 1e5, 0.0, 1.0)
+    assert np.allclose(k, -(0.0 + (1e5 - 0.0) * 2.0 * phi / (1.0 + phi)))
+    ua, va, wa = (rng.standard_normal(n) for _ in range(3))
+    s = orc.sens_min_dissipation(u, v, w, ua, va, wa, True, 0.5)
+    assert np.allclose(s, -(u * ua + v * va + w * wa) + 0.5 * (u * u + v * v + w * w))
+
+
+def test_projection_reproduces_solution(orc):
+    m = orc.build_mesh(2, 2, 2, 5, amp=0.05, seed=21)
+    mask = orc.mask_face_xmax(2, 2, 2, 5)
+    rng = np.random.default_rng(6)
+    P = orc.Projection(m.n, 4)
+    base = orc.assemble_rhs(m, rng.uniform(-1, 1, m.n), mask)
+    its = []
+    for k in range(6):
+        f = base + 0.05 * k * orc.assemble_rhs(m, rng.uniform(-1, 1, m.n), mask)
+        x_ref, _, _, _ = orc.cg(m, f, mask=mask, rtol=1e-12)
+        b = f.copy()
+        P.pre(b, m.mult)
+        dx, it, _, _ = orc.cg(m, b, mask=mask, rtol=1e-12 * np.linalg.norm(f) / max(np.linalg.norm(b), 1e-300))
+        adx = orc.op_apply(m, dx, mask=mask)
+        x = P.post(dx, adx, m.mult)
+        its.append(it)
+        assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+    # the basis is A-orthonormal
+    mm = P.m
+    Gm = np.array([[orc.glsc3(P.xs[i], P.axs[j], m.mult) for j in range(mm)] for i in range(mm)])
+    assert np.allclose(Gm, np.eye(mm), atol=1e-8)
+    assert its[-1] < its[0]
