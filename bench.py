@@ -1,0 +1,456 @@
+#!/usr/bin/env python
+"""Benchmark: time to a 1e-10 relative residual for the SEM pressure-Poisson
+solve on one GB300, learned-free mixed precision (FP32 inner Jacobi-PCG in an
+FP64 flexible CG) against the plain FP64 Jacobi-PCG drop-in, plus the Ax
+GDOF/s of both precisions.
+
+Workload (default, --config c2): 32^3 hex elements, N = 7 (16.8M local
+DOFs), box deformed by a seeded sinusoid of amplitude 0.05 h per axis,
+pressure-Poisson (h1 = 1, h2 = 0) with a Dirichlet face at x = 1, RHS the weak
+form of 16 seeded Fourier modes with amplitudes ~ |k|^-2.  Inputs are
+synthetic (seeded generators in the library) and larger than L2.
+
+One step = one full solve from a zero initial guess, RHS resident in HBM.
+`e2e` repeats the step through the public API with the RHS copied from pinned
+host memory and the solution copied back inside the timed region.
+
+--impl reference times the reference algorithm's CPU implementation (the C
+oracle: FP64 Jacobi-PCG, matrix-free sum factorisation, OpenMP) on the host
+cores, each step a bounded sample of CG iterations scaled to a full solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Poisson solve time to 1e-10 & Ax GDOF/s: learned+FP32 vs plain FP64, 1 GB300"
+
+CONFIGS = {
+    "c1": dict(E=(8, 8, 8), amp=0.0, case="brinkman_uniform", dirichlet=False,
+               desc="8^3 affine unit cube, N=7, h1=1, h2=chi(rho) RAMP q=8 chimax=1e4, rho~U[0,1], "
+                    "zero-mean uniform RHS, Jacobi-PCG to 1e-10 rel"),
+    "c2": dict(E=(32, 32, 32), amp=0.05, case="poisson_fourier", dirichlet=True,
+               desc="32^3 deformed hex (0.05h sinusoid), N=7, pressure-Poisson h1=1 h2=0, Dirichlet x=1, "
+                    "16 Fourier modes ~|k|^-2, solve to 1e-10 rel"),
+    "c3": dict(E=(32, 32, 32), amp=0.05, case="brinkman_blobs", dirichlet=True,
+               desc="32^3 deformed hex, N=7, Brinkman Helmholtz h1=1/Re=0.01, h2=chi(12 Gaussian blobs), "
+                    "Dirichlet x=1, 16 Fourier modes, solve to 1e-10 rel"),
+    "c5": dict(E=(64, 64, 64), amp=0.05, case="poisson_fourier", dirichlet=True,
+               desc="64^3 deformed hex, N=7 (134M local DOFs), pressure-Poisson, Dirichlet x=1, "
+                    "16 Fourier modes, solve to 1e-10 rel"),
+}
+LX = 8
+MESH_SEED, RHS_SEED, RHO_SEED = 1, 2, 3
+RTOL = 1e-10
+
+
+# ---------------------------------------------------------------------------
+# helpers shared by both arms
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(value: float, ws: int) -> float:
+    """Maximum of a per-rank float (time) over all ranks; identity at 1 rank."""
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def setup_gpu_case(pkg, cfg, dev):
+    import torch
+    ex, ey, ez = cfg["E"]
+    coef = pkg.coef_t.box(ex, ey, ez, LX, amp=cfg["amp"], seed=MESH_SEED, device=dev)
+    ncoef = 0
+    if cfg["dirichlet"]:
+        coef.set_mask(pkg.mask_face_xmax(ex, ey, ez, LX, device=dev), base=1)
+    if cfg["case"] == "poisson_fourier":
+        coef.set_coefs(h1c=1.0, ifh2=False)
+        f = coef.rhs_assemble(coef.field_fourier(16, RHS_SEED))
+    elif cfg["case"] == "brinkman_blobs":
+        rho = coef.field_blobs(RHO_SEED, 12, 0.1)
+        chi = torch.empty_like(rho)
+        pkg.RAMP_mapping_t(0.0, 1e4, 8.0, False).apply_forward(chi, 1.0 - rho)
+        coef.set_coefs(h1c=0.01, h2=chi, ifh2=True)
+        ncoef = 1
+        f = coef.rhs_assemble(coef.field_fourier(16, RHS_SEED))
+    else:  # brinkman_uniform
+        rho = coef.field_uniform(RHO_SEED, 2, 0.0, 1.0)
+        chi = torch.empty_like(rho)
+        pkg.RAMP_mapping_t(0.0, 1e4, 8.0, False).apply_forward(chi, 1.0 - rho)
+        coef.set_coefs(h1c=1.0, h2=chi, ifh2=True)
+        ncoef = 1
+        b = coef.field_uniform(RHS_SEED, 3, -1.0, 1.0)
+        g = coef.geometry()
+        b = b - (b * g["mult"]).sum() / coef.nu
+        f = b
+    torch.cuda.synchronize()
+    return coef, f, ncoef
+
+
+def time_solves(ksp, x, f, k, ev):
+    import torch
+    mons = []
+    e0, e1 = ev(), ev()
+    e0.record()
+    for _ in range(k):
+        x.zero_()
+        mons.append(ksp.solve(x, f))
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, mons
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    L = pkg.lib()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = CONFIGS[args.config]
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    t_setup = time.time()
+    coef, f, ncoef = setup_gpu_case(pkg, cfg, dev)
+    n = coef.n
+    ksp_mx = pkg.krylov_solver_factory(coef, "fcg_mixed", 200, RTOL)
+    ksp_mx.set_inner(args.inner_rtol, args.inner_max)
+    ksp64 = pkg.krylov_solver_factory(coef, "cg", 20000, RTOL)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    t_setup = time.time() - t_setup
+
+    # warm-up, then the timed steps (inputs > L2: FP32 G alone is 24 B/DOF)
+    for _ in range(args.warmup):
+        x.zero_()
+        ksp_mx.solve(x, f)
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = int(L.ntg_launch_count())
+    with ClockSampler(dev.index if dev.index is not None else 0) as clk:
+        t_mx, mons = time_solves(ksp_mx, x, f, args.steps, ev)
+    launches = int(L.ntg_launch_count()) - l0
+    barrier(ws)
+    t_mx = max_over_ranks(t_mx, ws)
+    x_mx = x.clone()
+    for m in mons:
+        assert m.status == pkg.NTG_OK and m.res_final <= RTOL * m.rhs_norm * (1 + 1e-9), m
+
+    # the plain FP64 drop-in on the same GPU
+    x.zero_()
+    ksp64.solve(x, f)  # warm-up
+    t64, mons64 = time_solves(ksp64, x, f, args.fp64_steps, ev)
+    x64 = x.clone()
+    err_vs_fp64 = float(torch.linalg.norm(x_mx - x64) / torch.linalg.norm(x64))
+
+    # Ax alone, both precisions
+    def time_ax(dtype, reps=20):
+        u = torch.randn(n, dtype=dtype, device=dev)
+        w = torch.empty_like(u)
+        ax = pkg.ax_helm_t()
+        for _ in range(3):
+            ax.compute(w, u, coef)
+        a, b = ev(), ev()
+        a.record()
+        for _ in range(reps):
+            ax.compute(w, u, coef)
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / reps
+    t_ax64, t_ax32 = time_ax(torch.float64), time_ax(torch.float32)
+
+    # live per-kernel device times inside one profiled solve
+    L.ntg_timer_reset()
+    L.ntg_timer_enable(1)
+    x.zero_()
+    ksp_mx.solve(x, f)
+    torch.cuda.synchronize()
+    L.ntg_timer_enable(0)
+    import ctypes as C
+    names = {0: "ax_fp64", 1: "ax_fp32", 2: "gs_fp64", 3: "gs_fp32", 4: "cg_update_fp64", 5: "cg_update_fp32",
+             6: "cg_dir_fp64", 7: "cg_dir_fp32"}
+    ktimes = {}
+    for i, nm in names.items():
+        ms, cnt = C.c_double(), C.c_longlong()
+        L.ntg_timer_read(i, C.byref(ms), C.byref(cnt))
+        if cnt.value:
+            ktimes[nm] = {"total_ms": round(ms.value, 4), "launches": cnt.value,
+                          "avg_us": round(ms.value / cnt.value * 1e3, 2)}
+    tot = sum(v["total_ms"] for v in ktimes.values()) or 1.0
+    for v in ktimes.values():
+        v["share"] = round(v["total_ms"] / tot, 4)
+
+    # roofline of the dominant kernel (FP32 Ax, HBM bound):
+    # algorithmic bytes per local DOF = (u in + w out + 6 G + ncoef) * 4 B
+    pk, pk_kind = peaks()
+    ax32 = ktimes.get("ax_fp32")
+    bytes_per_dof = (2 + 6 + ncoef) * 4
+    t_launch = ax32["avg_us"] * 1e-6 if ax32 else t_ax32
+    achieved = bytes_per_dof * n / t_launch / 1e9
+    roof = {"kernel": "k_ax_helm<float,8> (FP32 Ax inside the timed solve)", "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / pk["hbm_gbs"], 4), "peak_source": pk_kind,
+            "bytes_per_dof": bytes_per_dof, "traffic": args.traffic}
+
+    # end to end through the public API: host RHS in, host solution out
+    f_h = f.cpu().pin_memory()
+    x_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    f_d = torch.empty_like(f)
+    e0, e1 = ev(), ev()
+    barrier(ws)
+    torch.cuda.synchronize()
+    w0 = time.time()
+    e0.record()
+    for _ in range(args.steps):
+        f_d.copy_(f_h, non_blocking=True)
+        x.zero_()
+        ksp_mx.solve(x, f_d)
+        x_h.copy_(x, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws)
+    w_e2e = time.time() - w0
+
+    mx_outer = statistics.mean(m.iter for m in mons)
+    mx_inner = statistics.mean(m.inner_iter for m in mons)
+    out = {
+        "metric": METRIC,
+        "value": round(ws * args.steps / t_mx, 4),
+        "unit": "solves/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t_mx / args.steps * 1e3, 3),
+        "s_per_solve": round(t_mx / args.steps, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 inner / f64 outer",
+        "data": "synthetic (seeded generators; no dataset)",
+        "config": {"workload": f"{args.config}: {cfg['desc']}", "n_local_dofs": n, "n_unique_dofs": coef.nu,
+                   "method": f"fcg_mixed (inner Jacobi-PCG FP32 to {args.inner_rtol:g}, outer FCG(1) FP64)",
+                   "l2": "inputs larger than L2 (FP64 G 805 MB, FP32 G 403 MB at c2)",
+                   "parallelism": "replicas only" if ws > 1 else "1 GPU"},
+        "iterations": {"outer_mean": mx_outer, "inner_mean": mx_inner,
+                       "fp64_ax_per_solve": mons[-1].fp64_ax},
+        "fp64_dropin": {"s_per_solve": round(t64 / args.fp64_steps, 5), "iters": mons64[-1].iter,
+                        "status": mons64[-1].status},
+        "speedup_vs_fp64_dropin": round((t64 / args.fp64_steps) / (t_mx / args.steps), 3),
+        "error_vs_fp64_solution": err_vs_fp64,
+        "ax_gdof_s": {"fp64": round(n / t_ax64 / 1e9, 3), "fp32": round(n / t_ax32 / 1e9, 3)},
+        "roofline": roof,
+        "kernels_in_one_solve": ktimes,
+        "e2e": {"value": round(ws * args.steps / t_e2e, 4), "unit": "solves/s",
+                "h2d_bytes_per_step": int(f_h.numel() * 8), "d2h_bytes_per_step": int(x_h.numel() * 8),
+                "wall_s": round(w_e2e, 4)},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "setup_s": round(t_setup, 3),
+    }
+    # CPU baseline: the oracle on this host, rank 0 at N=1 only
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_sample(cfg, args.cpu_iters, mons64[-1].iter)
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU (reference algorithm) arm
+# ---------------------------------------------------------------------------
+def setup_cpu_case(cfg):
+    import numpy as np
+    from oracle import oracle as orc
+    orc.build()
+    ex, ey, ez = cfg["E"]
+    m = orc.build_mesh(ex, ey, ez, LX, amp=cfg["amp"], seed=MESH_SEED)
+    mask = orc.mask_face_xmax(ex, ey, ez, LX) if cfg["dirichlet"] else None
+    h1c, h2 = 1.0, None
+    if cfg["case"] == "poisson_fourier":
+        k, a, ph = orc.fourier_params(RHS_SEED, 16)
+        f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+    elif cfg["case"] == "brinkman_blobs":
+        rho = orc.field_blobs(m, RHO_SEED, 12, 0.1)
+        h2 = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
+        h1c = 0.01
+        k, a, ph = orc.fourier_params(RHS_SEED, 16)
+        f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+    else:
+        rho = orc.field_uniform(m, RHO_SEED, 2, 0.0, 1.0)
+        h2 = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
+        b = orc.field_uniform(m, RHS_SEED, 3, -1.0, 1.0)
+        f = b - np.sum(b * m.mult) / m.nu
+    dinv = orc.jacobi(m, h1c=h1c, h2=h2, mask=mask)
+    return orc, m, mask, h1c, h2, f, dinv
+
+
+def cpu_sample(cfg, iters, solve_iters):
+    orc, m, mask, h1c, h2, f, dinv = setup_cpu_case(cfg)
+    t_it = orc.cg_time_per_iter(m, f, iters, h1c=h1c, h2=h2, mask=mask, dinv=dinv)
+    s_solve = t_it * solve_iters
+    return {"value": round(1.0 / s_solve, 5), "unit": "solves/s", "cores": orc.num_threads(), "kind": "port",
+            "s_per_solve": round(s_solve, 3), "s_per_iter": round(t_it, 5),
+            "sample": f"{iters} FP64 Jacobi-PCG iterations of the same case on {orc.num_threads()} host threads, "
+                      f"scaled by the {solve_iters} iterations of the FP64 solve to 1e-10"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    cfg = CONFIGS[args.config]
+    t0 = time.time()
+    orc, m, mask, h1c, h2, f, dinv = setup_cpu_case(cfg)
+    t_setup = time.time() - t0
+    # warm-up 1: one full solve to 1e-10 gives the iteration count
+    t0 = time.time()
+    _, iters, r0, r1 = orc.cg(m, f, h1c=h1c, h2=h2, mask=mask, dinv=dinv, rtol=RTOL, max_iter=20000)
+    t_full = time.time() - t0
+    for _ in range(max(args.warmup - 1, 0)):
+        orc.cg_time_per_iter(m, f, 2, h1c=h1c, h2=h2, mask=mask, dinv=dinv)
+    samples = []
+    for _ in range(args.steps):
+        samples.append(orc.cg_time_per_iter(m, f, args.cpu_iters, h1c=h1c, h2=h2, mask=mask, dinv=dinv))
+    t_it = statistics.median(samples)
+    s_solve = t_it * iters
+    val = round(1.0 / s_solve, 5)
+    cores = orc.num_threads()
+    sample = (f"each step: {args.cpu_iters} FP64 Jacobi-PCG iterations of the {args.config} case on {cores} host "
+              f"threads, scaled by the {iters} iterations of a full solve to 1e-10 (timed once: {t_full:.2f} s)")
+    return {
+        "metric": METRIC, "impl": "reference", "value": val, "unit": "solves/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(s_solve * 1e3, 3),
+        "s_per_solve": round(s_solve, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded generators; no dataset)",
+        "config": {"workload": f"{args.config}: {cfg['desc']}", "n_local_dofs": m.n, "n_unique_dofs": m.nu,
+                   "method": "FP64 Jacobi-PCG, matrix-free sum factorisation (C oracle, OpenMP)"},
+        "iterations": iters, "full_solve_s": round(t_full, 3), "setup_s": round(t_setup, 3),
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    p.add_argument("--inner-rtol", type=float, default=1e-4)
+    p.add_argument("--inner-max", type=int, default=2000)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--cpu-iters", type=int, default=20)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--traffic", type=float, default=None,
+                   help="dram bytes per FP32 Ax launch from an ncu capture (reported as roofline.traffic)")
+    args = p.parse_args(argv)
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        res = run_reference(args, ws, rank)
+        if res is not None:
+            print(json.dumps(res), flush=True)
+        return 0
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    res = run_ours(args, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -84,6 +84,15 @@ const char* ntg_version(void);
 const char* ntg_last_error(void);
 /* compiled polynomial orders: writes up to cap values of lx, returns count */
 int ntg_supported_lx(int* lx, int cap);
+/* kernels the library has launched in this process (all entry points) */
+unsigned long long ntg_launch_count(void);
+/* per-kernel device timers (CUDA events around each launch, on the
+   launching stream; the stand-in for Neko's profiler regions).  Ids: 0 FP64
+   Ax, 1 FP32 Ax, 2 FP64 gs, 3 FP32 gs, 4/5 CG update FP64/FP32, 6/7 CG
+   direction FP64/FP32.  Off by default. */
+int ntg_timer_enable(int on);
+int ntg_timer_read(int id, double* total_ms, long long* count);
+int ntg_timer_reset(void);
 
 /* ---------------------------------------------------------------------- */
 /* mesh / coef_t / gs_t plan                                               */
@@ -128,6 +137,19 @@ int ntg_mesh_box(int ex, int ey, int ez, int lx, const double* lo3, const double
 /* 1-based local indices of the x = hi face (nmask = ex*ey*ez/ex * lx^2
    entries when mask_d != NULL).  Returns the count in *nmask. */
 int ntg_mask_face_xmax(int ex, int ey, int ez, int lx, int32_t* mask_d, int64_t* nmask, void* stream);
+/* seeded synthetic fields (SplitMix64 keyed by (seed, stream_id, global id)):
+   uniform in [lo, hi) per global node */
+int ntg_field_uniform(const int64_t* gid_d, int64_t n, uint64_t seed, uint64_t stream_id, double lo, double hi,
+                      double* f_d, void* stream);
+/* sum of nmodes Fourier modes cos(2 pi k.X + phi) with amplitudes
+   U[-1,1]/|k|^2, k in [1,kmax]^3, X the coordinates normalised by the box */
+int ntg_field_fourier(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
+                      const double* hi3, int nmodes, int kmax, uint64_t seed, double* f_d, void* stream);
+/* clip(sum of nblobs Gaussians of the given width, 0, 1), centres U(box) */
+int ntg_field_blobs(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
+                    const double* hi3, uint64_t seed, int nblobs, double width, double* f_d, void* stream);
+/* weak right-hand side b = mask(gs(B f)) */
+int ntg_rhs_assemble(ntg_plan* plan, const double* f_d, double* b_d);
 
 /* ---------------------------------------------------------------------- */
 /* ax_t (ax_helm): w = h1 (D^T G D) u + h2 B u, element-local.            */

@@ -38,6 +38,10 @@ SIGNATURES = {
     "ntg_version": (C.c_char_p, []),
     "ntg_last_error": (C.c_char_p, []),
     "ntg_supported_lx": (_i, [_pi, _i]),
+    "ntg_launch_count": (C.c_ulonglong, []),
+    "ntg_timer_enable": (_i, [_i]),
+    "ntg_timer_read": (_i, [_i, _pd, C.POINTER(C.c_longlong)]),
+    "ntg_timer_reset": (_i, []),
     "ntg_plan_create": (_i, [C.POINTER(_vp), _i64, _i, _vp, _vp, _vp, _vp]),
     "ntg_plan_destroy": (_i, [_vp]),
     "ntg_plan_set_stream": (_i, [_vp, _vp]),
@@ -48,6 +52,10 @@ SIGNATURES = {
     "ntg_gs_export": (_i, [_vp, _vp, _vp]),
     "ntg_mesh_box": (_i, [_i, _i, _i, _i, _pd, _pd, _d, C.c_uint64, _vp, _vp, _vp, _vp, _vp]),
     "ntg_mask_face_xmax": (_i, [_i, _i, _i, _i, _vp, _pi64, _vp]),
+    "ntg_field_uniform": (_i, [_vp, _i64, C.c_uint64, C.c_uint64, _d, _d, _vp, _vp]),
+    "ntg_field_fourier": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, _i, _i, C.c_uint64, _vp, _vp]),
+    "ntg_field_blobs": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, C.c_uint64, _i, _d, _vp, _vp]),
+    "ntg_rhs_assemble": (_i, [_vp, _vp, _vp]),
     "ntg_ax_helm": (_i, [_vp, _vp, _vp]),
     "ntg_ax_helm_f32": (_i, [_vp, _vp, _vp]),
     "ntg_gs_op": (_i, [_vp, _vp, _i]),

@@ -129,6 +129,33 @@ class coef_t:
         torch.cuda.synchronize()
         return out
 
+    # seeded synthetic fields on this mesh (the box keeps x, y, z, gid)
+    def field_uniform(self, seed, stream_id, lo, hi):
+        f = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        check(lib().ntg_field_uniform(_ptr(self.gid, torch.int64), self.n, int(seed), int(stream_id), float(lo),
+                                      float(hi), _ptr(f), _stream()))
+        return f
+
+    def field_fourier(self, nmodes, seed, kmax=4):
+        f = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        lo3, hi3 = (C.c_double * 3)(*self.lo), (C.c_double * 3)(*self.hi)
+        check(lib().ntg_field_fourier(_ptr(self.x), _ptr(self.y), _ptr(self.z), self.n, lo3, hi3, int(nmodes),
+                                      int(kmax), int(seed), _ptr(f), _stream()))
+        return f
+
+    def field_blobs(self, seed, nblobs=12, width=0.1):
+        f = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        lo3, hi3 = (C.c_double * 3)(*self.lo), (C.c_double * 3)(*self.hi)
+        check(lib().ntg_field_blobs(_ptr(self.x), _ptr(self.y), _ptr(self.z), self.n, lo3, hi3, int(seed),
+                                    int(nblobs), float(width), _ptr(f), _stream()))
+        return f
+
+    def rhs_assemble(self, f):
+        """b = mask(gs(B f)): the weak right-hand side of a source f."""
+        b = torch.empty_like(f)
+        check(lib().ntg_rhs_assemble(self.handle, _ptr(f, n=self.n), _ptr(b, n=self.n)))
+        return b
+
     def gs_maps(self):
         perm = torch.empty(self.n, dtype=torch.int32, device=self.device)
         offs = torch.empty(self.nu + 1, dtype=torch.int64, device=self.device)

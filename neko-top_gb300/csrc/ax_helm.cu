@@ -152,8 +152,8 @@ static int launch_lx(ntg_plan* p, T* w, const T* u, const T* const* g, const T* 
   const bool h1arr = h1 != nullptr, h2 = hB != nullptr;
 #define NTG_AX_CASE(H1A, HH2, DT)                                                                              \
   if (h1arr == H1A && h2 == HH2 && (sc != nullptr) == DT) {                                                 \
-    k_ax_helm<T, LX, H1A, HH2, DT><<<grid, NT, 0, s>>>(w, u, g[0], g[1], g[2], g[3], g[4], g[5], h1, h1c, \
-                                                            hB, p->nelv, Dp, p->red_part, sc);              \
+    { k_ax_helm<T, LX, H1A, HH2, DT><<<grid, NT, 0, s>>>(w, u, g[0], g[1], g[2], g[3], g[4], g[5], h1, h1c, \
+                                                            hB, p->nelv, Dp, p->red_part, sc); NTG_COUNT_LAUNCH(); }              \
   }
   NTG_AX_CASE(false, false, false)
   NTG_AX_CASE(false, true, false)
@@ -187,15 +187,21 @@ static int ax_dispatch(ntg_plan* p, T* w, const T* u, const T* const* g, const T
 
 int ax_launch(ntg_plan* p, double* w, const double* u, Scalars* dot_scal, int, cudaStream_t s) {
   const double* g[6] = {p->g[0], p->g[1], p->g[2], p->g[3], p->g[4], p->g[5]};
-  return ax_dispatch<double>(p, w, u, g, p->h1_const ? nullptr : p->h1, p->h1c, p->ifh2 ? p->hB : nullptr,
-                             dot_scal, s);
+  timer_start(TM_AX64, s);
+  int st = ax_dispatch<double>(p, w, u, g, p->h1_const ? nullptr : p->h1, p->h1c, p->ifh2 ? p->hB : nullptr,
+                               dot_scal, s);
+  timer_stop(TM_AX64, s);
+  return st;
 }
 
 int ax_launch_f32(ntg_plan* p, float* w, const float* u, Scalars* dot_scal, int, cudaStream_t s) {
   NTG_TRY(ensure_fp32(p));
   const float* g[6] = {p->gf[0], p->gf[1], p->gf[2], p->gf[3], p->gf[4], p->gf[5]};
-  return ax_dispatch<float>(p, w, u, g, p->h1_const ? nullptr : p->h1f, (float)p->h1c,
-                            p->ifh2 ? p->hBf : nullptr, dot_scal, s);
+  timer_start(TM_AX32, s);
+  int st = ax_dispatch<float>(p, w, u, g, p->h1_const ? nullptr : p->h1f, (float)p->h1c,
+                              p->ifh2 ? p->hBf : nullptr, dot_scal, s);
+  timer_stop(TM_AX32, s);
+  return st;
 }
 
 }  // namespace ntg

@@ -129,6 +129,20 @@ struct ntg_plan {
 };
 
 namespace ntg {
+// Every kernel launch of the library bumps this counter (read through
+// ntg_launch_count); it is how callers count the library's launches.
+void count_launch();
+#define NTG_COUNT_LAUNCH() ::ntg::count_launch()
+
+// Optional per-kernel device timers (CUDA events on the launching stream),
+// off by default; enabled with ntg_timer_enable.
+enum TimerId {
+  TM_AX64 = 0, TM_AX32 = 1, TM_GS64 = 2, TM_GS32 = 3, TM_UPD64 = 4, TM_UPD32 = 5, TM_DIR64 = 6,
+  TM_DIR32 = 7, TM_COUNT = 16
+};
+void timer_start(int id, cudaStream_t s);
+void timer_stop(int id, cudaStream_t s);
+
 // launch helpers implemented in the .cu files
 int ax_launch(ntg_plan* p, double* w, const double* u, Scalars* dot_scal, int dot_slot, cudaStream_t s);
 int ax_launch_f32(ntg_plan* p, float* w, const float* u, Scalars* dot_scal, int dot_slot, cudaStream_t s);

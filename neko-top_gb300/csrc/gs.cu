@@ -46,11 +46,18 @@ static int gs_any(ntg_plan* p, T* u, int op, cudaStream_t s, const Scalars* sc) 
   if (p->nshared == 0) return NTG_OK;
   const int TPB = 256;
   const int G = grid_for(p->nshared, TPB);
+  const int tid = sizeof(T) == 8 ? TM_GS64 : TM_GS32;
+  timer_start(tid, s);
+  struct Stop {
+    int id;
+    cudaStream_t s;
+    ~Stop() { timer_stop(id, s); }
+  } stop_{tid, s};
   switch (op) {
-    case NTG_GS_ADD: k_gs_shared<T, NTG_GS_ADD><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); break;
-    case NTG_GS_MUL: k_gs_shared<T, NTG_GS_MUL><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); break;
-    case NTG_GS_MIN: k_gs_shared<T, NTG_GS_MIN><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); break;
-    case NTG_GS_MAX: k_gs_shared<T, NTG_GS_MAX><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); break;
+    case NTG_GS_ADD: { k_gs_shared<T, NTG_GS_ADD><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); NTG_COUNT_LAUNCH(); } break;
+    case NTG_GS_MUL: { k_gs_shared<T, NTG_GS_MUL><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); NTG_COUNT_LAUNCH(); } break;
+    case NTG_GS_MIN: { k_gs_shared<T, NTG_GS_MIN><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); NTG_COUNT_LAUNCH(); } break;
+    case NTG_GS_MAX: { k_gs_shared<T, NTG_GS_MAX><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); NTG_COUNT_LAUNCH(); } break;
     default: set_error("gs_op: unknown op %d", op); return NTG_ERR_INVALID;
   }
   NTG_CUDA_TRY(cudaGetLastError());
@@ -69,7 +76,7 @@ int gs_add_guarded_f32(ntg_plan* p, float* u, cudaStream_t s, const Scalars* sc)
 template <typename T>
 static int mask_any(ntg_plan* p, T* u, cudaStream_t s, const Scalars* sc) {
   if (p->nmask == 0) return NTG_OK;
-  k_mask_zero<T><<<grid_for(p->nmask, 256), 256, 0, s>>>(u, p->mask, p->nmask, sc);
+  { k_mask_zero<T><<<grid_for(p->nmask, 256), 256, 0, s>>>(u, p->mask, p->nmask, sc); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }

@@ -83,13 +83,13 @@ int jacobi_update(ntg_plan* p) {
   if (!p->dinvf) NTG_TRY(dev_alloc(&p->dinvf, p->n));
   DBig D;
   memcpy(D.d, p->D, sizeof(double) * p->lx * p->lx);
-  k_helm_diag<<<grid_for(p->n, 256), 256, 0, s>>>(p->nelv, p->lx, D, p->g[0], p->g[1], p->g[2], p->g[3], p->g[4],
+  { k_helm_diag<<<grid_for(p->n, 256), 256, 0, s>>>(p->nelv, p->lx, D, p->g[0], p->g[1], p->g[2], p->g[3], p->g[4],
                                                     p->g[5], p->h1_const ? nullptr : p->h1, p->h1c,
-                                                    p->ifh2 ? p->hB : nullptr, p->dinv);
+                                                    p->ifh2 ? p->hB : nullptr, p->dinv); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   NTG_TRY(gs_launch(p, p->dinv, NTG_GS_ADD, s));
-  if (p->nmask) k_set_masked<<<grid_for(p->nmask, 256), 256, 0, s>>>(p->dinv, p->mask, p->nmask, 1.0);
-  k_invert<<<grid_for(p->n, 256), 256, 0, s>>>(p->dinv, p->dinvf, p->n);
+  if (p->nmask) { k_set_masked<<<grid_for(p->nmask, 256), 256, 0, s>>>(p->dinv, p->mask, p->nmask, 1.0); NTG_COUNT_LAUNCH(); }
+  { k_invert<<<grid_for(p->n, 256), 256, 0, s>>>(p->dinv, p->dinvf, p->n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   p->jacobi_ready = 1;
   return NTG_OK;
@@ -114,7 +114,7 @@ __global__ void k_wdot(const double* __restrict__ a, const double* __restrict__ 
 
 int wdot(ntg_plan* p, const double* a, const double* b, const double* c, int64_t n, double* host_out,
          cudaStream_t s) {
-  k_wdot<<<grid_for(n, 256), 256, 0, s>>>(a, b, c, n, p->red_part, p->scal);
+  { k_wdot<<<grid_for(n, 256), 256, 0, s>>>(a, b, c, n, p->red_part, p->scal); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   NTG_CUDA_TRY(cudaMemcpyAsync(p->host_red, &p->scal->red[0], sizeof(double), cudaMemcpyDeviceToHost, s));
   NTG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -254,7 +254,7 @@ static int run_pcg(ntg_plan* pl, Scalars* sc, Scalars* hs_pinned, PcgVecs<T>& v,
     else NTG_TRY(op_apply_f32(pl, (float*)v.w, (const float*)x, s));
     if (fp_ax && sizeof(T) == 8) (*fp_ax)++;
   }
-  k_cg_init<T><<<G, TPB, 0, s>>>(f, zero_guess ? nullptr : v.w, dinv, mult, v.r, v.p, n, pl->red_part, sc);
+  { k_cg_init<T><<<G, TPB, 0, s>>>(f, zero_guess ? nullptr : v.w, dinv, mult, v.r, v.p, n, pl->red_part, sc); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   int launched = 0;
   for (;;) {
@@ -272,8 +272,12 @@ static int run_pcg(ntg_plan* pl, Scalars* sc, Scalars* hs_pinned, PcgVecs<T>& v,
         NTG_TRY(gs_add_guarded_f32(pl, (float*)v.w, s, sc));
         NTG_TRY(mask_guarded_f32(pl, (float*)v.w, s, sc));
       }
-      k_cg_update<T><<<G, TPB, 0, s>>>(x, v.p, v.r, v.w, dinv, mult, n, pl->red_part, sc);
-      k_cg_dir<T><<<G, TPB, 0, s>>>(v.p, v.r, dinv, n, sc);
+      timer_start(sizeof(T) == 8 ? TM_UPD64 : TM_UPD32, s);
+      { k_cg_update<T><<<G, TPB, 0, s>>>(x, v.p, v.r, v.w, dinv, mult, n, pl->red_part, sc); NTG_COUNT_LAUNCH(); }
+      timer_stop(sizeof(T) == 8 ? TM_UPD64 : TM_UPD32, s);
+      timer_start(sizeof(T) == 8 ? TM_DIR64 : TM_DIR32, s);
+      { k_cg_dir<T><<<G, TPB, 0, s>>>(v.p, v.r, dinv, n, sc); NTG_COUNT_LAUNCH(); }
+      timer_stop(sizeof(T) == 8 ? TM_DIR64 : TM_DIR32, s);
       NTG_CUDA_TRY(cudaGetLastError());
       ++launched;
     }
@@ -485,7 +489,7 @@ static int ksp_solve_mixed(ntg_ksp* k, double* x, const double* f, ntg_monitor* 
     NTG_TRY(op_apply(p, k->qd, x, s));
     fpax++;
   }
-  k_resid<<<G, TPB, 0, s>>>(f, xx != 0.0 ? k->qd : nullptr, p->mult, k->v64.r, n, p->red_part, k->sc);
+  { k_resid<<<G, TPB, 0, s>>>(f, xx != 0.0 ? k->qd : nullptr, p->mult, k->v64.r, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   NTG_CUDA_TRY(cudaMemcpyAsync(hs, k->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
   NTG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -502,21 +506,21 @@ static int ksp_solve_mixed(ntg_ksp* k, double* x, const double* f, ntg_monitor* 
   bool fallback = false;
   while (!hs->done) {
     // inner FP32 Jacobi-PCG on the normalised residual, zero guess
-    k_to_f32_scaled<<<G, TPB, 0, s>>>(k->v64.r, k->rin, n, k->sc);
-    k_zero_f<<<G, TPB, 0, s>>>(k->din, n);
+    { k_to_f32_scaled<<<G, TPB, 0, s>>>(k->v64.r, k->rin, n, k->sc); NTG_COUNT_LAUNCH(); }
+    { k_zero_f<<<G, TPB, 0, s>>>(k->din, n); NTG_COUNT_LAUNCH(); }
     NTG_CUDA_TRY(cudaGetLastError());
     NTG_TRY(run_pcg<float>(p, k->sc_in, &hin, k->v32, k->din, k->rin, p->dinvf, p->multf, k->inner_rtol, 0.0,
                            k->inner_max_iter, true, k->check_every, s, nullptr));
     inner_total += hin.iter;
     // direction: z = ||r|| din, FCG(1) orthogonalisation against pprev
-    k_from_f32<<<G, TPB, 0, s>>>(k->din, pd, have_prev ? qprev : nullptr, p->mult, n, p->red_part, k->sc);
-    k_fcg_orth<<<G, TPB, 0, s>>>(pd, have_prev ? pprev : nullptr, k->v64.r, p->mult, n, p->red_part, k->sc);
+    { k_from_f32<<<G, TPB, 0, s>>>(k->din, pd, have_prev ? qprev : nullptr, p->mult, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+    { k_fcg_orth<<<G, TPB, 0, s>>>(pd, have_prev ? pprev : nullptr, k->v64.r, p->mult, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
     // q = A p (FP64) with fused (p, Ap) -> alpha = (p, r) / (p, Ap)
     NTG_TRY(ax_launch(p, qd, pd, k->sc, 0, s));
     NTG_TRY(gs_launch(p, qd, NTG_GS_ADD, s));
     NTG_TRY(mask_launch(p, qd, s));
     fpax++;
-    k_fcg_update<<<G, TPB, 0, s>>>(x, pd, k->v64.r, qd, p->mult, n, p->red_part, k->sc);
+    { k_fcg_update<<<G, TPB, 0, s>>>(x, pd, k->v64.r, qd, p->mult, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
     NTG_CUDA_TRY(cudaGetLastError());
     NTG_CUDA_TRY(cudaMemcpyAsync(hs, k->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
     NTG_CUDA_TRY(cudaStreamSynchronize(s));
@@ -573,7 +577,7 @@ int ntg_pc_jacobi_solve(ntg_plan* plan, double* z_d, const double* r_d) {
   clear_error();
   NTG_CHECK_ARG(plan && z_d && r_d, "ntg_pc_jacobi_solve: null argument");
   if (!plan->jacobi_ready) NTG_TRY(jacobi_update(plan));
-  k_col3<<<grid_for(plan->n, 256), 256, 0, plan->stream>>>(z_d, plan->dinv, r_d, plan->n);
+  { k_col3<<<grid_for(plan->n, 256), 256, 0, plan->stream>>>(z_d, plan->dinv, r_d, plan->n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }

@@ -162,44 +162,44 @@ void cuda_cadd_mask(void* a, double* c, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return;
-  k_cadd_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, *c, mask, *mask_size);
+  { k_cadd_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, *c, mask, *mask_size); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_cadd_mask");
 }
 void cuda_invcol1_mask(void* a, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return;
-  k_invcol1_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, mask, *mask_size);
+  { k_invcol1_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, mask, *mask_size); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_invcol1_mask");
 }
 void cuda_cmult_mask(void* a, double* c, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return;
-  k_cmult_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, *c, mask, *mask_size);
+  { k_cmult_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, *c, mask, *mask_size); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_cmult_mask");
 }
 void cuda_col2_mask(void* a, void* b, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return;
-  k_col2_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, (const double*)b, mask, *mask_size);
+  { k_col2_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, (const double*)b, mask, *mask_size); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_col2_mask");
 }
 void cuda_col3_mask(void* a, void* b, void* c, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return;
-  k_col3_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, (const double*)b, (const double*)c, mask,
-                                                          *mask_size);
+  { k_col3_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, (const double*)b, (const double*)c, mask,
+                                                          *mask_size); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_col3_mask");
 }
 void cuda_sub3_mask(void* a, void* b, void* c, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return;
-  k_sub3_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, (const double*)b, (const double*)c, mask,
-                                                          *mask_size);
+  { k_sub3_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((double*)a, (const double*)b, (const double*)c, mask,
+                                                          *mask_size); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_sub3_mask");
 }
 double cuda_glsc2_mask(void* a, void* b, int* size, int* mask, int* mask_size) {
@@ -207,8 +207,8 @@ double cuda_glsc2_mask(void* a, void* b, int* size, int* mask, int* mask_size) {
   (void)size;
   if (*mask_size <= 0) return 0.0;
   if (ensure_glsc_scratch() != NTG_OK) return NAN;
-  k_glsc2_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((const double*)a, (const double*)b, mask, *mask_size,
-                                                           g_part, g_scal);
+  { k_glsc2_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((const double*)a, (const double*)b, mask, *mask_size,
+                                                           g_part, g_scal); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_glsc2_mask");
   cudaMemcpyAsync(g_host, &g_scal->red[0], sizeof(double), cudaMemcpyDeviceToHost, g_glb_queue);
   if (cudaStreamSynchronize(g_glb_queue) != cudaSuccess) {
@@ -223,7 +223,7 @@ int ntg_ramp_forward(double* xout_d, const double* xin_d, int64_t n, double fmin
   clear_error();
   NTG_CHECK_ARG(xout_d && xin_d && n >= 0, "ntg_ramp_forward: bad argument");
   if (n == 0) return NTG_OK;
-  k_ramp_fwd<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(xout_d, xin_d, n, fmin, fmax, q, convex_up);
+  { k_ramp_fwd<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(xout_d, xin_d, n, fmin, fmax, q, convex_up); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -233,7 +233,7 @@ int ntg_ramp_backward(double* dF_din_d, const double* dF_dout_d, const double* x
   clear_error();
   NTG_CHECK_ARG(dF_din_d && dF_dout_d && xin_d && n >= 0, "ntg_ramp_backward: bad argument");
   if (n == 0) return NTG_OK;
-  k_ramp_bwd<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(dF_din_d, dF_dout_d, xin_d, n, fmin, fmax, q, convex_up);
+  { k_ramp_bwd<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(dF_din_d, dF_dout_d, xin_d, n, fmin, fmax, q, convex_up); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -246,10 +246,10 @@ int ntg_brinkman_compute(double* fx_d, double* fy_d, double* fz_d, const double*
   cudaStream_t s = (cudaStream_t)stream;
   if (mask_d) {
     if (nmask <= 0) return NTG_OK;
-    k_brinkman_mask<<<grid1(nmask), 256, 0, s>>>(fx_d, fy_d, fz_d, u_d, v_d, w_d, chi_d, mask_d, nmask, base);
+    { k_brinkman_mask<<<grid1(nmask), 256, 0, s>>>(fx_d, fy_d, fz_d, u_d, v_d, w_d, chi_d, mask_d, nmask, base); NTG_COUNT_LAUNCH(); }
   } else {
     if (n == 0) return NTG_OK;
-    k_brinkman<<<grid1(n), 256, 0, s>>>(fx_d, fy_d, fz_d, u_d, v_d, w_d, chi_d, n);
+    { k_brinkman<<<grid1(n), 256, 0, s>>>(fx_d, fy_d, fz_d, u_d, v_d, w_d, chi_d, n); NTG_COUNT_LAUNCH(); }
   }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
@@ -261,7 +261,7 @@ int ntg_permeability(double* kappa_d, const double* phi_d, int64_t n, double per
   NTG_CHECK_ARG(kappa_d && phi_d && n >= 0, "ntg_permeability: bad argument");
   if (n == 0) return NTG_OK;
   double c = (perm0 - perm1) * (penalty + 1.0);
-  k_permeability<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(kappa_d, phi_d, n, c, perm1, penalty);
+  { k_permeability<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(kappa_d, phi_d, n, c, perm1, penalty); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -272,7 +272,7 @@ int ntg_sens_min_dissipation(double* s_d, const double* u_d, const double* v_d, 
   clear_error();
   NTG_CHECK_ARG(s_d && u_d && v_d && w_d && ua_d && va_d && wa_d && n >= 0, "ntg_sens_min_dissipation: bad argument");
   if (n == 0) return NTG_OK;
-  k_sens_md<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(s_d, u_d, v_d, w_d, ua_d, va_d, wa_d, n, if_lube, K_scale);
+  { k_sens_md<<<grid1(n), 256, 0, (cudaStream_t)stream>>>(s_d, u_d, v_d, w_d, ua_d, va_d, wa_d, n, if_lube, K_scale); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }

@@ -9,6 +9,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -26,6 +28,58 @@ void set_error(const char* fmt, ...) {
 }
 void clear_error() { g_err.clear(); }
 const char* last_error() { return g_err.c_str(); }
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// Device timers: one open (start) event per id; stopped pairs wait in a
+// list until ntg_timer_read resolves them.
+struct TimerState {
+  bool enabled = false;
+  cudaEvent_t open[TM_COUNT] = {};
+  struct Pair { int id; cudaEvent_t a, b; };
+  std::vector<Pair> pending;
+  std::vector<cudaEvent_t> pool;
+  double total_ms[TM_COUNT] = {};
+  long long count[TM_COUNT] = {};
+  std::mutex mu;
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+};
+static TimerState g_tm;
+
+void timer_start(int id, cudaStream_t s) {
+  if (!g_tm.enabled || id < 0 || id >= TM_COUNT) return;
+  std::lock_guard<std::mutex> lk(g_tm.mu);
+  if (!g_tm.open[id]) g_tm.open[id] = g_tm.get();
+  cudaEventRecord(g_tm.open[id], s);
+}
+void timer_stop(int id, cudaStream_t s) {
+  if (!g_tm.enabled || id < 0 || id >= TM_COUNT) return;
+  std::lock_guard<std::mutex> lk(g_tm.mu);
+  if (!g_tm.open[id]) return;
+  cudaEvent_t b = g_tm.get();
+  cudaEventRecord(b, s);
+  g_tm.pending.push_back({id, g_tm.open[id], b});
+  g_tm.open[id] = nullptr;
+}
+static void timer_resolve() {
+  for (auto& p : g_tm.pending) {
+    float ms = 0.f;
+    cudaEventSynchronize(p.b);
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      g_tm.total_ms[p.id] += ms;
+      g_tm.count[p.id] += 1;
+    }
+    g_tm.pool.push_back(p.a);
+    g_tm.pool.push_back(p.b);
+  }
+  g_tm.pending.clear();
+}
 
 int num_sms() {
   static int sms = 0;
@@ -278,10 +332,10 @@ int ensure_fp32(ntg_plan* p) {
   int G = grid_for(p->n, T);
   for (int a = 0; a < 6; ++a) {
     NTG_TRY(dev_alloc(&p->gf[a], p->n));
-    k_d2f<<<G, T, 0, p->stream>>>(p->g[a], p->gf[a], p->n);
+    { k_d2f<<<G, T, 0, p->stream>>>(p->g[a], p->gf[a], p->n); NTG_COUNT_LAUNCH(); }
   }
   NTG_TRY(dev_alloc(&p->multf, p->n));
-  k_d2f<<<G, T, 0, p->stream>>>(p->mult, p->multf, p->n);
+  { k_d2f<<<G, T, 0, p->stream>>>(p->mult, p->multf, p->n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -339,8 +393,8 @@ static int build_gs(ntg_plan* p, const int64_t* glb) {
   GS_ALLOC(pos, n);
   GS_ALLOC(offs_tmp, n + 1);
   GS_ALLOC(d_num, 1);
-  k_iota<<<G, T, 0, s>>>(vals, n);
-  k_iota64<<<G, T, 0, s>>>(pos, n);
+  { k_iota<<<G, T, 0, s>>>(vals, n); NTG_COUNT_LAUNCH(); }
+  { k_iota64<<<G, T, 0, s>>>(pos, n); NTG_COUNT_LAUNCH(); }
   // stable radix sort of (global id, local index)
   cub::DeviceRadixSort::SortPairs(nullptr, need, glb, keys_sorted, vals, p->perm, n, 0, end_bit, s);
   tmp_bytes = need;
@@ -348,7 +402,7 @@ static int build_gs(ntg_plan* p, const int64_t* glb) {
   if (need > tmp_bytes) tmp_bytes = need;
   if (cudaMalloc(&tmp, tmp_bytes) != cudaSuccess) { st = NTG_ERR_ALLOC; set_error("gs tmp alloc"); goto done; }
   cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, glb, keys_sorted, vals, p->perm, n, 0, end_bit, s);
-  k_head_flags<<<G, T, 0, s>>>(keys_sorted, n, flag);
+  { k_head_flags<<<G, T, 0, s>>>(keys_sorted, n, flag); NTG_COUNT_LAUNCH(); }
   cub::DeviceSelect::Flagged(tmp, tmp_bytes, pos, flag, offs_tmp, d_num, n, s);
   if (cudaMemcpyAsync(&nu, d_num, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess) {
@@ -361,7 +415,7 @@ static int build_gs(ntg_plan* p, const int64_t* glb) {
   GS_ALLOC(p->mult, n);
   GS_ALLOC(cnt, nu);
   GS_ALLOC(shflag, nu);
-  k_seg_info<<<grid_for(nu, T), T, 0, s>>>(p->offs, nu, p->perm, p->mult, cnt, shflag);
+  { k_seg_info<<<grid_for(nu, T), T, 0, s>>>(p->offs, nu, p->perm, p->mult, cnt, shflag); NTG_COUNT_LAUNCH(); }
   // shared segments: starts and counts
   GS_ALLOC(sh_start, nu);
   GS_ALLOC(sh_cnt, nu + 1);
@@ -395,7 +449,7 @@ static int build_gs(ntg_plan* p, const int64_t* glb) {
     GS_ALLOC(p->sh_off, nsh + 1);
     cudaMemcpyAsync(p->sh_off, sh_cnt, sizeof(int32_t) * (nsh + 1), cudaMemcpyDeviceToDevice, s);
     GS_ALLOC(p->sh_idx, total > 0 ? total : 1);
-    if (nsh > 0) k_fill_shared<<<grid_for(nsh, T), T, 0, s>>>(sh_start, p->sh_off, nsh, p->perm, p->sh_idx);
+    if (nsh > 0) { k_fill_shared<<<grid_for(nsh, T), T, 0, s>>>(sh_start, p->sh_off, nsh, p->perm, p->sh_idx); NTG_COUNT_LAUNCH(); }
   }
   if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
     st = NTG_ERR_CUDA;
@@ -417,6 +471,34 @@ extern "C" {
 
 const char* ntg_version(void) { return "ntgb300 0.1 (sm_103a)"; }
 const char* ntg_last_error(void) { return ntg::last_error(); }
+
+unsigned long long ntg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int ntg_timer_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_tm.mu);
+  g_tm.enabled = on != 0;
+  return NTG_OK;
+}
+
+int ntg_timer_read(int id, double* total_ms, long long* count) {
+  clear_error();
+  NTG_CHECK_ARG(id >= 0 && id < TM_COUNT && total_ms && count, "ntg_timer_read: bad argument");
+  std::lock_guard<std::mutex> lk(g_tm.mu);
+  timer_resolve();
+  *total_ms = g_tm.total_ms[id];
+  *count = g_tm.count[id];
+  return NTG_OK;
+}
+
+int ntg_timer_reset(void) {
+  std::lock_guard<std::mutex> lk(g_tm.mu);
+  timer_resolve();
+  for (int i = 0; i < TM_COUNT; ++i) {
+    g_tm.total_ms[i] = 0.0;
+    g_tm.count[i] = 0;
+  }
+  return NTG_OK;
+}
 
 int ntg_supported_lx(int* lx, int cap) {
   static const int L[] = {2, 3, 4, 5, 6, 7, 8, 9, 10};
@@ -447,7 +529,7 @@ int ntg_mesh_box(int ex, int ey, int ez, int lx, const double* lo3, const double
   df.h[2] = (hi3[2] - lo3[2]) / ez;
   df.amp = amp;
   int64_t n = (int64_t)ex * ey * ez * lx * lx * lx;
-  k_mesh_box<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(ex, ey, ez, lx, bs, df, x_d, y_d, z_d, glb_d);
+  { k_mesh_box<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(ex, ey, ez, lx, bs, df, x_d, y_d, z_d, glb_d); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -458,7 +540,7 @@ int ntg_mask_face_xmax(int ex, int ey, int ez, int lx, int32_t* mask_d, int64_t*
   int64_t total = (int64_t)ey * ez * lx * lx;
   *nmask = total;
   if (mask_d) {
-    k_mask_face_xmax<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(ex, ey, ez, lx, mask_d);
+    { k_mask_face_xmax<<<grid_for(total, 256), 256, 0, (cudaStream_t)stream>>>(ex, ey, ez, lx, mask_d); NTG_COUNT_LAUNCH(); }
     NTG_CUDA_TRY(cudaGetLastError());
   }
   return NTG_OK;
@@ -490,8 +572,8 @@ int ntg_plan_create(ntg_plan** plan, int64_t nelv, int lx, const double* x_d, co
     if ((st = dev_alloc(&p->scal, 1))) break;
     if (cudaMemset(p->scal, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMallocHost(&p->host_red, sizeof(double) * 16) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
-    k_geom<<<grid_for(p->n, 128), 128, 0, p->stream>>>(nelv, lx, bs, x_d, y_d, z_d, p->g[0], p->g[1], p->g[2],
-                                                        p->g[3], p->g[4], p->g[5], p->B);
+    { k_geom<<<grid_for(p->n, 128), 128, 0, p->stream>>>(nelv, lx, bs, x_d, y_d, z_d, p->g[0], p->g[1], p->g[2],
+                                                        p->g[3], p->g[4], p->g[5], p->B); NTG_COUNT_LAUNCH(); }
     if (cudaGetLastError() != cudaSuccess) { st = NTG_ERR_CUDA; set_error("k_geom launch failed"); break; }
     if ((st = build_gs(p, glb_d))) break;
   } while (0);
@@ -559,7 +641,7 @@ int ntg_coef_set(ntg_plan* p, const double* h1_d, double h1c, const double* h2_d
     if (!p->h1) NTG_TRY(dev_alloc(&p->h1, p->n));
     if (!p->h1f) NTG_TRY(dev_alloc(&p->h1f, p->n));
     NTG_CUDA_TRY(cudaMemcpyAsync(p->h1, h1_d, sizeof(double) * p->n, cudaMemcpyDeviceToDevice, p->stream));
-    k_d2f<<<G, T, 0, p->stream>>>(p->h1, p->h1f, p->n);
+    { k_d2f<<<G, T, 0, p->stream>>>(p->h1, p->h1f, p->n); NTG_COUNT_LAUNCH(); }
     p->h1_const = 0;
   } else {
     p->h1_const = 1;
@@ -569,8 +651,8 @@ int ntg_coef_set(ntg_plan* p, const double* h1_d, double h1c, const double* h2_d
   if (p->ifh2) {
     if (!p->hB) NTG_TRY(dev_alloc(&p->hB, p->n));
     if (!p->hBf) NTG_TRY(dev_alloc(&p->hBf, p->n));
-    k_mul<<<G, T, 0, p->stream>>>(h2_d, p->B, p->hB, h2c, p->n);
-    k_d2f<<<G, T, 0, p->stream>>>(p->hB, p->hBf, p->n);
+    { k_mul<<<G, T, 0, p->stream>>>(h2_d, p->B, p->hB, h2c, p->n); NTG_COUNT_LAUNCH(); }
+    { k_d2f<<<G, T, 0, p->stream>>>(p->hB, p->hBf, p->n); NTG_COUNT_LAUNCH(); }
   }
   p->jacobi_ready = 0;
   NTG_CUDA_TRY(cudaGetLastError());
@@ -589,7 +671,7 @@ int ntg_plan_set_mask(ntg_plan* p, const int32_t* mask_d, int64_t nmask, int bas
   int* bad = nullptr;
   NTG_TRY(dev_alloc(&bad, 1));
   cudaMemsetAsync(bad, 0, sizeof(int), p->stream);
-  k_copy_mask<<<grid_for(nmask, 256), 256, 0, p->stream>>>(mask_d, p->mask, nmask, base, p->n, bad);
+  { k_copy_mask<<<grid_for(nmask, 256), 256, 0, p->stream>>>(mask_d, p->mask, nmask, base, p->n, bad); NTG_COUNT_LAUNCH(); }
   int hbad = 0;
   cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, p->stream);
   cudaError_t e = cudaStreamSynchronize(p->stream);

@@ -110,9 +110,9 @@ int multidot(ntg_plan* p, const double* a, const double* base, int m, double* ou
   if (m <= 0) return NTG_OK;
   const int T = 256;
   int G = grid_for(p->n, T);
-  if (m <= 8) k_multidot<8><<<G, T, 0, s>>>(a, base, m, p->n, p->mult, p->red_part, sc, out_d);
-  else if (m <= 16) k_multidot<16><<<G, T, 0, s>>>(a, base, m, p->n, p->mult, p->red_part, sc, out_d);
-  else k_multidot<32><<<G, T, 0, s>>>(a, base, m, p->n, p->mult, p->red_part, sc, out_d);
+  if (m <= 8) { k_multidot<8><<<G, T, 0, s>>>(a, base, m, p->n, p->mult, p->red_part, sc, out_d); NTG_COUNT_LAUNCH(); }
+  else if (m <= 16) { k_multidot<16><<<G, T, 0, s>>>(a, base, m, p->n, p->mult, p->red_part, sc, out_d); NTG_COUNT_LAUNCH(); }
+  else { k_multidot<32><<<G, T, 0, s>>>(a, base, m, p->n, p->mult, p->red_part, sc, out_d); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -194,7 +194,7 @@ int ntg_proj_pre_solving(ntg_proj* q, double* b_d) {
   const int G = grid_for(n, 256);
   if (q->m > 0) {
     NTG_TRY(multidot(p, b_d, q->xs, q->m, q->coef, q->sc, s));
-    k_proj_pre<<<G, 256, 0, s>>>(q->xbar, q->axbar, b_d, q->xs, q->axs, q->coef, q->m, n);
+    { k_proj_pre<<<G, 256, 0, s>>>(q->xbar, q->axbar, b_d, q->xs, q->axs, q->coef, q->m, n); NTG_COUNT_LAUNCH(); }
     NTG_CUDA_TRY(cudaGetLastError());
   } else {
     NTG_CUDA_TRY(cudaMemsetAsync(q->xbar, 0, sizeof(double) * n, s));
@@ -216,13 +216,13 @@ int ntg_proj_post_solving(ntg_proj* q, double* x_d) {
   NTG_TRY(op_apply(p, q->adx, x_d, s));
   if (q->m >= q->L) {
     // restart from the full solution x = xbar + dx, A x = A xbar + A dx
-    k_sum3<<<G, 256, 0, s>>>(q->xs, q->xbar, x_d, n);
-    k_sum3<<<G, 256, 0, s>>>(q->axs, q->axbar, q->adx, n);
+    { k_sum3<<<G, 256, 0, s>>>(q->xs, q->xbar, x_d, n); NTG_COUNT_LAUNCH(); }
+    { k_sum3<<<G, 256, 0, s>>>(q->axs, q->axbar, q->adx, n); NTG_COUNT_LAUNCH(); }
     NTG_TRY(multidot(p, q->xs, q->axs, 1, q->coef + kProjMax, q->sc, s));
     NTG_CUDA_TRY(cudaMemcpyAsync(q->hcoef, q->coef + kProjMax, sizeof(double), cudaMemcpyDeviceToHost, s));
     NTG_CUDA_TRY(cudaStreamSynchronize(s));
     if (q->hcoef[0] > 0.0 && std::isfinite(q->hcoef[0])) {
-      k_scale2<<<G, 256, 0, s>>>(q->xs, q->axs, q->coef + kProjMax, n);
+      { k_scale2<<<G, 256, 0, s>>>(q->xs, q->axs, q->coef + kProjMax, n); NTG_COUNT_LAUNCH(); }
       q->m = 1;
     } else {
       q->m = 0;
@@ -234,18 +234,18 @@ int ntg_proj_post_solving(ntg_proj* q, double* x_d) {
     NTG_CUDA_TRY(cudaMemcpyAsync(av, q->adx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     for (int pass = 0; pass < 2 && q->m > 0; ++pass) {
       NTG_TRY(multidot(p, v, q->axs, q->m, q->coef, q->sc, s));
-      k_multiaxpy<<<G, 256, 0, s>>>(v, q->xs, av, q->axs, q->coef, q->m, n);
+      { k_multiaxpy<<<G, 256, 0, s>>>(v, q->xs, av, q->axs, q->coef, q->m, n); NTG_COUNT_LAUNCH(); }
     }
     NTG_TRY(multidot(p, v, av, 1, q->coef + kProjMax, q->sc, s));
     NTG_CUDA_TRY(cudaMemcpyAsync(q->hcoef, q->coef + kProjMax, sizeof(double), cudaMemcpyDeviceToHost, s));
     NTG_CUDA_TRY(cudaStreamSynchronize(s));
     if (q->hcoef[0] > 1e-300 && std::isfinite(q->hcoef[0])) {
-      k_scale2<<<G, 256, 0, s>>>(v, av, q->coef + kProjMax, n);
+      { k_scale2<<<G, 256, 0, s>>>(v, av, q->coef + kProjMax, n); NTG_COUNT_LAUNCH(); }
       q->m += 1;
     }
   }
   // x = xbar + dx
-  k_sum3<<<G, 256, 0, s>>>(x_d, q->xbar, x_d, n);
+  { k_sum3<<<G, 256, 0, s>>>(x_d, q->xbar, x_d, n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -271,7 +271,7 @@ int ntg_filter_apply(ntg_plan* p, ntg_ksp* ksp, double* X_out_d, const double* X
   p->nmask = 0;
   int st = NTG_OK;
   do {
-    k_mulB<<<G, 256, 0, s>>>(rhs, X_in_d, p->B, n);
+    { k_mulB<<<G, 256, 0, s>>>(rhs, X_in_d, p->B, n); NTG_COUNT_LAUNCH(); }
     if (cudaGetLastError() != cudaSuccess) { st = NTG_ERR_CUDA; set_error("filter rhs"); break; }
     if ((st = gs_launch(p, rhs, NTG_GS_ADD, s))) break;
     if (cudaMemcpyAsync(X_out_d, X_in_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
