@@ -266,6 +266,20 @@ double cuda_glsc2_mask(void* a, void* b, int* size, int* mask, int* mask_size);
 /* the stream the cuda_* kernels use (Neko's glb_cmd_queue) */
 void ntg_set_glb_queue(void* stream);
 
+/* Masked dot product sum_{i in mask} a[mask[i]-1] * b[mask[i]-1] that
+   allocates nothing.  No counterpart in the reference: it is the variant of
+   cuda_glsc2_mask for callers that cannot allocate device memory (device
+   memory owned by another allocator or exhausted, or no allocation-driven
+   synchronisation allowed mid-solve).  Its scratch is a fixed static device
+   array held by every GPU that loads the library until process exit; masks
+   longer than 16,777,216 entries are rejected with NTG_ERR_INVALID.  The
+   result goes to out_d (device, one double) on `stream`.  The first call on
+   each device looks up the scratch address and should come before any
+   stream capture.  Calls share the array: calls that overlap on the GPU
+   race; order them on one stream. */
+int ntg_glsc2_mask_noalloc(const double* a_d, const double* b_d, const int* mask_d, int mask_size,
+                           double* out_d, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

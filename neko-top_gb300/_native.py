@@ -90,6 +90,7 @@ SIGNATURES = {
     "cuda_cmult_mask": (None, [_vp, _pd, _pi, _vp, _pi]),
     "cuda_glsc2_mask": (_d, [_vp, _vp, _pi, _vp, _pi]),
     "ntg_set_glb_queue": (None, [_vp]),
+    "ntg_glsc2_mask_noalloc": (_i, [_vp, _vp, _vp, _i, _vp, _vp]),
 }
 
 _lib = None
