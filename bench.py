@@ -201,8 +201,12 @@ def run_ours(args, ws, rank, local):
     t_setup = time.time()
     coef, f, ncoef = setup_gpu_case(pkg, cfg, dev)
     n = coef.n
-    ksp_mx = pkg.krylov_solver_factory(coef, "fcg_mixed", 200, RTOL)
-    ksp_mx.set_inner(args.inner_rtol, args.inner_max)
+    if args.method == "cg_mixed":
+        ksp_mx = pkg.krylov_solver_factory(coef, "cg_mixed", 50000, RTOL)
+        ksp_mx.set_inner(args.delta, 1)
+    else:
+        ksp_mx = pkg.krylov_solver_factory(coef, "fcg_mixed", 200, RTOL)
+        ksp_mx.set_inner(args.inner_rtol, args.inner_max)
     ksp64 = pkg.krylov_solver_factory(coef, "cg", 20000, RTOL)
     x = torch.zeros(n, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
@@ -317,7 +321,9 @@ def run_ours(args, ws, rank, local):
         "dtype": "f32 inner / f64 outer",
         "data": "synthetic (seeded generators; no dataset)",
         "config": {"workload": f"{args.config}: {cfg['desc']}", "n_local_dofs": n, "n_unique_dofs": coef.nu,
-                   "method": f"fcg_mixed (inner Jacobi-PCG FP32 to {args.inner_rtol:g}, outer FCG(1) FP64)",
+                   "method": (f"cg_mixed (Jacobi-PCG in FP32, FP64 reliable updates at delta={args.delta:g})"
+                              if args.method == "cg_mixed" else
+                              f"fcg_mixed (inner Jacobi-PCG FP32 to {args.inner_rtol:g}, outer FCG(1) FP64)"),
                    "l2": "inputs larger than L2 (FP64 G 805 MB, FP32 G 403 MB at c2)",
                    "parallelism": "replicas only" if ws > 1 else "1 GPU"},
         "iterations": {"outer_mean": mx_outer, "inner_mean": mx_inner,
@@ -423,6 +429,8 @@ def main(argv=None):
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    p.add_argument("--method", choices=["cg_mixed", "fcg_mixed"], default="cg_mixed")
+    p.add_argument("--delta", type=float, default=0.1, help="reliable-update threshold of cg_mixed")
     p.add_argument("--inner-rtol", type=float, default=1e-4)
     p.add_argument("--inner-max", type=int, default=2000)
     p.add_argument("--fp64-steps", type=int, default=2)

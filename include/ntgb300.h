@@ -53,9 +53,15 @@ enum { NTG_FP64 = 0, NTG_FP32 = 1 };
 /* Krylov solver types */
 enum {
   NTG_KSP_CG = 0,        /* Jacobi-PCG, FP64 throughout (the plain drop-in) */
-  NTG_KSP_FCG_MIXED = 1  /* FP64 flexible CG whose preconditioner is an FP32
+  NTG_KSP_FCG_MIXED = 1, /* FP64 flexible CG whose preconditioner is an FP32
                             Jacobi-PCG inner solve (FP32 Ax, FP32 Jacobi, FP32
                             geometric factors); FP64 residuals and dots */
+  NTG_KSP_CG_MIXED = 2   /* Jacobi-PCG iterated in FP32 with FP64 reliable
+                            updates: the FP32 correction is folded into the
+                            FP64 solution and the residual recomputed in FP64
+                            (FP64 operator) whenever the FP32 residual fell by
+                            delta (ntg_ksp_set_inner's first argument, default
+                            0.1); convergence is confirmed on the FP64 residual */
 };
 
 typedef struct ntg_plan ntg_plan; /* mesh + coef_t + gs_t + Jacobi state */
@@ -121,6 +127,12 @@ int ntg_coef_set(ntg_plan* plan, const double* h1_d, double h1c, const double* h
 /* Dirichlet mask (bc_list): index list mask_d (device int32, nmask
    entries) in base `base` (1 for Neko masks).  nmask == 0 clears it. */
 int ntg_plan_set_mask(ntg_plan* plan, const int32_t* mask_d, int64_t nmask, int base);
+/* FP32 Ax path: 1 (default) = bulk-copy pipelined kernel for lx = 8, 0 =
+   the generic kernel (both give the same results within FP32 rounding) */
+int ntg_plan_set_ax_path(ntg_plan* plan, int use_tma);
+/* *flag = 1 if a bounded device wait of one of the plan's kernels ran out
+   since the last call (that launch's output is invalid) */
+int ntg_plan_check_error(ntg_plan* plan, int* flag);
 /* gs maps: perm (n int32: local indices sorted by global id, stable) and
    offs (nu+1 int64 segment offsets), device arrays */
 int ntg_gs_export(const ntg_plan* plan, int32_t* perm_d, int64_t* offs_d);

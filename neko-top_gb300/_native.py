@@ -10,7 +10,7 @@ _LIB = os.path.join(_HERE, "lib", "libntgb300.so")
 NTG_OK, NTG_ERR_INVALID, NTG_ERR_CUDA, NTG_ERR_ALLOC, NTG_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 NTG_MAXITER, NTG_BREAKDOWN, NTG_NONFINITE, NTG_GUESS_REJECTED = 10, 11, 12, 13
 GS_OP_ADD, GS_OP_MUL, GS_OP_MIN, GS_OP_MAX = 1, 2, 3, 4
-KSP_CG, KSP_FCG_MIXED = 0, 1
+KSP_CG, KSP_FCG_MIXED, KSP_CG_MIXED = 0, 1, 2
 
 _vp = C.c_void_p
 _i = C.c_int
@@ -50,6 +50,8 @@ SIGNATURES = {
     "ntg_coef_set": (_i, [_vp, _vp, _d, _vp, _d, _i]),
     "ntg_plan_set_mask": (_i, [_vp, _vp, _i64, _i]),
     "ntg_gs_export": (_i, [_vp, _vp, _vp]),
+    "ntg_plan_set_ax_path": (_i, [_vp, _i]),
+    "ntg_plan_check_error": (_i, [_vp, _pi]),
     "ntg_mesh_box": (_i, [_i, _i, _i, _i, _pd, _pd, _d, C.c_uint64, _vp, _vp, _vp, _vp, _vp]),
     "ntg_mask_face_xmax": (_i, [_i, _i, _i, _i, _vp, _pi64, _vp]),
     "ntg_field_uniform": (_i, [_vp, _i64, C.c_uint64, C.c_uint64, _d, _d, _vp, _vp]),

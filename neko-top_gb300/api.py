@@ -11,7 +11,8 @@ from dataclasses import dataclass
 
 import torch
 
-from ._native import (GS_OP_ADD, KSP_CG, KSP_FCG_MIXED, NtgError, check, check_last, lib, ntg_monitor)
+from ._native import (GS_OP_ADD, KSP_CG, KSP_CG_MIXED, KSP_FCG_MIXED, NtgError, check, check_last, lib,
+                      ntg_monitor)
 
 _DT = {torch.float64: "f64", torch.float32: "f32", torch.int32: "i32", torch.int64: "i64"}
 
@@ -163,6 +164,15 @@ class coef_t:
         torch.cuda.synchronize()
         return perm, offs
 
+    def set_ax_path(self, use_tma: bool):
+        """FP32 Ax: bulk-copy pipelined kernel (lx = 8) or the generic one."""
+        check(lib().ntg_plan_set_ax_path(self.handle, int(bool(use_tma))))
+
+    def check_error(self) -> bool:
+        f = C.c_int()
+        check(lib().ntg_plan_check_error(self.handle, C.byref(f)))
+        return bool(f.value)
+
     def free(self):
         if self._h is not None:
             check(lib().ntg_plan_destroy(self._h))
@@ -276,7 +286,7 @@ def krylov_solver_factory(coef: coef_t, type_: str = "cg", max_iter: int = 800, 
     """krylov_solver_factory(ksp, n, type, max_iter, abstol)
     (sources/adjoint/adjoint_scheme.f90:1046-1055).  type: 'cg' (FP64
     Jacobi-PCG) or 'fcg_mixed' (FP32 inner PCG in an FP64 flexible CG)."""
-    t = {"cg": KSP_CG, "fcg_mixed": KSP_FCG_MIXED}.get(type_)
+    t = {"cg": KSP_CG, "fcg_mixed": KSP_FCG_MIXED, "cg_mixed": KSP_CG_MIXED}.get(type_)
     if t is None:
         raise ValueError(f"unknown solver type {type_!r}")
     return _ksp(coef, t, max_iter, rtol, abstol)

@@ -26,21 +26,6 @@ struct DParam {
   T d[LX * LX];
 };
 
-// Fused dot finaliser: pap = sum p.(A p)_local; alpha = rz / pap.
-struct FinPap {
-  __device__ void operator()(const double* acc, Scalars* sc) const {
-    double pap = acc[0];
-    sc->pap = pap;
-    if (!(pap > 0.0) || !isfinite(pap)) {
-      sc->status = isfinite(pap) ? NTG_BREAKDOWN : NTG_NONFINITE;
-      sc->done = 1;
-      sc->alpha = 0.0;
-    } else {
-      sc->alpha = sc->rz / pap;
-    }
-  }
-};
-
 template <typename T, int LX>
 struct AxShape {
   static constexpr int LX2 = LX * LX, LX3 = LX * LX * LX;
@@ -76,7 +61,7 @@ __global__ void __launch_bounds__(AxShape<T, LX>::NT)
     DTi[l] = Dp.d[l * LX + i];
     DTj[l] = Dp.d[l * LX + j];
   }
-  double dot = 0.0;
+  T dot = 0;  // per-thread partial in the kernel's precision (FP64 math is scarce on GB300)
   const int64_t ngroups = (nelv + EPB - 1) / EPB;
   for (int64_t grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
     const int64_t e = grp * EPB + le;
@@ -128,16 +113,21 @@ __global__ void __launch_bounds__(AxShape<T, LX>::NT)
         const int64_t q = base + k * LX2;
         if (H2) acc = fma(hB[q], ureg[k], acc);
         w[q] = acc;
-        if (DOT) dot += (double)ureg[k] * (double)acc;
+        if (DOT) dot = fma(ureg[k], acc, dot);
       }
     }
     __syncthreads();
   }
   if (DOT) {
-    double v[1] = {dot};
+    double v[1] = {(double)dot};
     grid_reduce<1>(v, part, sc, FinPap());
   }
 }
+
+// TMA-pipelined FP32 kernel for lx = 8 (ax_helm_f32_tma.cu); returns
+// NTG_ERR_UNSUPPORTED when a pointer is not 16-byte aligned.
+int ax_f32_tma_launch(ntg_plan* p, float* w, const float* u, const float* const* g, const float* h1, float h1c,
+                      const float* hB, Scalars* sc, cudaStream_t s);
 
 template <typename T, int LX>
 static int launch_lx(ntg_plan* p, T* w, const T* u, const T* const* g, const T* h1, T h1c, const T* hB,
@@ -198,8 +188,11 @@ int ax_launch_f32(ntg_plan* p, float* w, const float* u, Scalars* dot_scal, int,
   NTG_TRY(ensure_fp32(p));
   const float* g[6] = {p->gf[0], p->gf[1], p->gf[2], p->gf[3], p->gf[4], p->gf[5]};
   timer_start(TM_AX32, s);
-  int st = ax_dispatch<float>(p, w, u, g, p->h1_const ? nullptr : p->h1f, (float)p->h1c,
-                              p->ifh2 ? p->hBf : nullptr, dot_scal, s);
+  const float* h1 = p->h1_const ? nullptr : p->h1f;
+  const float* hB = p->ifh2 ? p->hBf : nullptr;
+  int st = NTG_ERR_UNSUPPORTED;
+  if (p->lx == 8 && p->use_tma) st = ax_f32_tma_launch(p, w, u, g, h1, (float)p->h1c, hB, dot_scal, s);
+  if (st == NTG_ERR_UNSUPPORTED) st = ax_dispatch<float>(p, w, u, g, h1, (float)p->h1c, hB, dot_scal, s);
   timer_stop(TM_AX32, s);
   return st;
 }

@@ -76,7 +76,11 @@ struct Scalars {
   double pap_prev; // (p_{k-1}, A p_{k-1}) of the flexible CG
   double gamma;    // flexible-CG orthogonalisation coefficient
   double rr0;      // (r0, r0) at the start of the solve
+  double rmax;     // reliable updates: largest ||r|| since the last FP64 residual
+  double delta;    // reliable updates: replace the residual when ||r|| < delta * rmax
   double red[8];   // scratch results of generic reductions
+  int ru_mode;     // 1 = FP32 iteration with FP64 reliable updates
+  int need_ru;     // 1 = residual replacement due, 2 = FP32 residual converged (confirm in FP64)
   int iter;        // iterations performed
   int done;        // 1 = converged or stopped: later kernels are no-ops
   int status;      // NTG_OK / NTG_MAXITER / NTG_BREAKDOWN / NTG_NONFINITE
@@ -122,6 +126,9 @@ struct ntg_plan {
   double* dinv = nullptr;
   float* dinvf = nullptr;
   int jacobi_ready = 0;
+  // FP32 Ax path: 1 = bulk-copy pipelined kernel for lx = 8 (default)
+  int use_tma = 1;
+  int* dev_err = nullptr;        // set by kernels whose bounded waits ran out
   // reductions
   double* red_part = nullptr;    // kRedSlots * kRedLanes
   ntg::Scalars* scal = nullptr;  // generic scalars for standalone dots

@@ -182,7 +182,19 @@ struct FinUpd {
       sc->done = 1;
       return;
     }
-    if (acc[1] <= sc->tol2) {
+    if (sc->ru_mode) {
+      // FP32 residual: a converged one is only a candidate (the host
+      // confirms it with an FP64 residual); a drop by delta since the last
+      // FP64 residual asks for a replacement
+      if (acc[1] <= sc->tol2) {
+        sc->need_ru = 2;
+        sc->done = 1;
+        return;
+      }
+      const double rn = sqrt(acc[1]);
+      if (rn > sc->rmax) sc->rmax = rn;
+      if (rn < sc->delta * sc->rmax && sc->need_ru == 0) sc->need_ru = 1;
+    } else if (acc[1] <= sc->tol2) {
       sc->done = 1;
       return;
     }
@@ -203,18 +215,20 @@ __global__ void k_cg_update(T* __restrict__ x, const T* __restrict__ p, T* __res
                             double* __restrict__ part, Scalars* sc) {
   if (sc->done) return;
   const T alpha = (T)sc->alpha;
-  double rz = 0, rr = 0;
+  // per-thread partials in T: FP64 arithmetic is 1/58 of FP32 on GB300, so
+  // the FP32 iteration accumulates its short per-thread sums in FP32 and
+  // only the block/grid levels in FP64
+  T rz = 0, rr = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     T xi = x[i] + alpha * p[i];
     T ri = r[i] - alpha * w[i];
     x[i] = xi;
     r[i] = ri;
-    double m = (double)mult[i];
-    double rd = (double)ri;
-    rz += m * rd * (double)(dinv[i] * ri);
-    rr += m * rd * rd;
+    T mr = mult[i] * ri;
+    rz += mr * (dinv[i] * ri);
+    rr += mr * ri;
   }
-  double v[2] = {rz, rr};
+  double v[2] = {(double)rz, (double)rr};
   grid_reduce<2>(v, part, sc, FinUpd());
 }
 
@@ -406,6 +420,126 @@ __global__ void k_zero_f(float* __restrict__ a, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = 0.f;
 }
 
+// ---------------------------------------------------------------------------
+// Mixed-precision CG with reliable updates (Sleijpen & van der Vorst 1996;
+// the residual-replacement scheme lattice-QCD solvers use for mixed
+// precision).  One Jacobi-PCG runs in FP32 (operator, preconditioner,
+// vectors); the FP32 iterate y accumulates a correction that is folded into
+// the FP64 solution x whenever the FP32 residual has dropped by `delta`
+// since the last replacement, at which point the residual is recomputed in
+// FP64 (r = f - A x) and rounded back into the FP32 iteration.  The search
+// direction is kept across replacements, so the Krylov space is never
+// restarted.  Convergence is only declared on an FP64 residual.
+// ---------------------------------------------------------------------------
+struct FinRUInit {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    // acc: ff, rr (FP64), rz (FP32 iteration)
+    sc->ff = acc[0];
+    sc->rr = acc[1];
+    sc->rr0 = acc[1];
+    sc->rz = acc[2];
+    sc->rmax = sqrt(acc[1]);
+    double t = sc->rtol * sqrt(acc[0]);
+    if (sc->abstol > t) t = sc->abstol;
+    sc->tol2 = t * t;
+    sc->iter = 0;
+    sc->status = NTG_OK;
+    sc->done = 0;
+    sc->need_ru = 0;
+    if (!isfinite(acc[0]) || !isfinite(acc[1]) || !isfinite(acc[2])) {
+      sc->status = NTG_NONFINITE;
+      sc->done = 1;
+    } else if (acc[1] <= sc->tol2) {
+      sc->done = 1;
+    } else if (sc->max_iter <= 0) {
+      sc->status = NTG_MAXITER;
+      sc->done = 1;
+    }
+  }
+};
+
+// r = f - w (w null: r = f); r32 = (float) r; p32 = dinv32 r32; y32 = 0
+__global__ void k_ru_init(const double* __restrict__ f, const double* __restrict__ w, const float* __restrict__ dinv,
+                          const double* __restrict__ mult, double* __restrict__ r, float* __restrict__ r32,
+                          float* __restrict__ p32, float* __restrict__ y32, int64_t n, double* __restrict__ part,
+                          Scalars* sc) {
+  double ff = 0, rr = 0;
+  float rz = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double fi = f[i];
+    const double ri = w ? fi - w[i] : fi;
+    const float rf = (float)ri;
+    const float zf = dinv[i] * rf;
+    r[i] = ri;
+    r32[i] = rf;
+    p32[i] = zf;
+    y32[i] = 0.f;
+    const double m = mult[i];
+    ff += m * fi * fi;
+    rr += m * ri * ri;
+    rz += (float)m * rf * zf;
+  }
+  double v[3] = {ff, rr, (double)rz};
+  grid_reduce<3>(v, part, sc, FinRUInit());
+}
+
+// x += (double) y; y = 0
+__global__ void k_ru_accum(double* __restrict__ x, float* __restrict__ y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (double)y[i];
+    y[i] = 0.f;
+  }
+}
+
+struct FinRU {
+  int mode;  // 1: replacement during the iteration; 2: confirm a converged FP32 residual
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    // acc: rr (FP64), rz of the new FP32 residual
+    sc->rr = acc[0];
+    sc->rmax = sqrt(acc[0]);
+    sc->need_ru = 0;
+    if (!isfinite(acc[0]) || !isfinite(acc[1])) {
+      sc->status = NTG_NONFINITE;
+      sc->done = 1;
+      return;
+    }
+    if (acc[0] <= sc->tol2) {
+      sc->status = NTG_OK;
+      sc->done = 1;
+      return;
+    }
+    if (sc->iter >= sc->max_iter) {
+      sc->status = NTG_MAXITER;
+      sc->done = 1;
+      return;
+    }
+    // a confirmation that failed resumes the iteration: the direction update
+    // skipped at the candidate uses the replaced residual
+    if (mode == 2) sc->beta = acc[1] / sc->rz;
+    sc->rz = acc[1];
+    sc->done = 0;
+  }
+};
+
+// r = f - w (FP64); r32 = (float) r; sums (r, r)_mult, (r32, dinv32 r32)_mult
+__global__ void k_ru_resid(const double* __restrict__ f, const double* __restrict__ w, const float* __restrict__ dinv,
+                           const double* __restrict__ mult, double* __restrict__ r, float* __restrict__ r32, int64_t n,
+                           int mode, double* __restrict__ part, Scalars* sc) {
+  double rr = 0;
+  float rz = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = f[i] - w[i];
+    const float rf = (float)ri;
+    r[i] = ri;
+    r32[i] = rf;
+    const double m = mult[i];
+    rr += m * ri * ri;
+    rz += (float)m * rf * (dinv[i] * rf);
+  }
+  double v[2] = {rr, (double)rz};
+  grid_reduce<2>(v, part, sc, FinRU{mode});
+}
+
 }  // namespace ntg
 
 // ---------------------------------------------------------------------------
@@ -565,6 +699,106 @@ static int ksp_solve_mixed(ntg_ksp* k, double* x, const double* f, ntg_monitor* 
   return NTG_OK;
 }
 
+// Reliable-update mixed CG (NTG_KSP_CG_MIXED); see the kernels above.
+static int ksp_solve_mixed_ru(ntg_ksp* k, double* x, const double* f, ntg_monitor* mon) {
+  ntg_plan* p = k->plan;
+  cudaStream_t s = p->stream;
+  const int64_t n = p->n;
+  const int TPB = 256;
+  const int G = grid_for(n, TPB);
+  NTG_TRY(ensure_fp32(p));
+  if (!p->jacobi_ready) NTG_TRY(jacobi_update(p));
+  double xx = 0.0;
+  NTG_TRY(wdot(p, x, x, nullptr, n, &xx, s));
+  int fpax = 0, nru = 0;
+  Scalars* hs = k->hs;
+  memset(hs, 0, sizeof(Scalars));
+  hs->rtol = k->rtol;
+  hs->abstol = k->abstol;
+  hs->max_iter = k->max_iter;
+  hs->ru_mode = 1;
+  hs->delta = k->inner_rtol;
+  NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+  if (xx != 0.0) {
+    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    fpax++;
+  }
+  float* y32 = k->din;
+  { k_ru_init<<<G, TPB, 0, s>>>(f, xx != 0.0 ? k->v64.w : nullptr, p->dinvf, p->mult, k->v64.r, k->v32.r, k->v32.p, y32, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  auto poll = [&]() -> int {
+    NTG_CUDA_TRY(cudaMemcpyAsync(hs, k->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    NTG_CUDA_TRY(cudaStreamSynchronize(s));
+    return NTG_OK;
+  };
+  auto replace = [&](int mode) -> int {
+    { k_ru_accum<<<G, TPB, 0, s>>>(x, y32, n); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    fpax++;
+    nru++;
+    { k_ru_resid<<<G, TPB, 0, s>>>(f, k->v64.w, p->dinvf, p->mult, k->v64.r, k->v32.r, n, mode, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+    NTG_CUDA_TRY(cudaGetLastError());
+    return poll();
+  };
+  double rr0 = 0, ff = 0;
+  NTG_TRY(poll());
+  rr0 = hs->rr0;
+  ff = hs->ff;
+  bool y_dirty = false;  // y32 holds a correction not yet folded into x
+  int guard = 0;
+  for (;;) {
+    if (hs->done) {
+      if (hs->need_ru == 2) {
+        NTG_TRY(replace(2));
+        y_dirty = false;
+        if (hs->done) break;
+        { k_cg_dir<float><<<G, TPB, 0, s>>>(k->v32.p, k->v32.r, p->dinvf, n, k->sc); NTG_COUNT_LAUNCH(); }
+        continue;
+      }
+      break;
+    }
+    if (hs->need_ru == 1) {
+      NTG_TRY(replace(1));
+      y_dirty = false;
+      if (hs->done) break;
+    }
+    if (++guard > k->max_iter / k->check_every + 64) break;  // defensive: the device cap ends the loop first
+    for (int c = 0; c < k->check_every; ++c) {
+      NTG_TRY(ax_launch_f32(p, k->v32.w, k->v32.p, k->sc, 0, s));
+      NTG_TRY(gs_add_guarded_f32(p, k->v32.w, s, k->sc));
+      NTG_TRY(mask_guarded_f32(p, k->v32.w, s, k->sc));
+      timer_start(TM_UPD32, s);
+      { k_cg_update<float><<<G, TPB, 0, s>>>(y32, k->v32.p, k->v32.r, k->v32.w, p->dinvf, p->multf, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+      timer_stop(TM_UPD32, s);
+      timer_start(TM_DIR32, s);
+      { k_cg_dir<float><<<G, TPB, 0, s>>>(k->v32.p, k->v32.r, p->dinvf, n, k->sc); NTG_COUNT_LAUNCH(); }
+      timer_stop(TM_DIR32, s);
+    }
+    y_dirty = true;
+    NTG_TRY(poll());
+  }
+  int status = hs->status;
+  double rr_final = hs->rr;
+  if (y_dirty) {
+    // stopped inside the FP32 iteration (cap, breakdown, non-finite): fold
+    // the correction in and report the FP64 residual
+    const int iters = hs->iter;
+    NTG_TRY(replace(1));
+    rr_final = hs->rr;
+    hs->iter = iters;
+  }
+  if (mon) {
+    mon->iter = hs->iter;
+    mon->inner_iter = nru;
+    mon->res_start = sqrt(rr0);
+    mon->res_final = sqrt(rr_final);
+    mon->rhs_norm = sqrt(ff);
+    mon->status = status;
+    mon->fp64_ax = fpax;
+  }
+  return NTG_OK;
+}
+
 extern "C" {
 
 int ntg_pc_jacobi_update(ntg_plan* plan) {
@@ -599,7 +833,8 @@ int ntg_glsc3(ntg_plan* plan, const double* a_d, const double* b_d, const double
 int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double abstol, ntg_ksp** ksp) {
   clear_error();
   NTG_CHECK_ARG(plan && ksp, "ntg_ksp_create: null argument");
-  NTG_CHECK_ARG(type == NTG_KSP_CG || type == NTG_KSP_FCG_MIXED, "ntg_ksp_create: unknown solver type");
+  NTG_CHECK_ARG(type == NTG_KSP_CG || type == NTG_KSP_FCG_MIXED || type == NTG_KSP_CG_MIXED,
+                "ntg_ksp_create: unknown solver type");
   NTG_CHECK_ARG(max_iter >= 0 && rtol >= 0 && abstol >= 0, "ntg_ksp_create: bad tolerance or iteration cap");
   *ksp = nullptr;
   ntg_ksp* k = new ntg_ksp();
@@ -620,6 +855,13 @@ int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double a
     if (cudaMallocHost(&k->hs_in, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
     if (cudaMemset(k->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMemset(k->sc_in, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    if (type == NTG_KSP_CG_MIXED) {
+      k->inner_rtol = 0.1;  // reliable-update threshold delta
+      if ((st = dev_alloc(&k->v32.r, n))) break;
+      if ((st = dev_alloc(&k->v32.p, n))) break;
+      if ((st = dev_alloc(&k->v32.w, n))) break;
+      if ((st = dev_alloc(&k->din, n))) break;
+    }
     if (type == NTG_KSP_FCG_MIXED) {
       if ((st = dev_alloc(&k->pd, n))) break;
       if ((st = dev_alloc(&k->qd, n))) break;
@@ -670,6 +912,7 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
   NTG_CHECK_ARG(ksp && x_d && f_d, "ntg_ksp_solve: null argument");
   if (mon) memset(mon, 0, sizeof(*mon));
   if (ksp->type == NTG_KSP_FCG_MIXED) return ksp_solve_mixed(ksp, x_d, f_d, mon);
+  if (ksp->type == NTG_KSP_CG_MIXED) return ksp_solve_mixed_ru(ksp, x_d, f_d, mon);
   return ksp_solve_cg(ksp, x_d, f_d, mon);
 }
 

@@ -349,7 +349,7 @@ static void plan_free(ntg_plan* p) {
   dev_free(p->perm); dev_free(p->offs); dev_free(p->sh_idx); dev_free(p->sh_off);
   dev_free(p->h1); dev_free(p->h1f); dev_free(p->hB); dev_free(p->hBf);
   dev_free(p->mask); dev_free(p->dinv); dev_free(p->dinvf);
-  dev_free(p->red_part); dev_free(p->scal);
+  dev_free(p->red_part); dev_free(p->scal); dev_free(p->dev_err);
   if (p->host_red) cudaFreeHost(p->host_red);
   p->host_red = nullptr;
 }
@@ -570,6 +570,8 @@ int ntg_plan_create(ntg_plan** plan, int64_t nelv, int lx, const double* x_d, co
     if ((st = dev_alloc(&p->B, p->n))) break;
     if ((st = dev_alloc(&p->red_part, (size_t)kRedSlots * kRedLanes))) break;
     if ((st = dev_alloc(&p->scal, 1))) break;
+    if ((st = dev_alloc(&p->dev_err, 1))) break;
+    if (cudaMemset(p->dev_err, 0, sizeof(int)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMemset(p->scal, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMallocHost(&p->host_red, sizeof(double) * 16) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
     { k_geom<<<grid_for(p->n, 128), 128, 0, p->stream>>>(nelv, lx, bs, x_d, y_d, z_d, p->g[0], p->g[1], p->g[2],

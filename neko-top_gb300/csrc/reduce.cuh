@@ -70,4 +70,19 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NL], double* __restrict_
   }
 }
 
+// Fused dot finaliser: pap = sum p.(A p)_local; alpha = rz / pap.
+struct FinPap {
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    double pap = acc[0];
+    sc->pap = pap;
+    if (!(pap > 0.0) || !isfinite(pap)) {
+      sc->status = isfinite(pap) ? NTG_BREAKDOWN : NTG_NONFINITE;
+      sc->done = 1;
+      sc->alpha = 0.0;
+    } else {
+      sc->alpha = sc->rz / pap;
+    }
+  }
+};
+
 }  // namespace ntg

@@ -346,3 +346,48 @@ def test_synthetic_generators_match_oracle(pkg, orc, dev):
     c.set_mask(T(mask, dev, torch.int32), base=1)
     f = orc.field_fourier(m, k, a, ph)
     assert relerr(c.rhs_assemble(T(f, dev)), orc.assemble_rhs(m, f, mask)) < 1e-14
+
+
+@pytest.mark.parametrize("coefs", ["poisson", "h2", "h1_h2"])
+def test_ax_fp32_bulk_copy_pipeline(pkg, orc, dev, coefs):
+    """The bulk-copy (TMA) FP32 kernel against the generic FP32 kernel and the
+    oracle, on 27 elements (six full groups of four and a partial one)."""
+    m, c = make(pkg, orc, dev, 3, 3, 3, 8, amp=0.05, seed=6)
+    rng = np.random.default_rng(13)
+    u = rng.standard_normal(m.n)
+    h1 = rng.uniform(0.5, 2.0, m.n) if coefs == "h1_h2" else None
+    h2 = rng.uniform(0.0, 3.0, m.n) if coefs != "poisson" else None
+    c.set_coefs(h1=None if h1 is None else T(h1, dev), h1c=1.0, h2=None if h2 is None else T(h2, dev),
+                ifh2=h2 is not None)
+    ref = orc.ax_helm(m, u, h1=h1, h2=h2)
+    out = {}
+    for path in (1, 0):
+        c.set_ax_path(path)
+        w = torch.full((m.n,), float("nan"), dtype=torch.float32, device=dev)
+        pkg.ax_helm_t().compute(w, T(u, dev, torch.float32), c)
+        torch.cuda.synchronize()
+        out[path] = w.double()
+    assert not c.check_error()
+    assert relerr(out[1], ref) < 2e-5
+    assert relerr(out[1], out[0]) < 1e-5
+
+
+def test_cg_mixed_reliable_updates(pkg, orc, dev):
+    m, c, mask, f = poisson_deformed(pkg, orc, dev)
+    x_ref, it_ref, _, _ = orc.cg(m, f, mask=mask, rtol=1e-12)
+    _, it64, _, _ = orc.cg(m, f, mask=mask, rtol=1e-10)
+    ksp = pkg.krylov_solver_factory(c, "cg_mixed", 5000, 1e-10)
+    x = torch.zeros(m.n, dtype=torch.float64, device=dev)
+    mon = ksp.solve(x, T(f, dev))
+    torch.cuda.synchronize()
+    assert mon.status == pkg.NTG_OK, mon
+    xn = x.cpu().numpy()
+    r = f - orc.op_apply(m, xn, mask=mask)
+    assert np.sqrt(orc.glsc3(r, r, m.mult)) <= 1.5e-10 * np.sqrt(orc.glsc3(f, f, m.mult))
+    assert np.linalg.norm(xn - x_ref) <= 1e-7 * np.linalg.norm(x_ref)
+    # one Krylov space: close to the FP64 iteration count
+    assert mon.iter <= 1.3 * it64 + 10, (mon.iter, it64)
+    assert mon.fp64_ax >= 1
+    # with a non-zero initial guess (the solution itself): converges at once
+    mon2 = ksp.solve(x, T(f, dev))
+    assert mon2.status == pkg.NTG_OK and mon2.iter <= 2
