@@ -189,6 +189,25 @@ def time_solves(ksp, x, f, k, ev):
     return e0.elapsed_time(e1) / 1e3, mons
 
 
+def run_kernels_only(args, pkg, coef, f, dev):
+    """A few launches of each hot kernel on the workload (for profiler
+    captures): FP64 Ax, FP32 Ax, gs, and 24 iterations of the mixed solver."""
+    import torch
+    n = coef.n
+    ax = pkg.ax_helm_t()
+    for dt in (torch.float64, torch.float32):
+        u = torch.randn(n, dtype=dt, device=dev)
+        w = torch.empty_like(u)
+        for _ in range(3):
+            ax.compute(w, u, coef)
+        pkg.gs_t(coef).op(w)
+    ksp = pkg.krylov_solver_factory(coef, "cg_mixed", 24, RTOL)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    mon = ksp.solve(x, f)
+    torch.cuda.synchronize()
+    return {"kernels_only": True, "n_local_dofs": n, "iters": mon.iter, "status": mon.status}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     import __graft_entry__ as ge
@@ -200,6 +219,8 @@ def run_ours(args, ws, rank, local):
     ev = lambda: torch.cuda.Event(enable_timing=True)
     t_setup = time.time()
     coef, f, ncoef = setup_gpu_case(pkg, cfg, dev)
+    if args.kernels_only:
+        return run_kernels_only(args, pkg, coef, f, dev)
     n = coef.n
     if args.method == "cg_mixed":
         ksp_mx = pkg.krylov_solver_factory(coef, "cg_mixed", 50000, RTOL)
@@ -436,6 +457,8 @@ def main(argv=None):
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--cpu-iters", type=int, default=20)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--kernels-only", action="store_true",
+                   help="set up the workload and launch each hot kernel a few times (profiler captures)")
     p.add_argument("--traffic", type=float, default=None,
                    help="dram bytes per FP32 Ax launch from an ncu capture (reported as roofline.traffic)")
     args = p.parse_args(argv)
