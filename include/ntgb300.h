@@ -130,6 +130,9 @@ int ntg_plan_set_mask(ntg_plan* plan, const int32_t* mask_d, int64_t nmask, int 
 /* FP32 Ax path: 1 (default) = bulk-copy pipelined kernel for lx = 8, 0 =
    the generic kernel (both give the same results within FP32 rounding) */
 int ntg_plan_set_ax_path(ntg_plan* plan, int use_tma);
+/* gather-scatter kernel: 1 (default) = groups split by multiplicity with
+   vector index loads, 0 = one thread per group (bit-identical results) */
+int ntg_plan_set_gs_path(ntg_plan* plan, int by_class);
 /* *flag = 1 if a bounded device wait of one of the plan's kernels ran out
    since the last call (that launch's output is invalid) */
 int ntg_plan_check_error(ntg_plan* plan, int* flag);

@@ -51,6 +51,7 @@ SIGNATURES = {
     "ntg_plan_set_mask": (_i, [_vp, _vp, _i64, _i]),
     "ntg_gs_export": (_i, [_vp, _vp, _vp]),
     "ntg_plan_set_ax_path": (_i, [_vp, _i]),
+    "ntg_plan_set_gs_path": (_i, [_vp, _i]),
     "ntg_plan_check_error": (_i, [_vp, _pi]),
     "ntg_mesh_box": (_i, [_i, _i, _i, _i, _pd, _pd, _d, C.c_uint64, _vp, _vp, _vp, _vp, _vp]),
     "ntg_mask_face_xmax": (_i, [_i, _i, _i, _i, _vp, _pi64, _vp]),

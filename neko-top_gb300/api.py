@@ -168,6 +168,10 @@ class coef_t:
         """FP32 Ax: bulk-copy pipelined kernel (lx = 8) or the generic one."""
         check(lib().ntg_plan_set_ax_path(self.handle, int(bool(use_tma))))
 
+    def set_gs_path(self, by_class: bool):
+        """gather-scatter: multiplicity classes (default) or one thread per group."""
+        check(lib().ntg_plan_set_gs_path(self.handle, int(bool(by_class))))
+
     def check_error(self) -> bool:
         f = C.c_int()
         check(lib().ntg_plan_check_error(self.handle, C.byref(f)))

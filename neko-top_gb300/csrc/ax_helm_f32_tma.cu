@@ -299,6 +299,15 @@ extern "C" int ntg_plan_set_ax_path(ntg_plan* plan, int use_tma) {
   return NTG_OK;
 }
 
+// Select the gather-scatter kernel: 1 = by multiplicity class (default),
+// 0 = one thread per shared group.  Both give bit-identical results.
+extern "C" int ntg_plan_set_gs_path(ntg_plan* plan, int by_class) {
+  clear_error();
+  NTG_CHECK_ARG(plan, "ntg_plan_set_gs_path: null plan");
+  plan->gs_classes = by_class ? 1 : 0;
+  return NTG_OK;
+}
+
 // 1 if a bounded wait of a kernel of this plan ran out (the flag is cleared).
 extern "C" int ntg_plan_check_error(ntg_plan* plan, int* flag) {
   clear_error();

@@ -111,6 +111,15 @@ struct ntg_plan {
   int64_t* offs = nullptr;
   int32_t* sh_idx = nullptr;  // local indices of nodes with > 1 copy, grouped
   int32_t* sh_off = nullptr;  // nshared + 1 offsets into sh_idx
+  // the same groups split by multiplicity (2, 4, 8, other), each class
+  // ordered by its first local index (gs_classes.cu)
+  int gs_classes = 1;           // 1: class kernel (default); 0: one thread per group
+  int64_t ncls[4] = {0, 0, 0, 0};
+  int2* gs2 = nullptr;
+  int4* gs4 = nullptr;
+  int4* gs8 = nullptr;          // two int4 per group
+  int32_t* gsx_idx = nullptr;
+  int32_t* gsx_off = nullptr;
   // coefficients
   int h1_const = 1;
   double h1c = 1.0;
@@ -168,6 +177,9 @@ int gs_add_guarded_f32(ntg_plan* p, float* u, cudaStream_t s, const Scalars* sc)
 int mask_guarded(ntg_plan* p, double* u, cudaStream_t s, const Scalars* sc);
 int mask_guarded_f32(ntg_plan* p, float* u, cudaStream_t s, const Scalars* sc);
 int ensure_fp32(ntg_plan* p);
+int build_gs_classes(ntg_plan* p);
+template <typename T>
+int gs_cls_launch(ntg_plan* p, T* u, int op, cudaStream_t s, const Scalars* sc);
 int grid_for(int64_t work, int threads);
 int num_sms();
 }  // namespace ntg

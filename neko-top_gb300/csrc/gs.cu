@@ -53,6 +53,7 @@ static int gs_any(ntg_plan* p, T* u, int op, cudaStream_t s, const Scalars* sc) 
     cudaStream_t s;
     ~Stop() { timer_stop(id, s); }
   } stop_{tid, s};
+  if (p->gs_classes) return gs_cls_launch<T>(p, u, op, s, sc);
   switch (op) {
     case NTG_GS_ADD: { k_gs_shared<T, NTG_GS_ADD><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); NTG_COUNT_LAUNCH(); } break;
     case NTG_GS_MUL: { k_gs_shared<T, NTG_GS_MUL><<<G, TPB, 0, s>>>(u, p->sh_idx, p->sh_off, p->nshared, sc); NTG_COUNT_LAUNCH(); } break;

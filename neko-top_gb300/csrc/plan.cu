@@ -350,6 +350,7 @@ static void plan_free(ntg_plan* p) {
   dev_free(p->h1); dev_free(p->h1f); dev_free(p->hB); dev_free(p->hBf);
   dev_free(p->mask); dev_free(p->dinv); dev_free(p->dinvf);
   dev_free(p->red_part); dev_free(p->scal); dev_free(p->dev_err);
+  dev_free(p->gs2); dev_free(p->gs4); dev_free(p->gs8); dev_free(p->gsx_idx); dev_free(p->gsx_off);
   if (p->host_red) cudaFreeHost(p->host_red);
   p->host_red = nullptr;
 }
@@ -578,6 +579,7 @@ int ntg_plan_create(ntg_plan** plan, int64_t nelv, int lx, const double* x_d, co
                                                         p->g[3], p->g[4], p->g[5], p->B); NTG_COUNT_LAUNCH(); }
     if (cudaGetLastError() != cudaSuccess) { st = NTG_ERR_CUDA; set_error("k_geom launch failed"); break; }
     if ((st = build_gs(p, glb_d))) break;
+    if ((st = build_gs_classes(p))) break;
   } while (0);
   if (st) {
     plan_free(p);

@@ -100,15 +100,24 @@ def test_ax_helm_fp32(pkg, orc, dev):
 
 
 @pytest.mark.parametrize("op", [1, 2, 3, 4])
-def test_gs_ops_bitexact(pkg, orc, dev, op):
-    m, c = make(pkg, orc, dev, 3, 3, 2, 6, amp=0.05, seed=8)
+@pytest.mark.parametrize("shape", [(3, 3, 2, 6), (5, 1, 3, 3), (9, 7, 5, 8)])
+@pytest.mark.parametrize("path", [1, 0])
+def test_gs_ops_bitexact(pkg, orc, dev, op, shape, path):
+    ex, ey, ez, lx = shape
+    m, c = make(pkg, orc, dev, ex, ey, ez, lx, amp=0.05, seed=8)
+    c.set_gs_path(path)
     rng = np.random.default_rng(op)
     u = rng.uniform(0.5, 1.5, m.n)
     ref = orc.gs_op(m, u, op)
-    v = T(u, dev)
-    pkg.gs_t(c).op(v, op)
-    torch.cuda.synchronize()
-    assert np.array_equal(v.cpu().numpy(), ref)
+    for dt in (torch.float64, torch.float32):
+        v = T(u, dev, dt)
+        pkg.gs_t(c).op(v, op)
+        torch.cuda.synchronize()
+        if dt == torch.float64:
+            assert np.array_equal(v.cpu().numpy(), ref)
+        else:
+            ref32 = orc.gs_op(m, u.astype(np.float32).astype(np.float64), op)
+            assert np.allclose(v.cpu().numpy(), ref32, rtol=1e-6)
 
 
 def test_jacobi_and_mask(pkg, orc, dev):
