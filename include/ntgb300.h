@@ -80,6 +80,7 @@ typedef struct ntg_monitor {
   double rhs_norm;   /* ||f|| */
   int status;        /* NTG_OK, NTG_MAXITER, NTG_BREAKDOWN, NTG_NONFINITE */
   int fp64_ax;       /* FP64 operator applications performed */
+  int guess_rejected; /* 1 if the guess guard replaced the guess by zero */
 } ntg_monitor;
 
 /* ---------------------------------------------------------------------- */
@@ -160,6 +161,11 @@ int ntg_field_uniform(const int64_t* gid_d, int64_t n, uint64_t seed, uint64_t s
    U[-1,1]/|k|^2, k in [1,kmax]^3, X the coordinates normalised by the box */
 int ntg_field_fourier(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
                       const double* hi3, int nmodes, int kmax, uint64_t seed, double* f_d, void* stream);
+/* the same modes with explicit parameters (host arrays: k 3*nmodes ints,
+   amplitudes, phases), for right-hand-side sequences */
+int ntg_field_modes(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
+                    const double* hi3, int nmodes, const int* k, const double* amp, const double* ph, double* f_d,
+                    void* stream);
 /* clip(sum of nblobs Gaussians of the given width, 0, 1), centres U(box) */
 int ntg_field_blobs(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
                     const double* hi3, uint64_t seed, int nblobs, double width, double* f_d, void* stream);
@@ -207,6 +213,12 @@ int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double a
 int ntg_ksp_destroy(ntg_ksp* ksp);
 /* mixed solver: inner relative tolerance and inner iteration cap */
 int ntg_ksp_set_inner(ntg_ksp* ksp, double inner_rtol, int inner_max_iter);
+/* change the stopping tolerances of an existing solver */
+int ntg_ksp_set_tol(ntg_ksp* ksp, double rtol, double abstol);
+/* guess guard (default off): when the initial guess's residual exceeds the
+   right-hand side's norm, restart from a zero guess and report
+   NTG_GUESS_REJECTED in ntg_monitor.guess_rejected */
+int ntg_ksp_set_guess_guard(ntg_ksp* ksp, int on);
 /* how many iterations run between host convergence checks (default 16) */
 int ntg_ksp_set_check_every(ntg_ksp* ksp, int every);
 /* x_d: initial guess in, solution out.  f_d: assembled, masked RHS. */
@@ -228,6 +240,37 @@ int ntg_proj_pre_solving(ntg_proj* proj, double* b_d);
    one FP64 operator application updates the basis */
 int ntg_proj_post_solving(ntg_proj* proj, double* x_d);
 int ntg_proj_size(const ntg_proj* proj);
+
+/* ---------------------------------------------------------------------- */
+/* learned initial guess (new; the reference has no learned part).  A      */
+/* per-element MLP, (history + 1) * lx^3 -> hidden -> hidden -> lx^3, BF16 */
+/* weights and tensor-core GEMMs with FP32 accumulation, trained online    */
+/* with Adam on the solver's own solutions.  Inserted where the reference  */
+/* sets the initial guess: projection pre_solving                          */
+/* (sources/adjoint/adjoint_pnpn.f90:729) and the filter's guess copy      */
+/* (sources/mapping_functions/PDE_filter_mapping.f90:246,332).             */
+/* ---------------------------------------------------------------------- */
+int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg_guess** guess);
+int ntg_guess_destroy(ntg_guess* guess);
+int ntg_guess_set_lr(ntg_guess* guess, double lr);
+/* guess for the rhs b_d from the stored solution history; *ready = 0 (and
+   x_d untouched) until `history` solutions have been observed.  The guess
+   is continuous (mult-averaged over shared nodes) and zero on the mask. */
+int ntg_guess_predict(ntg_guess* guess, const double* b_d, double* x_d, int* ready);
+/* record the solution x_d of rhs b_d: with train_steps > 0 (and a full
+   history) first take that many Adam steps on (history, b) -> x, then push
+   x into the history.  *loss = the last training loss (-1 if none). */
+int ntg_guess_observe(ntg_guess* guess, const double* b_d, const double* x_d, int train_steps, double* loss);
+int ntg_guess_reset_history(ntg_guess* guess);
+/* parameters as one flat FP32 array [W1 | b1 | W2 | b2 | W3 | b3] (W row
+   major, [in x out]); set != 0 writes them */
+int64_t ntg_guess_num_params(const ntg_guess* guess);
+int ntg_guess_params(ntg_guess* guess, float* params_d, int set);
+/* raw access for gradient checks: X_d rows are BF16 bit patterns */
+int ntg_guess_forward_raw(ntg_guess* guess, const uint16_t* X_d, int64_t E, float* Y_d);
+int ntg_guess_grad_raw(ntg_guess* guess, const uint16_t* X_d, const float* T_d, int64_t E, float* grad_d,
+                       double* loss);
+int ntg_guess_train_raw(ntg_guess* guess, const uint16_t* X_d, const float* T_d, int64_t E, double* loss);
 
 /* ---------------------------------------------------------------------- */
 /* dot products (FP64 accumulation, deterministic order)                   */

@@ -24,7 +24,7 @@ _pd = C.POINTER(C.c_double)
 class ntg_monitor(C.Structure):
     _fields_ = [("iter", C.c_int), ("inner_iter", C.c_int), ("res_start", C.c_double),
                 ("res_final", C.c_double), ("rhs_norm", C.c_double), ("status", C.c_int),
-                ("fp64_ax", C.c_int)]
+                ("fp64_ax", C.c_int), ("guess_rejected", C.c_int)]
 
 
 class NtgError(RuntimeError):
@@ -58,6 +58,9 @@ SIGNATURES = {
     "ntg_field_uniform": (_i, [_vp, _i64, C.c_uint64, C.c_uint64, _d, _d, _vp, _vp]),
     "ntg_field_fourier": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, _i, _i, C.c_uint64, _vp, _vp]),
     "ntg_field_blobs": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, C.c_uint64, _i, _d, _vp, _vp]),
+    "ntg_field_modes": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, _i, _pi, _pd, _pd, _vp, _vp]),
+    "ntg_ksp_set_guess_guard": (_i, [_vp, _i]),
+    "ntg_ksp_set_tol": (_i, [_vp, _d, _d]),
     "ntg_rhs_assemble": (_i, [_vp, _vp, _vp]),
     "ntg_ax_helm": (_i, [_vp, _vp, _vp]),
     "ntg_ax_helm_f32": (_i, [_vp, _vp, _vp]),
@@ -79,6 +82,17 @@ SIGNATURES = {
     "ntg_proj_post_solving": (_i, [_vp, _vp]),
     "ntg_proj_size": (_i, [_vp]),
     "ntg_glsc3": (_i, [_vp, _vp, _vp, _vp, _i64, _pd]),
+    "ntg_guess_create": (_i, [_vp, _i, _i, C.c_uint64, C.POINTER(_vp)]),
+    "ntg_guess_destroy": (_i, [_vp]),
+    "ntg_guess_set_lr": (_i, [_vp, _d]),
+    "ntg_guess_predict": (_i, [_vp, _vp, _vp, _pi]),
+    "ntg_guess_observe": (_i, [_vp, _vp, _vp, _i, _pd]),
+    "ntg_guess_reset_history": (_i, [_vp]),
+    "ntg_guess_num_params": (_i64, [_vp]),
+    "ntg_guess_params": (_i, [_vp, _vp, _i]),
+    "ntg_guess_forward_raw": (_i, [_vp, _vp, _i64, _vp]),
+    "ntg_guess_grad_raw": (_i, [_vp, _vp, _vp, _i64, _vp, _pd]),
+    "ntg_guess_train_raw": (_i, [_vp, _vp, _vp, _i64, _pd]),
     "ntg_ramp_forward": (_i, [_vp, _vp, _i64, _d, _d, _d, _i, _vp]),
     "ntg_ramp_backward": (_i, [_vp, _vp, _vp, _i64, _d, _d, _d, _i, _vp]),
     "ntg_brinkman_compute": (_i, [_vp] * 7 + [_i64, _vp, _i64, _i, _vp]),

@@ -47,10 +47,12 @@ class ksp_monitor_t:
     status: int
     inner_iter: int = 0
     fp64_ax: int = 0
+    guess_rejected: int = 0
 
     @classmethod
     def from_c(cls, m: ntg_monitor):
-        return cls(m.iter, m.res_start, m.res_final, m.rhs_norm, m.status, m.inner_iter, m.fp64_ax)
+        return cls(m.iter, m.res_start, m.res_final, m.rhs_norm, m.status, m.inner_iter, m.fp64_ax,
+                   m.guess_rejected)
 
 
 def mask_face_xmax(ex, ey, ez, lx, device="cuda"):
@@ -149,6 +151,19 @@ class coef_t:
         lo3, hi3 = (C.c_double * 3)(*self.lo), (C.c_double * 3)(*self.hi)
         check(lib().ntg_field_blobs(_ptr(self.x), _ptr(self.y), _ptr(self.z), self.n, lo3, hi3, int(seed),
                                     int(nblobs), float(width), _ptr(f), _stream()))
+        return f
+
+    def field_modes(self, k, amp, ph):
+        """Fourier modes with explicit parameters (k: 3*m ints, amp, ph)."""
+        import numpy as np
+        k = np.ascontiguousarray(k, dtype=np.int32).ravel()
+        amp = np.ascontiguousarray(amp, dtype=np.float64)
+        ph = np.ascontiguousarray(ph, dtype=np.float64)
+        f = torch.empty(self.n, dtype=torch.float64, device=self.device)
+        lo3, hi3 = (C.c_double * 3)(*self.lo), (C.c_double * 3)(*self.hi)
+        check(lib().ntg_field_modes(_ptr(self.x), _ptr(self.y), _ptr(self.z), self.n, lo3, hi3, len(amp),
+                                    k.ctypes.data_as(C.POINTER(C.c_int)), amp.ctypes.data_as(C.POINTER(C.c_double)),
+                                    ph.ctypes.data_as(C.POINTER(C.c_double)), _ptr(f), _stream()))
         return f
 
     def rhs_assemble(self, f):
@@ -258,6 +273,13 @@ class _ksp:
     def set_check_every(self, k):
         check(lib().ntg_ksp_set_check_every(self._h, int(k)))
 
+    def set_tol(self, rtol, abstol):
+        check(lib().ntg_ksp_set_tol(self._h, float(rtol), float(abstol)))
+
+    def set_guess_guard(self, on=True):
+        """Restart from zero when the initial guess's residual exceeds ||f||."""
+        check(lib().ntg_ksp_set_guess_guard(self._h, int(bool(on))))
+
     def solve(self, x, f) -> ksp_monitor_t:
         """ksp%solve(Ax, x, f, n, coef, blst, gs): x = guess in, solution out;
         f = assembled, masked RHS."""
@@ -327,6 +349,149 @@ class projection_t:
             self.free()
         except Exception:
             pass
+
+
+class learned_guess_t:
+    """Per-element MLP initial guess, trained online on the solver's own
+    solutions (BF16 tensor-core GEMMs, FP32 accumulate, Adam)."""
+
+    def __init__(self, coef: coef_t, history=4, hidden=64, seed=0, lr=1e-3):
+        self.coef = coef
+        h = C.c_void_p()
+        check(lib().ntg_guess_create(coef.handle, int(history), int(hidden), int(seed), C.byref(h)))
+        self._h = h
+        self.history, self.hidden = history, hidden
+        self.F = (history + 1) * coef.lx ** 3
+        self.O = coef.lx ** 3
+        check(lib().ntg_guess_set_lr(h, float(lr)))
+
+    def predict(self, b, x):
+        """Write the guess for rhs b into x; False until the history is full."""
+        ready = C.c_int()
+        check(lib().ntg_guess_predict(self._h, _ptr(b, n=self.coef.n), _ptr(x, n=self.coef.n), C.byref(ready)))
+        return bool(ready.value)
+
+    def observe(self, b, x, train_steps=0):
+        loss = C.c_double()
+        check(lib().ntg_guess_observe(self._h, _ptr(b, n=self.coef.n), _ptr(x, n=self.coef.n), int(train_steps),
+                                      C.byref(loss)))
+        return loss.value
+
+    def reset_history(self):
+        check(lib().ntg_guess_reset_history(self._h))
+
+    @property
+    def num_params(self):
+        return int(lib().ntg_guess_num_params(self._h))
+
+    def get_params(self):
+        p = torch.empty(self.num_params, dtype=torch.float32, device=self.coef.device)
+        check(lib().ntg_guess_params(self._h, _ptr(p, torch.float32), 0))
+        torch.cuda.synchronize()
+        return p
+
+    def set_params(self, p):
+        check(lib().ntg_guess_params(self._h, _ptr(p, torch.float32, self.num_params, "params"), 1))
+
+    # raw network access (X: int16 tensor of BF16 bit patterns, [E, F])
+    def forward_raw(self, Xbits, E):
+        Y = torch.empty(E * self.O, dtype=torch.float32, device=self.coef.device)
+        check(lib().ntg_guess_forward_raw(self._h, C.c_void_p(Xbits.data_ptr()), int(E), _ptr(Y, torch.float32)))
+        torch.cuda.synchronize()
+        return Y.view(E, self.O)
+
+    def grad_raw(self, Xbits, T, E):
+        g = torch.empty(self.num_params, dtype=torch.float32, device=self.coef.device)
+        loss = C.c_double()
+        check(lib().ntg_guess_grad_raw(self._h, C.c_void_p(Xbits.data_ptr()), _ptr(T, torch.float32), int(E),
+                                       _ptr(g, torch.float32), C.byref(loss)))
+        torch.cuda.synchronize()
+        return loss.value, g
+
+    def train_raw(self, Xbits, T, E):
+        loss = C.c_double()
+        check(lib().ntg_guess_train_raw(self._h, C.c_void_p(Xbits.data_ptr()), _ptr(T, torch.float32), int(E),
+                                        C.byref(loss)))
+        return loss.value
+
+    def free(self):
+        if self._h is not None:
+            check(lib().ntg_guess_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def ar1_modes(seed, nmodes, nsolves, rho=0.98, kmax=4):
+    """Mode parameters of a right-hand-side sequence: integer wave vectors in
+    [1, kmax]^3 and phases fixed per mode, amplitudes c_m(t)/|k_m|^2 with
+    c_m an AR(1) process c(t+1) = rho c(t) + sqrt(1 - rho^2) eps (standard
+    normal innovations, seeded).  Returns (k [3*nmodes], phases, amps
+    [nsolves x nmodes])."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    k = rng.integers(1, kmax + 1, size=(nmodes, 3)).astype(np.int32)
+    ph = rng.uniform(0, 2 * np.pi, nmodes)
+    kk = (k.astype(np.float64) ** 2).sum(1)
+    c = np.empty((nsolves, nmodes))
+    c[0] = rng.standard_normal(nmodes)
+    s = np.sqrt(1 - rho * rho)
+    for t in range(1, nsolves):
+        c[t] = rho * c[t - 1] + s * rng.standard_normal(nmodes)
+    return k.ravel(), ph, c / kk
+
+
+class SolveSequence:
+    """Solve-sequence driver in the reference's order
+    (sources/adjoint/adjoint_pnpn.f90:714-743): the caller's RHS is already
+    gs-assembled and masked; then initial guess (zero, Fischer projection or
+    the learned guess) -> pc update -> ksp solve -> projection post / history
+    update.  Every solve converges to the same relative tolerance whatever the
+    guess; a learned guess worse than zero is rejected by the ksp's guard."""
+
+    def __init__(self, coef: coef_t, method="cg_mixed", guess="zero", rtol=1e-10, max_iter=50000, L=20,
+                 history=4, hidden=64, seed=0, lr=1e-3, train_steps=20):
+        self.coef, self.guess, self.rtol = coef, guess, rtol
+        self.ksp = krylov_solver_factory(coef, method, max_iter, rtol)
+        self.proj = projection_t(coef, L) if guess == "projection" else None
+        self.net = learned_guess_t(coef, history, hidden, seed, lr) if guess == "learned" else None
+        if self.net is not None:
+            self.ksp.set_guess_guard(True)
+        self.train_steps = train_steps
+        self.training = True
+        self.x = torch.zeros(coef.n, dtype=torch.float64, device=coef.device)
+
+    def solve(self, f):
+        x = self.x
+        x.zero_()
+        used = "zero"
+        if self.proj is not None:
+            # the reduced system's tolerance stays relative to the original RHS
+            b = f.clone()
+            fn = glsc3(self.coef, f, f, self._mult()) ** 0.5
+            self.proj.pre_solving(b)
+            self.ksp.set_tol(0.0, self.rtol * fn)
+            mon = self.ksp.solve(x, b)
+            self.proj.post_solving(x)
+            used = "projection"
+        else:
+            if self.net is not None and self.net.predict(f, x):
+                used = "learned"
+            mon = self.ksp.solve(x, f)
+            if mon.guess_rejected:
+                used = "zero (learned rejected)"
+            if self.net is not None:
+                self.net.observe(f, x, self.train_steps if self.training else 0)
+        return x, mon, used
+
+    def _mult(self):
+        if not hasattr(self, "_mult_t"):
+            self._mult_t = self.coef.geometry()["mult"]
+        return self._mult_t
 
 
 def glsc3(coef: coef_t, a, b, c=None) -> float:

@@ -553,6 +553,7 @@ struct ntg_ksp {
   double inner_rtol = 1e-4;
   int inner_max_iter = 400;
   int check_every = 16;
+  int guess_guard = 0;
   // FP64 workspace
   ntg::PcgVecs<double> v64;
   double *pd = nullptr, *qd = nullptr, *pprev = nullptr, *qprev = nullptr;
@@ -907,13 +908,53 @@ int ntg_ksp_set_check_every(ntg_ksp* ksp, int every) {
   return NTG_OK;
 }
 
+int ntg_ksp_set_tol(ntg_ksp* ksp, double rtol, double abstol) {
+  clear_error();
+  NTG_CHECK_ARG(ksp && rtol >= 0 && abstol >= 0, "ntg_ksp_set_tol: bad argument");
+  ksp->rtol = rtol;
+  ksp->abstol = abstol;
+  return NTG_OK;
+}
+
+int ntg_ksp_set_guess_guard(ntg_ksp* ksp, int on) {
+  clear_error();
+  NTG_CHECK_ARG(ksp, "ntg_ksp_set_guess_guard: null argument");
+  ksp->guess_guard = on ? 1 : 0;
+  return NTG_OK;
+}
+
 int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon) {
   clear_error();
   NTG_CHECK_ARG(ksp && x_d && f_d, "ntg_ksp_solve: null argument");
   if (mon) memset(mon, 0, sizeof(*mon));
-  if (ksp->type == NTG_KSP_FCG_MIXED) return ksp_solve_mixed(ksp, x_d, f_d, mon);
-  if (ksp->type == NTG_KSP_CG_MIXED) return ksp_solve_mixed_ru(ksp, x_d, f_d, mon);
-  return ksp_solve_cg(ksp, x_d, f_d, mon);
+  int rejected = 0;
+  if (ksp->guess_guard) {
+    // a guess is kept only if its residual is below ||f||: one FP64
+    // operator application and two dots decide
+    ntg_plan* p = ksp->plan;
+    cudaStream_t s = p->stream;
+    double xx = 0.0;
+    NTG_TRY(wdot(p, x_d, x_d, nullptr, p->n, &xx, s));
+    if (xx != 0.0) {
+      NTG_TRY(op_apply(p, ksp->v64.w, x_d, s));
+      { k_resid<<<grid_for(p->n, 256), 256, 0, s>>>(f_d, ksp->v64.w, p->mult, ksp->v64.r, p->n, p->red_part, ksp->sc); NTG_COUNT_LAUNCH(); }
+      NTG_CUDA_TRY(cudaMemcpyAsync(ksp->hs, ksp->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+      NTG_CUDA_TRY(cudaStreamSynchronize(s));
+      if (!(ksp->hs->rr <= ksp->hs->ff)) {
+        NTG_CUDA_TRY(cudaMemsetAsync(x_d, 0, sizeof(double) * p->n, s));
+        rejected = 1;
+      }
+    }
+  }
+  int st = NTG_OK;
+  if (ksp->type == NTG_KSP_FCG_MIXED) st = ksp_solve_mixed(ksp, x_d, f_d, mon);
+  else if (ksp->type == NTG_KSP_CG_MIXED) st = ksp_solve_mixed_ru(ksp, x_d, f_d, mon);
+  else st = ksp_solve_cg(ksp, x_d, f_d, mon);
+  if (mon) {
+    mon->guess_rejected = rejected;
+    if (rejected) mon->fp64_ax += 1;
+  }
+  return st;
 }
 
 int ntg_ksp_solve_coupled(ntg_ksp* ksp, double* x_d, double* y_d, double* z_d, const double* fx_d,

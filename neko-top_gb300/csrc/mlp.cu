@@ -1,0 +1,611 @@
+// Learned initial guess: a per-element MLP trained online on the solver's own
+// solutions, with hand-written BF16 tensor-core GEMMs (FP32 accumulate) for
+// the forward pass, the backward pass and an Adam update.
+//
+// Insertion points in the reference: the initial guess of the pressure /
+// filter solves -- projection pre_solving at sources/adjoint/adjoint_pnpn.f90:729
+// and the filter's guess copy at sources/mapping_functions/PDE_filter_mapping.f90:246,332.
+// The reference has no learned part; this is new.
+//
+// Network (per element, rows = elements):
+//   X [E x 5*512]  = last 4 solutions / s and the right-hand side / s_b on the
+//                    element's 512 nodes (BF16)
+//   H1 = relu(X W1 + b1)   [E x 64]
+//   H2 = relu(H1 W2 + b2)  [E x 64]
+//   Y  = H2 W3 + b3        [E x 512]   ->  guess = s * Y, made continuous by
+//                                          the mult-weighted gather-scatter
+// Loss: mean squared error against the solved x / s.
+//
+// GEMMs: one tiled kernel, C = op(A) op(B) with arbitrary strides (so the
+// transposes of the backward pass need no copies), 64x64x32 tiles, 4 warps of
+// mma.sync m16n8k16 BF16 -> FP32, optional split-K whose partials are summed in
+// a fixed order (deterministic), epilogue bias / ReLU / BF16 copy.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "reduce.cuh"
+
+namespace ntg {
+
+namespace mlp {
+
+constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+constexpr int GT = 128;  // 4 warps
+
+struct GemmArgs {
+  const __nv_bfloat16* A;
+  int64_t lda_m, lda_k;
+  const __nv_bfloat16* B;
+  int64_t ldb_k, ldb_n;
+  float* C;             // fp32 output (row-major, ldc), or split-K partials
+  int64_t ldc;
+  int64_t split_stride; // elements between split-K partial matrices
+  __nv_bfloat16* Cb;    // optional bf16 copy (row-major, ldc)
+  const float* bias;    // optional, per column
+  int relu;
+  int64_t M, N, K, kchunk;
+};
+
+__device__ __forceinline__ unsigned su32(const void* p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void ldm_x4(unsigned (&r)[4], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(su32(p)));
+}
+__device__ __forceinline__ void ldm_x2(unsigned (&r)[2], const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(su32(p)));
+}
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(GT) k_gemm_bf16(GemmArgs g) {
+  __shared__ __align__(16) __nv_bfloat16 sA[BM][BK + PAD];
+  __shared__ __align__(16) __nv_bfloat16 sB[BN][BK + PAD];  // n-major, k contiguous
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 1, wn = warp & 1;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  const int64_t kbeg = (int64_t)blockIdx.z * g.kchunk;
+  int64_t kend = kbeg + g.kchunk;
+  if (kend > g.K) kend = g.K;
+  float acc[2][4][4];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
+    // load tiles: BM*BK = 2048 elements each, 16 per thread
+#pragma unroll 4
+    for (int q = 0; q < (BM * BK) / GT; ++q) {
+      const int e = q * GT + tid;
+      // A: walk m fastest when A is column-major (lda_m == 1), else k fastest
+      int mm, kk;
+      if (g.lda_m == 1) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
+      const int64_t gm = m0 + mm, gk = k0 + kk;
+      sA[mm][kk] = (gm < g.M && gk < kend) ? g.A[gm * g.lda_m + gk * g.lda_k] : zero;
+      int nn, kb;
+      if (g.ldb_n == 1) { nn = e % BN; kb = e / BN; } else { kb = e % BK; nn = e / BK; }
+      const int64_t gn = n0 + nn, gkb = k0 + kb;
+      sB[nn][kb] = (gn < g.N && gkb < kend) ? g.B[gkb * g.ldb_k + gn * g.ldb_n] : zero;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < BK; ks += 16) {
+      unsigned af[2][4], bf[4][2];
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi) ldm_x4(af[mi], &sA[wm * 32 + mi * 16 + (lane & 15)][ks + (lane >> 4) * 8]);
+#pragma unroll
+      for (int ni = 0; ni < 4; ++ni) ldm_x2(bf[ni], &sB[wn * 32 + ni * 8 + (lane & 7)][ks + ((lane >> 3) & 1) * 8]);
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], af[mi], bf[ni]);
+    }
+    __syncthreads();
+  }
+  // epilogue
+  float* C = g.C + (int64_t)blockIdx.z * g.split_stride;
+  const int gr = lane >> 2, gc = (lane & 3) * 2;
+#pragma unroll
+  for (int mi = 0; mi < 2; ++mi)
+#pragma unroll
+    for (int ni = 0; ni < 4; ++ni)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int64_t row = m0 + wm * 32 + mi * 16 + gr + h * 8;
+        if (row >= g.M) continue;
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+          const int64_t col = n0 + wn * 32 + ni * 8 + gc + cc;
+          if (col >= g.N) continue;
+          float v = acc[mi][ni][h * 2 + cc];
+          if (g.bias) v += g.bias[col];
+          if (g.relu) v = v > 0.f ? v : 0.f;
+          if (C) C[row * g.ldc + col] = v;
+          if (g.Cb) g.Cb[row * g.ldc + col] = __float2bfloat16(v);
+        }
+      }
+}
+
+// sum of S split-K partials (fixed order) -> out
+__global__ void k_sum_splits(const float* __restrict__ part, int S, int64_t len, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < S; ++z) s += part[(int64_t)z * len + i];
+    out[i] = s;
+  }
+}
+
+// column sums of a row-major [M x N] fp32 matrix, deterministic: block per
+// column chunk, fixed row partition, fixed tree
+__global__ void k_colsum(const float* __restrict__ a, int64_t M, int N, float* __restrict__ out) {
+  __shared__ float red[8][32];
+  const int col = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int rw = threadIdx.x >> 5;  // 8 row lanes
+  float s = 0.f;
+  if (col < N)
+    for (int64_t r = rw; r < M; r += 8) s += a[r * N + col];
+  red[rw][threadIdx.x & 31] = s;
+  __syncthreads();
+  if (rw == 0 && col < N) {
+    float t = 0.f;
+    for (int q = 0; q < 8; ++q) t += red[q][threadIdx.x & 31];
+    out[col] = t;
+  }
+}
+
+// X[m][f*512 + node] = bf16(field_f[m*512 + node] * scale_f), f < nf
+struct PrepArgs {
+  const float* hist[8];
+  const double* b;
+  float scale[8];
+  float bscale;
+  int nhist;
+};
+__global__ void k_prep_x(PrepArgs pa, int64_t E, int lx3, __nv_bfloat16* __restrict__ X) {
+  const int F = (pa.nhist + 1) * lx3;
+  const int64_t total = E * F;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = i / F;
+    const int k = (int)(i - m * F);
+    const int f = k / lx3, node = k - f * lx3;
+    const int64_t l = m * lx3 + node;
+    float v = f < pa.nhist ? pa.hist[f][l] * pa.scale[f] : (float)(pa.b[l] * pa.bscale);
+    X[i] = __float2bfloat16(v);
+  }
+}
+
+// dY = (Y - T) * g ; bf16 copy; per-thread squared error sums -> loss
+struct FinLoss {
+  __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[1] = acc[0]; }
+};
+__global__ void k_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, int64_t len, float g,
+                            __nv_bfloat16* __restrict__ dYb, float* __restrict__ dY, double* __restrict__ part,
+                            Scalars* sc) {
+  float s = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    const float d = Y[i] - T[i];
+    s += d * d;
+    const float gd = d * g;
+    dY[i] = gd;
+    dYb[i] = __float2bfloat16(gd);
+  }
+  double v[1] = {(double)s};
+  grid_reduce<1>(v, part, sc, FinLoss());
+}
+
+// dZ = dH * (H > 0), bf16 copy
+__global__ void k_relu_back(const float* __restrict__ dH, const __nv_bfloat16* __restrict__ H, int64_t len,
+                            float* __restrict__ dZ, __nv_bfloat16* __restrict__ dZb) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = __bfloat162float(H[i]) > 0.f ? dH[i] : 0.f;
+    dZ[i] = v;
+    dZb[i] = __float2bfloat16(v);
+  }
+}
+
+// Adam (bias-corrected), FP32 master weights, BF16 copy for the GEMMs
+__global__ void k_adam(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ gr,
+                       float* __restrict__ m1, float* __restrict__ m2, int64_t len, float lr, float b1, float b2,
+                       float c1, float c2, float eps) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gg = gr[i];
+    const float a = b1 * m1[i] + (1.f - b1) * gg;
+    const float b = b2 * m2[i] + (1.f - b2) * gg * gg;
+    m1[i] = a;
+    m2[i] = b;
+    const float v = w[i] - lr * (a * c1) / (sqrtf(b * c2) + eps);
+    w[i] = v;
+    if (wb) wb[i] = __float2bfloat16(v);
+  }
+}
+
+__global__ void k_f2bf(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = __float2bfloat16(a[i]);
+}
+
+// guess_local = s * Y (element-local, doubles) times mult, for the averaging gs
+__global__ void k_scale_out(const float* __restrict__ Y, const double* __restrict__ mult, double s, int64_t n,
+                            double* __restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = s * (double)Y[i] * mult[i];
+}
+// target T = x / s (float); history push h = x (float)
+__global__ void k_target(const double* __restrict__ x, double inv_s, int64_t n, float* __restrict__ T,
+                         float* __restrict__ h) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    T[i] = (float)(x[i] * inv_s);
+    if (h) h[i] = (float)x[i];
+  }
+}
+// sum of squares of a float / double array (RMS scales), deterministic
+struct FinSlot2 {
+  __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[2] = acc[0]; }
+};
+template <typename T>
+__global__ void k_sumsq(const T* __restrict__ a, int64_t n, double* __restrict__ part, Scalars* sc) {
+  float s = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = (float)a[i];
+    s += v * v;
+  }
+  double v[1] = {(double)s};
+  grid_reduce<1>(v, part, sc, FinSlot2());
+}
+
+}  // namespace mlp
+
+}  // namespace ntg
+
+struct ntg_guess {
+  ntg_plan* plan = nullptr;
+  int nhist = 4, H = 64, F = 0, O = 0, lx3 = 0;
+  int64_t E = 0, n = 0;
+  // parameters: flat FP32 [W1 F*H | b1 H | W2 H*H | b2 H | W3 H*O | b3 O]
+  int64_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0, np = 0;
+  float *P = nullptr, *G = nullptr, *m1 = nullptr, *m2 = nullptr;
+  __nv_bfloat16* Pb = nullptr;
+  // activations
+  __nv_bfloat16 *X = nullptr, *H1b = nullptr, *H2b = nullptr, *dYb = nullptr, *dZb = nullptr;
+  float *Y = nullptr, *T = nullptr, *dY = nullptr, *dH = nullptr, *dZ = nullptr, *split = nullptr;
+  int splits = 16;
+  // history ring of solutions (FP32), newest at hist[(head - 1) mod nhist]
+  float* hist[8] = {};
+  double hrms[8] = {};
+  int hcount = 0, head = 0;
+  double* xloc = nullptr;
+  ntg::Scalars* sc = nullptr;
+  ntg::Scalars* hs = nullptr;  // pinned
+  long long t = 0;
+  float lr = 1e-3f, beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
+};
+
+using namespace ntg;
+using namespace ntg::mlp;
+
+static void guess_free(ntg_guess* g) {
+  dev_free(g->P); dev_free(g->G); dev_free(g->m1); dev_free(g->m2); dev_free(g->Pb);
+  dev_free(g->X); dev_free(g->H1b); dev_free(g->H2b); dev_free(g->dYb); dev_free(g->dZb);
+  dev_free(g->Y); dev_free(g->T); dev_free(g->dY); dev_free(g->dH); dev_free(g->dZ); dev_free(g->split);
+  for (int i = 0; i < 8; ++i) dev_free(g->hist[i]);
+  dev_free(g->xloc); dev_free(g->sc);
+  if (g->hs) cudaFreeHost(g->hs);
+  g->hs = nullptr;
+}
+
+static int gemm(ntg_guess* g, const __nv_bfloat16* A, int64_t lda_m, int64_t lda_k, const __nv_bfloat16* B,
+                int64_t ldb_k, int64_t ldb_n, float* C, __nv_bfloat16* Cb, const float* bias, int relu, int64_t M,
+                int64_t N, int64_t K, int splits, float* out_after_split) {
+  cudaStream_t s = g->plan->stream;
+  GemmArgs a;
+  a.A = A; a.lda_m = lda_m; a.lda_k = lda_k;
+  a.B = B; a.ldb_k = ldb_k; a.ldb_n = ldb_n;
+  a.ldc = N;
+  a.Cb = Cb; a.bias = bias; a.relu = relu;
+  a.M = M; a.N = N; a.K = K;
+  if (splits > 1) {
+    int64_t kc = (K + splits - 1) / splits;
+    kc = (kc + BK - 1) / BK * BK;
+    splits = (int)((K + kc - 1) / kc);
+    a.kchunk = kc;
+    a.C = g->split;
+    a.split_stride = M * N;
+    a.Cb = nullptr; a.bias = nullptr; a.relu = 0;
+  } else {
+    a.kchunk = (K + BK - 1) / BK * BK;
+    a.C = C;
+    a.split_stride = 0;
+    splits = 1;
+  }
+  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)splits);
+  { k_gemm_bf16<<<grid, GT, 0, s>>>(a); NTG_COUNT_LAUNCH(); }
+  if (a.C == g->split) {
+    { k_sum_splits<<<grid_for(M * N, 256), 256, 0, s>>>(g->split, splits, M * N, out_after_split); NTG_COUNT_LAUNCH(); }
+  }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+// forward on E rows of X -> Y (fp32), keeping H1b/H2b for the backward pass
+static int guess_forward(ntg_guess* g, const __nv_bfloat16* X, int64_t E) {
+  const int H = g->H;
+  NTG_TRY(gemm(g, X, g->F, 1, g->Pb + g->oW1, H, 1, nullptr, g->H1b, g->P + g->ob1, 1, E, H, g->F, 1, nullptr));
+  NTG_TRY(gemm(g, g->H1b, H, 1, g->Pb + g->oW2, H, 1, nullptr, g->H2b, g->P + g->ob2, 1, E, H, H, 1, nullptr));
+  NTG_TRY(gemm(g, g->H2b, H, 1, g->Pb + g->oW3, g->O, 1, g->Y, nullptr, g->P + g->ob3, 0, E, g->O, H, 1, nullptr));
+  return NTG_OK;
+}
+
+// loss and gradients into G for targets T (after guess_forward on X)
+static int guess_backward(ntg_guess* g, const __nv_bfloat16* X, const float* T, int64_t E) {
+  cudaStream_t s = g->plan->stream;
+  const int H = g->H, O = g->O;
+  const int64_t len = E * O;
+  { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, 2.0f / (float)len, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  // layer 3
+  NTG_TRY(gemm(g, g->H2b, 1, H, g->dYb, O, 1, nullptr, nullptr, nullptr, 0, H, O, E, g->splits, g->G + g->oW3));
+  { k_colsum<<<(O + 31) / 32, 256, 0, s>>>(g->dY, E, O, g->G + g->ob3); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(gemm(g, g->dYb, O, 1, g->Pb + g->oW3, 1, O, g->dH, nullptr, nullptr, 0, E, H, O, 1, nullptr));
+  { k_relu_back<<<grid_for(E * H, 256), 256, 0, s>>>(g->dH, g->H2b, E * H, g->dZ, g->dZb); NTG_COUNT_LAUNCH(); }
+  // layer 2
+  NTG_TRY(gemm(g, g->H1b, 1, H, g->dZb, H, 1, nullptr, nullptr, nullptr, 0, H, H, E, g->splits, g->G + g->oW2));
+  { k_colsum<<<(H + 31) / 32, 256, 0, s>>>(g->dZ, E, H, g->G + g->ob2); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(gemm(g, g->dZb, H, 1, g->Pb + g->oW2, 1, H, g->dH, nullptr, nullptr, 0, E, H, H, 1, nullptr));
+  { k_relu_back<<<grid_for(E * H, 256), 256, 0, s>>>(g->dH, g->H1b, E * H, g->dZ, g->dZb); NTG_COUNT_LAUNCH(); }
+  // layer 1
+  NTG_TRY(gemm(g, X, 1, g->F, g->dZb, H, 1, nullptr, nullptr, nullptr, 0, g->F, H, E, g->splits, g->G + g->oW1));
+  { k_colsum<<<(H + 31) / 32, 256, 0, s>>>(g->dZ, E, H, g->G + g->ob1); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+static int guess_adam(ntg_guess* g) {
+  g->t += 1;
+  const float c1 = 1.0f / (1.0f - powf(g->beta1, (float)g->t));
+  const float c2 = 1.0f / (1.0f - powf(g->beta2, (float)g->t));
+  { k_adam<<<grid_for(g->np, 256), 256, 0, g->plan->stream>>>(g->P, g->Pb, g->G, g->m1, g->m2, g->np, g->lr, g->beta1, g->beta2, c1, c2, g->eps); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+static int poll_red(ntg_guess* g, int slot, double* out) {
+  cudaStream_t s = g->plan->stream;
+  NTG_CUDA_TRY(cudaMemcpyAsync(g->hs, g->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  *out = g->hs->red[slot];
+  return NTG_OK;
+}
+
+// X from the history (newest first) and b, with RMS scalings
+static int build_x(ntg_guess* g, const double* b, double* s_out) {
+  cudaStream_t s = g->plan->stream;
+  double bb = 0;
+  { k_sumsq<double><<<grid_for(g->n, 256), 256, 0, s>>>(b, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(poll_red(g, 2, &bb));
+  const double sb = sqrt(bb / (double)g->n);
+  const int newest = (g->head - 1 + g->nhist) % g->nhist;
+  double sx = g->hrms[newest];
+  if (!(sx > 0)) sx = 1.0;
+  PrepArgs pa;
+  pa.nhist = g->nhist;
+  for (int f = 0; f < g->nhist; ++f) {
+    const int slot = (g->head - 1 - f + 2 * g->nhist) % g->nhist;
+    pa.hist[f] = g->hist[slot];
+    pa.scale[f] = (float)(1.0 / sx);
+  }
+  pa.b = b;
+  pa.bscale = (float)(sb > 0 ? 1.0 / sb : 1.0);
+  { k_prep_x<<<grid_for(g->E * g->F, 256), 256, 0, s>>>(pa, g->E, g->lx3, g->X); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  *s_out = sx;
+  return NTG_OK;
+}
+
+extern "C" {
+
+int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg_guess** out) {
+  clear_error();
+  NTG_CHECK_ARG(plan && out, "ntg_guess_create: null argument");
+  NTG_CHECK_ARG(history >= 1 && history <= 7, "ntg_guess_create: history must be in [1, 7]");
+  NTG_CHECK_ARG(hidden >= 8 && hidden <= 512, "ntg_guess_create: hidden must be in [8, 512]");
+  *out = nullptr;
+  ntg_guess* g = new ntg_guess();
+  g->plan = plan;
+  g->nhist = history;
+  g->H = hidden;
+  g->lx3 = plan->lx * plan->lx * plan->lx;
+  g->F = (history + 1) * g->lx3;
+  g->O = g->lx3;
+  g->E = plan->nelv;
+  g->n = plan->n;
+  const int64_t F = g->F, H = g->H, O = g->O, E = g->E;
+  g->oW1 = 0; g->ob1 = F * H; g->oW2 = g->ob1 + H; g->ob2 = g->oW2 + H * H; g->oW3 = g->ob2 + H;
+  g->ob3 = g->oW3 + H * O; g->np = g->ob3 + O;
+  int st = NTG_OK;
+  do {
+    if ((st = dev_alloc(&g->P, g->np)) || (st = dev_alloc(&g->G, g->np)) || (st = dev_alloc(&g->m1, g->np)) ||
+        (st = dev_alloc(&g->m2, g->np)) || (st = dev_alloc(&g->Pb, g->np)))
+      break;
+    if ((st = dev_alloc(&g->X, E * F)) || (st = dev_alloc(&g->H1b, E * H)) || (st = dev_alloc(&g->H2b, E * H)) ||
+        (st = dev_alloc(&g->dYb, E * O)) || (st = dev_alloc(&g->dZb, E * H)) || (st = dev_alloc(&g->Y, E * O)) ||
+        (st = dev_alloc(&g->T, E * O)) || (st = dev_alloc(&g->dY, E * O)) || (st = dev_alloc(&g->dH, E * H)) ||
+        (st = dev_alloc(&g->dZ, E * H)))
+      break;
+    const int64_t split_len = (int64_t)g->splits * std::max(F * H, H * O);
+    if ((st = dev_alloc(&g->split, split_len))) break;
+    for (int i = 0; i < history && !st; ++i) st = dev_alloc(&g->hist[i], g->n);
+    if (st) break;
+    if ((st = dev_alloc(&g->xloc, g->n)) || (st = dev_alloc(&g->sc, 1))) break;
+    if (cudaMemset(g->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    if (cudaMallocHost(&g->hs, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
+    // He-uniform weights from SplitMix64, zero biases
+    std::vector<float> hp(g->np, 0.0f);
+    auto fill = [&](int64_t off, int64_t cnt, int64_t fan_in, uint64_t stream_id) {
+      const double lim = std::sqrt(6.0 / (double)fan_in);
+      for (int64_t i = 0; i < cnt; ++i) {
+        uint64_t z = seed * 0x9E3779B97F4A7C15ULL + stream_id * 0xD1B54A32D192ED03ULL + (uint64_t)(i + 1) * 0x632BE59BD9B4E019ULL;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+        hp[off + i] = (float)((2.0 * u - 1.0) * lim);
+      }
+    };
+    fill(g->oW1, F * H, F, 11);
+    fill(g->oW2, H * H, H, 12);
+    fill(g->oW3, H * O, H, 13);
+    if (cudaMemcpy(g->P, hp.data(), sizeof(float) * g->np, cudaMemcpyHostToDevice) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    cudaMemset(g->m1, 0, sizeof(float) * g->np);
+    cudaMemset(g->m2, 0, sizeof(float) * g->np);
+    { k_f2bf<<<grid_for(g->np, 256), 256, 0, plan->stream>>>(g->P, g->Pb, g->np); NTG_COUNT_LAUNCH(); }
+    if (cudaStreamSynchronize(plan->stream) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+  } while (0);
+  if (st) {
+    guess_free(g);
+    delete g;
+    return st;
+  }
+  *out = g;
+  return NTG_OK;
+}
+
+int ntg_guess_destroy(ntg_guess* g) {
+  clear_error();
+  if (!g) return NTG_OK;
+  cudaStreamSynchronize(g->plan->stream);
+  guess_free(g);
+  delete g;
+  return NTG_OK;
+}
+
+int ntg_guess_set_lr(ntg_guess* g, double lr) {
+  clear_error();
+  NTG_CHECK_ARG(g && lr > 0, "ntg_guess_set_lr: bad argument");
+  g->lr = (float)lr;
+  return NTG_OK;
+}
+
+int64_t ntg_guess_num_params(const ntg_guess* g) { return g ? g->np : 0; }
+
+int ntg_guess_params(ntg_guess* g, float* params_d, int set) {
+  clear_error();
+  NTG_CHECK_ARG(g && params_d, "ntg_guess_params: null argument");
+  cudaStream_t s = g->plan->stream;
+  if (set) {
+    NTG_CUDA_TRY(cudaMemcpyAsync(g->P, params_d, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, s));
+    { k_f2bf<<<grid_for(g->np, 256), 256, 0, s>>>(g->P, g->Pb, g->np); NTG_COUNT_LAUNCH(); }
+    NTG_CUDA_TRY(cudaGetLastError());
+  } else {
+    NTG_CUDA_TRY(cudaMemcpyAsync(params_d, g->P, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, s));
+  }
+  return NTG_OK;
+}
+
+// Raw network access (rows of X are BF16 bit patterns, row length
+// (history + 1) * lx^3): Y = net(X) for E <= nelv rows.
+int ntg_guess_forward_raw(ntg_guess* g, const uint16_t* X_d, int64_t E, float* Y_d) {
+  clear_error();
+  NTG_CHECK_ARG(g && X_d && Y_d && E >= 1 && E <= g->E, "ntg_guess_forward_raw: bad argument");
+  NTG_TRY(guess_forward(g, reinterpret_cast<const __nv_bfloat16*>(X_d), E));
+  NTG_CUDA_TRY(cudaMemcpyAsync(Y_d, g->Y, sizeof(float) * E * g->O, cudaMemcpyDeviceToDevice, g->plan->stream));
+  return NTG_OK;
+}
+
+// Gradients of the MSE loss mean((net(X) - T)^2) into grad_d (flat, the
+// parameter layout), loss value in *loss.
+int ntg_guess_grad_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int64_t E, float* grad_d, double* loss) {
+  clear_error();
+  NTG_CHECK_ARG(g && X_d && T_d && grad_d && loss && E >= 1 && E <= g->E, "ntg_guess_grad_raw: bad argument");
+  const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
+  NTG_TRY(guess_forward(g, X, E));
+  NTG_TRY(guess_backward(g, X, T_d, E));
+  NTG_CUDA_TRY(cudaMemcpyAsync(grad_d, g->G, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, g->plan->stream));
+  double sse = 0;
+  NTG_TRY(poll_red(g, 1, &sse));
+  *loss = sse / (double)(E * g->O);
+  return NTG_OK;
+}
+
+// One Adam step on explicit data (raw access, for tests).
+int ntg_guess_train_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int64_t E, double* loss) {
+  clear_error();
+  NTG_CHECK_ARG(g && X_d && T_d && loss && E >= 1 && E <= g->E, "ntg_guess_train_raw: bad argument");
+  const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
+  NTG_TRY(guess_forward(g, X, E));
+  NTG_TRY(guess_backward(g, X, T_d, E));
+  NTG_TRY(guess_adam(g));
+  double sse = 0;
+  NTG_TRY(poll_red(g, 1, &sse));
+  *loss = sse / (double)(E * g->O);
+  return NTG_OK;
+}
+
+int ntg_guess_predict(ntg_guess* g, const double* b_d, double* x_d, int* ready) {
+  clear_error();
+  NTG_CHECK_ARG(g && b_d && x_d && ready, "ntg_guess_predict: null argument");
+  *ready = 0;
+  if (g->hcount < g->nhist) return NTG_OK;
+  double sx = 1.0;
+  NTG_TRY(build_x(g, b_d, &sx));
+  NTG_TRY(guess_forward(g, g->X, g->E));
+  cudaStream_t s = g->plan->stream;
+  // average the element-local prediction over shared nodes, then mask
+  { k_scale_out<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, g->plan->mult, sx, g->n, x_d); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(gs_launch(g->plan, x_d, NTG_GS_ADD, s));
+  NTG_TRY(mask_launch(g->plan, x_d, s));
+  *ready = 1;
+  return NTG_OK;
+}
+
+int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int train_steps, double* loss) {
+  clear_error();
+  NTG_CHECK_ARG(g && b_d && x_d, "ntg_guess_observe: null argument");
+  cudaStream_t s = g->plan->stream;
+  double last = -1.0;
+  if (g->hcount >= g->nhist && train_steps > 0) {
+    double sx = 1.0;
+    NTG_TRY(build_x(g, b_d, &sx));
+    { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, 1.0 / sx, g->n, g->T, nullptr); NTG_COUNT_LAUNCH(); }
+    for (int it = 0; it < train_steps; ++it) {
+      NTG_TRY(guess_forward(g, g->X, g->E));
+      NTG_TRY(guess_backward(g, g->X, g->T, g->E));
+      NTG_TRY(guess_adam(g));
+    }
+    double sse = 0;
+    NTG_TRY(poll_red(g, 1, &sse));
+    last = sse / (double)(g->E * g->O);
+  }
+  // push x into the history ring
+  float* slot = g->hist[g->head];
+  { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, 1.0, g->n, g->T, slot); NTG_COUNT_LAUNCH(); }
+  double xx = 0;
+  { k_sumsq<float><<<grid_for(g->n, 256), 256, 0, s>>>(slot, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(poll_red(g, 2, &xx));
+  g->hrms[g->head] = sqrt(xx / (double)g->n);
+  g->head = (g->head + 1) % g->nhist;
+  if (g->hcount < g->nhist) g->hcount++;
+  if (loss) *loss = last;
+  return NTG_OK;
+}
+
+int ntg_guess_reset_history(ntg_guess* g) {
+  clear_error();
+  NTG_CHECK_ARG(g, "ntg_guess_reset_history: null argument");
+  g->hcount = 0;
+  g->head = 0;
+  return NTG_OK;
+}
+
+}  // extern "C"

@@ -117,6 +117,32 @@ int ntg_field_fourier(const double* x_d, const double* y_d, const double* z_d, i
   return NTG_OK;
 }
 
+// Fourier modes with explicit parameters (host arrays): k (3*nmodes ints),
+// amplitudes and phases; used for right-hand-side sequences whose mode
+// amplitudes evolve between solves.
+int ntg_field_modes(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
+                    const double* hi3, int nmodes, const int* k, const double* amp, const double* ph, double* f_d,
+                    void* stream) {
+  clear_error();
+  NTG_CHECK_ARG(x_d && y_d && z_d && f_d && lo3 && hi3 && k && amp && ph && n >= 0, "ntg_field_modes: bad argument");
+  NTG_CHECK_ARG(nmodes >= 1 && nmodes <= kMaxModes, "ntg_field_modes: 1 <= nmodes <= 64");
+  Modes md;
+  md.nm = nmodes;
+  for (int m = 0; m < nmodes; ++m) {
+    for (int d = 0; d < 3; ++d) md.k[3 * m + d] = k[3 * m + d];
+    md.a[m] = amp[m];
+    md.ph[m] = ph[m];
+  }
+  for (int d = 0; d < 3; ++d) {
+    md.lo[d] = lo3[d];
+    md.hi[d] = hi3[d];
+  }
+  if (n == 0) return NTG_OK;
+  { k_fourier<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(x_d, y_d, z_d, n, md, f_d); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
 int ntg_field_blobs(const double* x_d, const double* y_d, const double* z_d, int64_t n, const double* lo3,
                     const double* hi3, uint64_t seed, int nblobs, double width, double* f_d, void* stream) {
   clear_error();

@@ -1,0 +1,102 @@
+"""The learned initial guess on the GPU: its BF16 tensor-core forward and
+backward passes against the numpy oracle (oracle/mlp_ref.py, BF16 roundings
+emulated, FP64 accumulation), Adam training, and what the trained network
+gains on a right-hand-side sequence -- with every solve still converging to
+the same tolerance, and a bad guess rejected."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def small_plan(pkg, dev, E=(3, 3, 3)):
+    c = pkg.coef_t.box(*E, 8, amp=0.05, seed=4, device=dev)
+    return c
+
+
+def blocks(p, F, H, O):
+    lay, _ = mlp_ref.layout(F, H, O)
+    return {k: p[o:o + int(np.prod(s))] for k, (o, s) in lay.items()}
+
+
+def test_forward_and_gradients_match_oracle(pkg, dev):
+    c = small_plan(pkg, dev)
+    net = pkg.learned_guess_t(c, history=4, hidden=64, seed=1)
+    F, H, O = net.F, 64, net.O
+    rng = np.random.default_rng(3)
+    E = 27  # not a multiple of the 64-row tile
+    p = mlp_ref.init_params(F, H, O, rng).astype(np.float32)
+    X = rng.standard_normal((E, F)).astype(np.float32)
+    T = rng.standard_normal((E, O)).astype(np.float32)
+    net.set_params(torch.from_numpy(p).to(dev))
+    Xbits = torch.from_numpy(mlp_ref.bf16_bits(X).view(np.int16)).to(dev)
+    Y = net.forward_raw(Xbits, E).cpu().numpy()
+    Yref, _ = mlp_ref.forward(p.astype(np.float64), X, F, H, O, emulate_bf16=True)
+    assert np.abs(Y - Yref).max() <= 2e-4 * np.abs(Yref).max()
+    loss, g = net.grad_raw(Xbits, torch.from_numpy(T).to(dev), E)
+    lref, gref = mlp_ref.loss_and_grad(p.astype(np.float64), X, T, F, H, O, emulate_bf16=True)
+    assert abs(loss - lref) <= 1e-4 * lref
+    gb, gr = blocks(g.cpu().numpy().astype(np.float64), F, H, O), blocks(gref, F, H, O)
+    for k in gb:
+        err = np.linalg.norm(gb[k] - gr[k]) / max(np.linalg.norm(gr[k]), 1e-30)
+        assert err < 5e-3, (k, err)
+
+
+def test_adam_training_fits_a_linear_map(pkg, dev):
+    c = small_plan(pkg, dev, E=(4, 4, 4))
+    net = pkg.learned_guess_t(c, history=4, hidden=64, seed=2, lr=2e-3)
+    E, F, O = 64, net.F, net.O
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((E, F)).astype(np.float32)
+    T = (0.9 * X[:, :O] + 0.1 * X[:, 4 * O:]).astype(np.float32)  # newest solution and rhs
+    Xbits = torch.from_numpy(mlp_ref.bf16_bits(X).view(np.int16)).to(dev)
+    Tt = torch.from_numpy(T).to(dev)
+    first = net.train_raw(Xbits, Tt, E)
+    for _ in range(300):
+        last = net.train_raw(Xbits, Tt, E)
+    assert last < 0.1 * first, (first, last)
+
+
+def test_learned_guess_on_a_sequence(pkg, orc, dev):
+    """Online training on an AR(1) right-hand-side sequence: the trained
+    network's guess saves iterations against a zero guess, and every solve
+    reaches the same 1e-10 relative residual."""
+    ex, ey, ez = 8, 4, 4
+    c = pkg.coef_t.box(ex, ey, ez, 8, lo=(0, 0, 0), hi=(4.0, 2.0, 2.0), amp=0.0, seed=0, device=dev)
+    c.set_mask(pkg.mask_face_xmax(ex, ey, ez, 8, device=dev), base=1)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    nsolve, ntrain = 40, 28
+    k, ph, amps = pkg.ar1_modes(7, 16, nsolve, rho=0.98)
+    fs = [c.rhs_assemble(c.field_modes(k, amps[t], ph)) for t in range(nsolve)]
+    seq_l = pkg.SolveSequence(c, "cg_mixed", "learned", train_steps=30, seed=3, lr=1e-3)
+    seq_0 = pkg.SolveSequence(c, "cg_mixed", "zero")
+    it_l, it_0 = [], []
+    for t in range(nsolve):
+        seq_l.training = t < ntrain
+        x, mon, used = seq_l.solve(fs[t])
+        assert mon.status == pkg.NTG_OK and mon.res_final <= 1e-10 * mon.rhs_norm * (1 + 1e-9)
+        x0, mon0, _ = seq_0.solve(fs[t])
+        assert mon0.status == pkg.NTG_OK
+        if t >= ntrain:
+            assert used == "learned"
+            it_l.append(mon.iter)
+            it_0.append(mon0.iter)
+    assert np.mean(it_l) < 0.9 * np.mean(it_0), (it_l, it_0)
+
+
+def test_bad_guess_is_rejected(pkg, dev):
+    ex, ey, ez = 4, 3, 3
+    c = pkg.coef_t.box(ex, ey, ez, 8, amp=0.05, seed=1, device=dev)
+    c.set_mask(pkg.mask_face_xmax(ex, ey, ez, 8, device=dev), base=1)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    f = c.rhs_assemble(c.field_fourier(16, 5))
+    ksp = pkg.krylov_solver_factory(c, "cg_mixed", 5000, 1e-10)
+    ksp.set_guess_guard(True)
+    x = 1e3 * torch.randn(c.n, dtype=torch.float64, device=dev)  # an adversarial guess
+    pkg.gs_t(c).op(x)
+    mon = ksp.solve(x, f)
+    assert mon.guess_rejected == 1 and mon.status == pkg.NTG_OK
+    assert mon.res_final <= 1e-10 * mon.rhs_norm * (1 + 1e-9)
