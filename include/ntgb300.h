@@ -236,6 +236,12 @@ int ntg_proj_create(ntg_plan* plan, int L, ntg_proj** proj);
 int ntg_proj_destroy(ntg_proj* proj);
 /* b_d (assembled, masked) is replaced by b - A xbar; xbar is kept */
 int ntg_proj_pre_solving(ntg_proj* proj, double* b_d);
+/* pre_solving plus one extra direction g_d for this solve only (a learned
+   guess): g is A-orthogonalised against the basis and the Galerkin
+   component of b along it joins xbar, so the projected guess is never worse
+   in the A-norm than plain projection.  One FP64 operator application.
+   *used = 0 when g adds no new direction. */
+int ntg_proj_pre_solving_with(ntg_proj* proj, double* b_d, const double* g_d, int* used);
 /* x_d: the correction solved for on entry, the full solution on exit;
    one FP64 operator application updates the basis */
 int ntg_proj_post_solving(ntg_proj* proj, double* x_d);

@@ -80,6 +80,7 @@ SIGNATURES = {
     "ntg_proj_destroy": (_i, [_vp]),
     "ntg_proj_pre_solving": (_i, [_vp, _vp]),
     "ntg_proj_post_solving": (_i, [_vp, _vp]),
+    "ntg_proj_pre_solving_with": (_i, [_vp, _vp, _vp, _pi]),
     "ntg_proj_size": (_i, [_vp]),
     "ntg_glsc3": (_i, [_vp, _vp, _vp, _vp, _i64, _pd]),
     "ntg_guess_create": (_i, [_vp, _i, _i, C.c_uint64, C.POINTER(_vp)]),

@@ -332,6 +332,13 @@ class projection_t:
     def pre_solving(self, b):
         check(lib().ntg_proj_pre_solving(self._h, _ptr(b, n=self.coef.n, name="b")))
 
+    def pre_solving_with(self, b, g):
+        """pre_solving plus the extra direction g for this solve (learned guess)."""
+        used = C.c_int()
+        check(lib().ntg_proj_pre_solving_with(self._h, _ptr(b, n=self.coef.n, name="b"),
+                                              _ptr(g, n=self.coef.n, name="g"), C.byref(used)))
+        return bool(used.value)
+
     def post_solving(self, x):
         check(lib().ntg_proj_post_solving(self._h, _ptr(x, n=self.coef.n, name="x")))
 
@@ -448,45 +455,62 @@ def ar1_modes(seed, nmodes, nsolves, rho=0.98, kmax=4):
 class SolveSequence:
     """Solve-sequence driver in the reference's order
     (sources/adjoint/adjoint_pnpn.f90:714-743): the caller's RHS is already
-    gs-assembled and masked; then initial guess (zero, Fischer projection or
-    the learned guess) -> pc update -> ksp solve -> projection post / history
-    update.  Every solve converges to the same relative tolerance whatever the
-    guess; a learned guess worse than zero is rejected by the ksp's guard."""
+    gs-assembled and masked; then initial guess -> pc update -> ksp solve ->
+    projection post / history update.  Guess modes:
+
+      "zero"          x0 = 0
+      "projection"    Fischer residual projection over the last L solutions
+      "learned"       projection whose space is enriched, for this solve, by
+                      the learned guess (Galerkin in the A-norm: never worse
+                      than "projection")
+      "learned_only"  the learned guess as x0, behind the ksp's guard (a guess
+                      worse than zero is replaced by zero)
+
+    Every solve converges to the same tolerance, relative to the original
+    right-hand side, whatever the guess."""
 
     def __init__(self, coef: coef_t, method="cg_mixed", guess="zero", rtol=1e-10, max_iter=50000, L=20,
                  history=4, hidden=64, seed=0, lr=1e-3, train_steps=20):
+        if guess not in ("zero", "projection", "learned", "learned_only"):
+            raise ValueError(f"unknown guess mode {guess!r}")
         self.coef, self.guess, self.rtol = coef, guess, rtol
         self.ksp = krylov_solver_factory(coef, method, max_iter, rtol)
-        self.proj = projection_t(coef, L) if guess == "projection" else None
-        self.net = learned_guess_t(coef, history, hidden, seed, lr) if guess == "learned" else None
-        if self.net is not None:
+        self.proj = projection_t(coef, L) if guess in ("projection", "learned") else None
+        self.net = learned_guess_t(coef, history, hidden, seed, lr) if guess.startswith("learned") else None
+        if guess == "learned_only":
             self.ksp.set_guess_guard(True)
         self.train_steps = train_steps
         self.training = True
         self.x = torch.zeros(coef.n, dtype=torch.float64, device=coef.device)
+        self.g = torch.zeros(coef.n, dtype=torch.float64, device=coef.device) if self.net is not None else None
 
     def solve(self, f):
+        """Returns (x, monitor, guess used, ||f||)."""
         x = self.x
         x.zero_()
         used = "zero"
+        fn = glsc3(self.coef, f, f, self._mult()) ** 0.5
         if self.proj is not None:
-            # the reduced system's tolerance stays relative to the original RHS
+            # the reduced system keeps the tolerance of the original RHS
             b = f.clone()
-            fn = glsc3(self.coef, f, f, self._mult()) ** 0.5
-            self.proj.pre_solving(b)
+            used = "projection"
+            if self.net is not None and self.net.predict(f, self.g):
+                if self.proj.pre_solving_with(b, self.g):
+                    used = "projection+learned"
+            else:
+                self.proj.pre_solving(b)
             self.ksp.set_tol(0.0, self.rtol * fn)
             mon = self.ksp.solve(x, b)
             self.proj.post_solving(x)
-            used = "projection"
         else:
             if self.net is not None and self.net.predict(f, x):
                 used = "learned"
             mon = self.ksp.solve(x, f)
             if mon.guess_rejected:
                 used = "zero (learned rejected)"
-            if self.net is not None:
-                self.net.observe(f, x, self.train_steps if self.training else 0)
-        return x, mon, used
+        if self.net is not None:
+            self.net.observe(f, x, self.train_steps if self.training else 0)
+        return x, mon, used, fn
 
     def _mult(self):
         if not hasattr(self, "_mult_t"):

@@ -86,6 +86,18 @@ __global__ void k_proj_pre(double* __restrict__ xbar, double* __restrict__ axbar
   }
 }
 
+// xbar += beta v; axbar += beta A v; b -= beta A v  (beta = c[0])
+__global__ void k_proj_add(double* __restrict__ xbar, double* __restrict__ axbar, double* __restrict__ b,
+                           const double* __restrict__ v, const double* __restrict__ av, const double* __restrict__ c,
+                           int64_t n) {
+  const double beta = c[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    xbar[i] += beta * v[i];
+    axbar[i] += beta * av[i];
+    b[i] -= beta * av[i];
+  }
+}
+
 // a *= 1/sqrt(nrm2), b likewise
 __global__ void k_scale2(double* __restrict__ a, double* __restrict__ b, const double* __restrict__ nrm2, int64_t n) {
   const double s = 1.0 / sqrt(*nrm2);
@@ -127,6 +139,8 @@ struct ntg_proj {
   double* xbar = nullptr;
   double* axbar = nullptr;  // A xbar = b_original - b_reduced
   double* adx = nullptr;
+  double* gv = nullptr;     // extra direction and its A-image (pre_solving_with)
+  double* gav = nullptr;
   double* coef = nullptr;   // kProjMax + 1 device coefficients
   ntg::Scalars* sc = nullptr;
   double* hcoef = nullptr;  // pinned
@@ -137,6 +151,7 @@ using namespace ntg;
 
 static void proj_free(ntg_proj* q) {
   dev_free(q->xs); dev_free(q->axs); dev_free(q->xbar); dev_free(q->axbar); dev_free(q->adx);
+  dev_free(q->gv); dev_free(q->gav);
   dev_free(q->coef); dev_free(q->sc);
   if (q->hcoef) cudaFreeHost(q->hcoef);
   q->hcoef = nullptr;
@@ -160,6 +175,8 @@ int ntg_proj_create(ntg_plan* plan, int L, ntg_proj** proj) {
     if ((st = dev_alloc(&q->xbar, n))) break;
     if ((st = dev_alloc(&q->axbar, n))) break;
     if ((st = dev_alloc(&q->adx, n))) break;
+    if ((st = dev_alloc(&q->gv, n))) break;
+    if ((st = dev_alloc(&q->gav, n))) break;
     if ((st = dev_alloc(&q->coef, kProjMax + 1))) break;
     if ((st = dev_alloc(&q->sc, 1))) break;
     if (cudaMemset(q->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
@@ -201,6 +218,45 @@ int ntg_proj_pre_solving(ntg_proj* q, double* b_d) {
     NTG_CUDA_TRY(cudaMemsetAsync(q->axbar, 0, sizeof(double) * n, s));
   }
   q->have_pre = 1;
+  return NTG_OK;
+}
+
+// pre_solving with one extra direction g (e.g. a learned guess): after the
+// usual projection, g is A-orthogonalised against the basis (classical
+// Gram-Schmidt, twice), A-normalised, and the Galerkin component of b along
+// it is moved into xbar as well.  The direction is used for this solve only.
+// Costs one FP64 operator application.  *used = 0 when g adds nothing.
+int ntg_proj_pre_solving_with(ntg_proj* q, double* b_d, const double* g_d, int* used) {
+  clear_error();
+  NTG_CHECK_ARG(q && b_d && g_d && used, "ntg_proj_pre_solving_with: null argument");
+  *used = 0;
+  NTG_TRY(ntg_proj_pre_solving(q, b_d));
+  ntg_plan* p = q->plan;
+  cudaStream_t s = p->stream;
+  const int64_t n = p->n;
+  const int G = grid_for(n, 256);
+  double* v = q->gv;
+  double* av = q->gav;
+  NTG_CUDA_TRY(cudaMemcpyAsync(v, g_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  NTG_TRY(op_apply(p, av, v, s));
+  // (g, A g) for the rank test
+  NTG_TRY(multidot(p, v, av, 1, q->coef + kProjMax, q->sc, s));
+  NTG_CUDA_TRY(cudaMemcpyAsync(q->hcoef + 1, q->coef + kProjMax, sizeof(double), cudaMemcpyDeviceToHost, s));
+  for (int pass = 0; pass < 2 && q->m > 0; ++pass) {
+    NTG_TRY(multidot(p, av, q->xs, q->m, q->coef, q->sc, s));
+    { k_multiaxpy<<<G, 256, 0, s>>>(v, q->xs, av, q->axs, q->coef, q->m, n); NTG_COUNT_LAUNCH(); }
+  }
+  NTG_TRY(multidot(p, v, av, 1, q->coef + kProjMax, q->sc, s));
+  NTG_CUDA_TRY(cudaMemcpyAsync(q->hcoef, q->coef + kProjMax, sizeof(double), cudaMemcpyDeviceToHost, s));
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  const double nrm2 = q->hcoef[0], gag = q->hcoef[1];
+  if (!(nrm2 > 1e-14 * gag) || !std::isfinite(nrm2)) return NTG_OK;
+  { k_scale2<<<G, 256, 0, s>>>(v, av, q->coef + kProjMax, n); NTG_COUNT_LAUNCH(); }
+  // beta = (v, b); xbar += beta v; b -= beta A v
+  NTG_TRY(multidot(p, b_d, v, 1, q->coef, q->sc, s));
+  { k_proj_add<<<G, 256, 0, s>>>(q->xbar, q->axbar, b_d, v, av, q->coef, n); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  *used = 1;
   return NTG_OK;
 }
 
