@@ -98,6 +98,16 @@ __global__ void k_proj_add(double* __restrict__ xbar, double* __restrict__ axbar
   }
 }
 
+// v += beta g; av += beta A g  (beta = c[0])
+__global__ void k_proj_add_back(double* __restrict__ v, double* __restrict__ av, const double* __restrict__ g,
+                                const double* __restrict__ ag, const double* __restrict__ c, int64_t n) {
+  const double beta = c[0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    v[i] += beta * g[i];
+    av[i] += beta * ag[i];
+  }
+}
+
 // a *= 1/sqrt(nrm2), b likewise
 __global__ void k_scale2(double* __restrict__ a, double* __restrict__ b, const double* __restrict__ nrm2, int64_t n) {
   const double s = 1.0 / sqrt(*nrm2);
@@ -145,6 +155,7 @@ struct ntg_proj {
   ntg::Scalars* sc = nullptr;
   double* hcoef = nullptr;  // pinned
   int have_pre = 0;
+  int have_extra = 0;       // this solve's xbar includes beta * gv (coef[kProjMax + 2])
 };
 
 using namespace ntg;
@@ -177,7 +188,7 @@ int ntg_proj_create(ntg_plan* plan, int L, ntg_proj** proj) {
     if ((st = dev_alloc(&q->adx, n))) break;
     if ((st = dev_alloc(&q->gv, n))) break;
     if ((st = dev_alloc(&q->gav, n))) break;
-    if ((st = dev_alloc(&q->coef, kProjMax + 1))) break;
+    if ((st = dev_alloc(&q->coef, kProjMax + 4))) break;
     if ((st = dev_alloc(&q->sc, 1))) break;
     if (cudaMemset(q->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMallocHost(&q->hcoef, sizeof(double) * (kProjMax + 1)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
@@ -218,6 +229,7 @@ int ntg_proj_pre_solving(ntg_proj* q, double* b_d) {
     NTG_CUDA_TRY(cudaMemsetAsync(q->axbar, 0, sizeof(double) * n, s));
   }
   q->have_pre = 1;
+  q->have_extra = 0;
   return NTG_OK;
 }
 
@@ -253,9 +265,10 @@ int ntg_proj_pre_solving_with(ntg_proj* q, double* b_d, const double* g_d, int* 
   if (!(nrm2 > 1e-14 * gag) || !std::isfinite(nrm2)) return NTG_OK;
   { k_scale2<<<G, 256, 0, s>>>(v, av, q->coef + kProjMax, n); NTG_COUNT_LAUNCH(); }
   // beta = (v, b); xbar += beta v; b -= beta A v
-  NTG_TRY(multidot(p, b_d, v, 1, q->coef, q->sc, s));
-  { k_proj_add<<<G, 256, 0, s>>>(q->xbar, q->axbar, b_d, v, av, q->coef, n); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(multidot(p, b_d, v, 1, q->coef + kProjMax + 2, q->sc, s));
+  { k_proj_add<<<G, 256, 0, s>>>(q->xbar, q->axbar, b_d, v, av, q->coef + kProjMax + 2, n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
+  q->have_extra = 1;
   *used = 1;
   return NTG_OK;
 }
@@ -288,6 +301,11 @@ int ntg_proj_post_solving(ntg_proj* q, double* x_d) {
     double* av = q->axs + (int64_t)q->m * n;
     NTG_CUDA_TRY(cudaMemcpyAsync(v, x_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     NTG_CUDA_TRY(cudaMemcpyAsync(av, q->adx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    if (q->have_extra) {
+      // the basis takes x minus its projection on the old basis: add back the
+      // extra direction's share so no part of it enters the basis as noise
+      { k_proj_add_back<<<G, 256, 0, s>>>(v, av, q->gv, q->gav, q->coef + kProjMax + 2, n); NTG_COUNT_LAUNCH(); }
+    }
     for (int pass = 0; pass < 2 && q->m > 0; ++pass) {
       NTG_TRY(multidot(p, v, q->axs, q->m, q->coef, q->sc, s));
       { k_multiaxpy<<<G, 256, 0, s>>>(v, q->xs, av, q->axs, q->coef, q->m, n); NTG_COUNT_LAUNCH(); }

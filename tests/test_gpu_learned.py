@@ -40,7 +40,7 @@ def test_forward_and_gradients_match_oracle(pkg, dev):
     assert np.linalg.norm(Y - Yref) <= 1e-3 * np.linalg.norm(Yref)
     loss, g = net.grad_raw(Xbits, torch.from_numpy(T).to(dev), E)
     lref, gref = mlp_ref.loss_and_grad(p.astype(np.float64), X, T, F, H, O, emulate_bf16=True)
-    assert abs(loss - lref) <= 1e-4 * lref
+    assert abs(loss - lref) <= 1e-3 * lref
     gb, gr = blocks(g.cpu().numpy().astype(np.float64), F, H, O), blocks(gref, F, H, O)
     for k in gb:
         err = np.linalg.norm(gb[k] - gr[k]) / max(np.linalg.norm(gr[k]), 1e-30)
