@@ -268,6 +268,10 @@ int ntg_guess_predict(ntg_guess* guess, const double* b_d, double* x_d, int* rea
    x into the history.  *loss = the last training loss (-1 if none). */
 int ntg_guess_observe(ntg_guess* guess, const double* b_d, const double* x_d, int train_steps, double* loss);
 int ntg_guess_reset_history(ntg_guess* guess);
+/* online-training loss: 1 (default) = relative element-energy error
+   (e, A_e e)/(x, A_e x) plus relative L2 error (CG pays for energy-norm
+   error, so a guess trained in L2 alone carries nodal noise); 0 = MSE */
+int ntg_guess_set_loss(ntg_guess* guess, int energy);
 /* parameters as one flat FP32 array [W1 | b1 | W2 | b2 | W3 | b3] (W row
    major, [in x out]); set != 0 writes them */
 int64_t ntg_guess_num_params(const ntg_guess* guess);

@@ -206,6 +206,40 @@ __global__ void k_loss_grad(const float* __restrict__ Y, const float* __restrict
   grid_reduce<1>(v, part, sc, FinLoss());
 }
 
+// D = Y - T
+__global__ void k_diff(const float* __restrict__ Y, const float* __restrict__ T, int64_t len, float* __restrict__ D) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+    D[i] = Y[i] - T[i];
+}
+// energy + L2 loss: loss = (D, A D) * ge / 2 + (D, D) * gl / 2,
+// dY = ge * A D + gl * D  (ge = 2 / (T, A T), gl = 2 / (T, T))
+__global__ void k_energy_grad(const float* __restrict__ D, const float* __restrict__ AD, int64_t len, float ge,
+                              float gl, __nv_bfloat16* __restrict__ dYb, float* __restrict__ dY,
+                              double* __restrict__ part, Scalars* sc) {
+  float s = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    const float d = D[i], ad = AD[i];
+    s += 0.5f * (ge * d * ad + gl * d * d);
+    const float gd = ge * ad + gl * d;
+    dY[i] = gd;
+    dYb[i] = __float2bfloat16(gd);
+  }
+  double v[1] = {(double)s};
+  grid_reduce<1>(v, part, sc, FinLoss());
+}
+// (a, b) in FP32 per thread, FP64 across blocks -> red[3]
+struct FinSlot3 {
+  __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[3] = acc[0]; }
+};
+__global__ void k_dot_f(const float* __restrict__ a, const float* __restrict__ b, int64_t n, double* __restrict__ part,
+                        Scalars* sc) {
+  float s = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += a[i] * b[i];
+  double v[1] = {(double)s};
+  grid_reduce<1>(v, part, sc, FinSlot3());
+}
+
 // dZ = dH * (H > 0), bf16 copy
 __global__ void k_relu_back(const float* __restrict__ dH, const __nv_bfloat16* __restrict__ H, int64_t len,
                             float* __restrict__ dZ, __nv_bfloat16* __restrict__ dZb) {
@@ -281,6 +315,9 @@ struct ntg_guess {
   // activations
   __nv_bfloat16 *X = nullptr, *H1b = nullptr, *H2b = nullptr, *dYb = nullptr, *dZb = nullptr;
   float *Y = nullptr, *T = nullptr, *dY = nullptr, *dH = nullptr, *dZ = nullptr, *split = nullptr;
+  float *D = nullptr, *AD = nullptr;  // energy loss: error and its element-local A image
+  double tat = 1.0, tt = 1.0;         // (T, A T) and (T, T) of the current target
+  int loss_mode = 1;                  // 1: relative energy + L2 (online training); 0: MSE
   int splits = 16;
   // history ring of solutions (FP32), newest at hist[(head - 1) mod nhist]
   float* hist[8] = {};
@@ -300,6 +337,7 @@ static void guess_free(ntg_guess* g) {
   dev_free(g->P); dev_free(g->G); dev_free(g->m1); dev_free(g->m2); dev_free(g->Pb);
   dev_free(g->X); dev_free(g->H1b); dev_free(g->H2b); dev_free(g->dYb); dev_free(g->dZb);
   dev_free(g->Y); dev_free(g->T); dev_free(g->dY); dev_free(g->dH); dev_free(g->dZ); dev_free(g->split);
+  dev_free(g->D); dev_free(g->AD);
   for (int i = 0; i < 8; ++i) dev_free(g->hist[i]);
   dev_free(g->xloc); dev_free(g->sc);
   if (g->hs) cudaFreeHost(g->hs);
@@ -348,12 +386,21 @@ static int guess_forward(ntg_guess* g, const __nv_bfloat16* X, int64_t E) {
   return NTG_OK;
 }
 
-// loss and gradients into G for targets T (after guess_forward on X)
-static int guess_backward(ntg_guess* g, const __nv_bfloat16* X, const float* T, int64_t E) {
+// loss and gradients into G for targets T (after guess_forward on X).
+// energy != 0 (rows = all elements of the plan): relative element-energy +
+// relative L2 loss, with (T, A T) and (T, T) in g->tat / g->tt.
+static int guess_backward(ntg_guess* g, const __nv_bfloat16* X, const float* T, int64_t E, int energy) {
   cudaStream_t s = g->plan->stream;
   const int H = g->H, O = g->O;
   const int64_t len = E * O;
-  { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, 2.0f / (float)len, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  if (energy) {
+    { k_diff<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, g->D); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(ax_launch_f32(g->plan, g->AD, g->D, nullptr, 0, s));
+    const float ge = (float)(2.0 / g->tat), gl = (float)(2.0 / g->tt);
+    { k_energy_grad<<<grid_for(len, 256), 256, 0, s>>>(g->D, g->AD, len, ge, gl, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  } else {
+    { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, 2.0f / (float)len, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  }
   // layer 3
   NTG_TRY(gemm(g, g->H2b, 1, H, g->dYb, O, 1, nullptr, nullptr, nullptr, 0, H, O, E, g->splits, g->G + g->oW3));
   { k_colsum<<<(O + 31) / 32, 256, 0, s>>>(g->dY, E, O, g->G + g->ob3); NTG_COUNT_LAUNCH(); }
@@ -441,7 +488,7 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
     if ((st = dev_alloc(&g->X, E * F)) || (st = dev_alloc(&g->H1b, E * H)) || (st = dev_alloc(&g->H2b, E * H)) ||
         (st = dev_alloc(&g->dYb, E * O)) || (st = dev_alloc(&g->dZb, E * H)) || (st = dev_alloc(&g->Y, E * O)) ||
         (st = dev_alloc(&g->T, E * O)) || (st = dev_alloc(&g->dY, E * O)) || (st = dev_alloc(&g->dH, E * H)) ||
-        (st = dev_alloc(&g->dZ, E * H)))
+        (st = dev_alloc(&g->dZ, E * H)) || (st = dev_alloc(&g->D, E * O)) || (st = dev_alloc(&g->AD, E * O)))
       break;
     const int64_t split_len = (int64_t)g->splits * std::max(F * H, H * O);
     if ((st = dev_alloc(&g->split, split_len))) break;
@@ -530,7 +577,7 @@ int ntg_guess_grad_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int6
   NTG_CHECK_ARG(g && X_d && T_d && grad_d && loss && E >= 1 && E <= g->E, "ntg_guess_grad_raw: bad argument");
   const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
   NTG_TRY(guess_forward(g, X, E));
-  NTG_TRY(guess_backward(g, X, T_d, E));
+  NTG_TRY(guess_backward(g, X, T_d, E, 0));
   NTG_CUDA_TRY(cudaMemcpyAsync(grad_d, g->G, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, g->plan->stream));
   double sse = 0;
   NTG_TRY(poll_red(g, 1, &sse));
@@ -544,7 +591,7 @@ int ntg_guess_train_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int
   NTG_CHECK_ARG(g && X_d && T_d && loss && E >= 1 && E <= g->E, "ntg_guess_train_raw: bad argument");
   const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
   NTG_TRY(guess_forward(g, X, E));
-  NTG_TRY(guess_backward(g, X, T_d, E));
+  NTG_TRY(guess_backward(g, X, T_d, E, 0));
   NTG_TRY(guess_adam(g));
   double sse = 0;
   NTG_TRY(poll_red(g, 1, &sse));
@@ -578,14 +625,26 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
     double sx = 1.0;
     NTG_TRY(build_x(g, b_d, &sx));
     { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, 1.0 / sx, g->n, g->T, nullptr); NTG_COUNT_LAUNCH(); }
+    const int energy = g->loss_mode == 1;
+    if (energy) {
+      // normalisers of the relative losses: (T, A T) with the element-local
+      // operator, and (T, T)
+      NTG_TRY(ax_launch_f32(g->plan, g->AD, g->T, nullptr, 0, s));
+      { k_dot_f<<<grid_for(g->n, 256), 256, 0, s>>>(g->T, g->AD, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(poll_red(g, 3, &g->tat));
+      { k_dot_f<<<grid_for(g->n, 256), 256, 0, s>>>(g->T, g->T, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(poll_red(g, 3, &g->tt));
+      if (!(g->tat > 0)) g->tat = 1.0;
+      if (!(g->tt > 0)) g->tt = 1.0;
+    }
     for (int it = 0; it < train_steps; ++it) {
       NTG_TRY(guess_forward(g, g->X, g->E));
-      NTG_TRY(guess_backward(g, g->X, g->T, g->E));
+      NTG_TRY(guess_backward(g, g->X, g->T, g->E, energy));
       NTG_TRY(guess_adam(g));
     }
     double sse = 0;
     NTG_TRY(poll_red(g, 1, &sse));
-    last = sse / (double)(g->E * g->O);
+    last = energy ? sse : sse / (double)(g->E * g->O);
   }
   // push x into the history ring
   float* slot = g->hist[g->head];
@@ -597,6 +656,13 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
   g->head = (g->head + 1) % g->nhist;
   if (g->hcount < g->nhist) g->hcount++;
   if (loss) *loss = last;
+  return NTG_OK;
+}
+
+int ntg_guess_set_loss(ntg_guess* g, int energy) {
+  clear_error();
+  NTG_CHECK_ARG(g, "ntg_guess_set_loss: null argument");
+  g->loss_mode = energy ? 1 : 0;
   return NTG_OK;
 }
 

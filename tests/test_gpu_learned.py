@@ -75,10 +75,12 @@ def test_learned_guess_on_a_sequence(pkg, orc, dev):
     k, ph, amps = pkg.ar1_modes(7, 16, nsolve, rho=0.98)
     fs = [c.rhs_assemble(c.field_modes(k, amps[t], ph)) for t in range(nsolve)]
     seqs = {m: pkg.SolveSequence(c, "cg_mixed", m, L=8, train_steps=30, seed=3, lr=1e-3)
-            for m in ("zero", "projection", "learned")}
+            for m in ("zero", "projection", "learned", "learned_only")}
     its = {m: [] for m in seqs}
+    uses = []
     for t in range(nsolve):
-        seqs["learned"].training = t < ntrain
+        for m in ("learned", "learned_only"):
+            seqs[m].training = t < ntrain
         for m, seq in seqs.items():
             x, mon, used, fn = seq.solve(fs[t])
             assert mon.status == pkg.NTG_OK and mon.res_final <= 1e-10 * fn * (1 + 1e-9), (m, t, mon)
@@ -86,7 +88,9 @@ def test_learned_guess_on_a_sequence(pkg, orc, dev):
                 its[m].append(mon.iter)
                 if m == "learned":
                     assert used == "projection+learned"
-    print({m: float(np.mean(v)) for m, v in its.items()})
+                if m == "learned_only":
+                    uses.append(used)
+    print({m: float(np.mean(v)) for m, v in its.items()}, uses)
     assert np.mean(its["projection"]) < np.mean(its["zero"])
     assert np.mean(its["learned"]) <= np.mean(its["projection"]) + 1
 
