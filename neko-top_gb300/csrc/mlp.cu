@@ -271,17 +271,19 @@ __global__ void k_f2bf(const float* __restrict__ a, __nv_bfloat16* __restrict__ 
     b[i] = __float2bfloat16(a[i]);
 }
 
-// guess_local = s * Y (element-local, doubles) times mult, for the averaging gs
-__global__ void k_scale_out(const float* __restrict__ Y, const double* __restrict__ mult, double s, int64_t n,
-                            double* __restrict__ x) {
+// guess_local = (x_prev + s * Y) * mult (element-local, doubles), for the
+// averaging gs: the network predicts the correction to the newest solution
+// (an FP32 skip connection, so BF16 rounding never touches the guess's bulk)
+__global__ void k_scale_out(const float* __restrict__ Y, const float* __restrict__ xprev,
+                            const double* __restrict__ mult, double s, int64_t n, double* __restrict__ x) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] = s * (double)Y[i] * mult[i];
+    x[i] = ((double)xprev[i] + s * (double)Y[i]) * mult[i];
 }
-// target T = x / s (float); history push h = x (float)
-__global__ void k_target(const double* __restrict__ x, double inv_s, int64_t n, float* __restrict__ T,
-                         float* __restrict__ h) {
+// target T = (x - x_prev) / s (float; x_prev may be null); history push h = x
+__global__ void k_target(const double* __restrict__ x, const float* __restrict__ xprev, double inv_s, int64_t n,
+                         float* __restrict__ T, float* __restrict__ h) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    T[i] = (float)(x[i] * inv_s);
+    if (T) T[i] = (float)((x[i] - (xprev ? (double)xprev[i] : 0.0)) * inv_s);
     if (h) h[i] = (float)x[i];
   }
 }
@@ -513,6 +515,8 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
     fill(g->oW1, F * H, F, 11);
     fill(g->oW2, H * H, H, 12);
     fill(g->oW3, H * O, H, 13);
+    // the output layer starts small: the untrained guess is the newest solution
+    for (int64_t i = 0; i < H * O; ++i) hp[g->oW3 + i] *= 0.01f;
     if (cudaMemcpy(g->P, hp.data(), sizeof(float) * g->np, cudaMemcpyHostToDevice) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     cudaMemset(g->m1, 0, sizeof(float) * g->np);
     cudaMemset(g->m2, 0, sizeof(float) * g->np);
@@ -609,7 +613,8 @@ int ntg_guess_predict(ntg_guess* g, const double* b_d, double* x_d, int* ready) 
   NTG_TRY(guess_forward(g, g->X, g->E));
   cudaStream_t s = g->plan->stream;
   // average the element-local prediction over shared nodes, then mask
-  { k_scale_out<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, g->plan->mult, sx, g->n, x_d); NTG_COUNT_LAUNCH(); }
+  const float* xprev = g->hist[(g->head - 1 + g->nhist) % g->nhist];
+  { k_scale_out<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, xprev, g->plan->mult, sx, g->n, x_d); NTG_COUNT_LAUNCH(); }
   NTG_TRY(gs_launch(g->plan, x_d, NTG_GS_ADD, s));
   NTG_TRY(mask_launch(g->plan, x_d, s));
   *ready = 1;
@@ -624,7 +629,8 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
   if (g->hcount >= g->nhist && train_steps > 0) {
     double sx = 1.0;
     NTG_TRY(build_x(g, b_d, &sx));
-    { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, 1.0 / sx, g->n, g->T, nullptr); NTG_COUNT_LAUNCH(); }
+    const float* xprev = g->hist[(g->head - 1 + g->nhist) % g->nhist];
+    { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, xprev, 1.0 / sx, g->n, g->T, nullptr); NTG_COUNT_LAUNCH(); }
     const int energy = g->loss_mode == 1;
     if (energy) {
       // normalisers of the relative losses: (T, A T) with the element-local
@@ -648,7 +654,7 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
   }
   // push x into the history ring
   float* slot = g->hist[g->head];
-  { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, 1.0, g->n, g->T, slot); NTG_COUNT_LAUNCH(); }
+  { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, nullptr, 1.0, g->n, nullptr, slot); NTG_COUNT_LAUNCH(); }
   double xx = 0;
   { k_sumsq<float><<<grid_for(g->n, 256), 256, 0, s>>>(slot, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
   NTG_TRY(poll_red(g, 2, &xx));

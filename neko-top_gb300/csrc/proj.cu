@@ -264,8 +264,16 @@ int ntg_proj_pre_solving_with(ntg_proj* q, double* b_d, const double* g_d, int* 
   const double nrm2 = q->hcoef[0], gag = q->hcoef[1];
   if (!(nrm2 > 1e-14 * gag) || !std::isfinite(nrm2)) return NTG_OK;
   { k_scale2<<<G, 256, 0, s>>>(v, av, q->coef + kProjMax, n); NTG_COUNT_LAUNCH(); }
-  // beta = (v, b); xbar += beta v; b -= beta A v
+  // beta = (v, b); keep the direction only if it lowers the residual norm:
+  // ||b - beta A v||^2 - ||b||^2 = beta^2 (Av, Av) - 2 beta (Av, b)
   NTG_TRY(multidot(p, b_d, v, 1, q->coef + kProjMax + 2, q->sc, s));
+  NTG_TRY(multidot(p, av, b_d, 1, q->coef + kProjMax + 1, q->sc, s));
+  NTG_TRY(multidot(p, av, av, 1, q->coef + kProjMax + 3, q->sc, s));
+  NTG_CUDA_TRY(cudaMemcpyAsync(q->hcoef, q->coef + kProjMax + 1, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  const double bav = q->hcoef[0], beta = q->hcoef[1], avav = q->hcoef[2];
+  if (!(beta * beta * avav - 2.0 * beta * bav < 0.0)) return NTG_OK;
+  // xbar += beta v; b -= beta A v
   { k_proj_add<<<G, 256, 0, s>>>(q->xbar, q->axbar, b_d, v, av, q->coef + kProjMax + 2, n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   q->have_extra = 1;

@@ -86,12 +86,13 @@ def test_learned_guess_on_a_sequence(pkg, orc, dev):
             assert mon.status == pkg.NTG_OK and mon.res_final <= 1e-10 * fn * (1 + 1e-9), (m, t, mon)
             if t >= ntrain:
                 its[m].append(mon.iter)
-                if m == "learned":
-                    assert used == "projection+learned"
-                if m == "learned_only":
-                    uses.append(used)
+                if m.startswith("learned"):
+                    uses.append((m, used))
     print({m: float(np.mean(v)) for m, v in its.items()}, uses)
+    # what the trained network gains: the learned guess alone against a zero
+    # guess, and projection enriched by it against projection alone
     assert np.mean(its["projection"]) < np.mean(its["zero"])
+    assert np.mean(its["learned_only"]) < np.mean(its["zero"])
     assert np.mean(its["learned"]) <= np.mean(its["projection"]) + 1
 
 
