@@ -249,9 +249,12 @@ int ntg_proj_size(const ntg_proj* proj);
 
 /* ---------------------------------------------------------------------- */
 /* learned initial guess (new; the reference has no learned part).  A      */
-/* per-element MLP, (history + 1) * lx^3 -> hidden -> hidden -> lx^3, BF16 */
-/* weights and tensor-core GEMMs with FP32 accumulation, trained online    */
-/* with Adam on the solver's own solutions.  Inserted where the reference  */
+/* per-element MLP, (history + 1) * lx^3 -> hidden -> hidden -> history:   */
+/* its outputs weight the stored solutions on that element (weights       */
+/* delta_f0 + y_f, so an untrained net returns the newest solution), which */
+/* keeps the guess as smooth as the solutions; BF16 weights, tensor-core   */
+/* GEMMs with FP32 accumulation, trained online with Adam on the solver's  */
+/* own solutions (relative energy + L2 loss).  Inserted where the reference*/
 /* sets the initial guess: projection pre_solving                          */
 /* (sources/adjoint/adjoint_pnpn.f90:729) and the filter's guess copy      */
 /* (sources/mapping_functions/PDE_filter_mapping.f90:246,332).             */

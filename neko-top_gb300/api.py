@@ -369,7 +369,7 @@ class learned_guess_t:
         self._h = h
         self.history, self.hidden = history, hidden
         self.F = (history + 1) * coef.lx ** 3
-        self.O = coef.lx ** 3
+        self.O = history  # per-element weights of the stored solutions
         check(lib().ntg_guess_set_lr(h, float(lr)))
 
     def predict(self, b, x):

@@ -53,7 +53,7 @@ def test_adam_training_fits_a_linear_map(pkg, dev):
     E, F, O = 64, net.F, net.O
     rng = np.random.default_rng(5)
     X = rng.standard_normal((E, F)).astype(np.float32)
-    T = (0.9 * X[:, :O] + 0.1 * X[:, 4 * O:]).astype(np.float32)  # newest solution and rhs
+    T = (0.9 * X[:, :O] + 0.1 * X[:, O:2 * O]).astype(np.float32)
     Xbits = torch.from_numpy(mlp_ref.bf16_bits(X).view(np.int16)).to(dev)
     Tt = torch.from_numpy(T).to(dev)
     first = net.train_raw(Xbits, Tt, E)
