@@ -541,8 +541,11 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
       break;
     if ((st = dev_alloc(&g->X, E * F)) || (st = dev_alloc(&g->H1b, E * H)) || (st = dev_alloc(&g->H2b, E * H)) ||
         (st = dev_alloc(&g->dYb, E * O)) || (st = dev_alloc(&g->dZb, E * H)) || (st = dev_alloc(&g->Y, E * O)) ||
-        (st = dev_alloc(&g->T, E * O)) || (st = dev_alloc(&g->dY, E * O)) || (st = dev_alloc(&g->dH, E * H)) ||
-        (st = dev_alloc(&g->dZ, E * H)) || (st = dev_alloc(&g->D, E * O)) || (st = dev_alloc(&g->AD, E * O)))
+        // T, D, AD hold nodal fields (E * lx^3): the target solution, the
+        // combined guess's error and its A image; T also takes E * O raw targets
+        (st = dev_alloc(&g->T, std::max(g->n, E * O))) || (st = dev_alloc(&g->dY, E * O)) ||
+        (st = dev_alloc(&g->dH, E * H)) || (st = dev_alloc(&g->dZ, E * H)) || (st = dev_alloc(&g->D, g->n)) ||
+        (st = dev_alloc(&g->AD, g->n)))
       break;
     const int64_t split_len = (int64_t)g->splits * std::max(F * H, H * O);
     if ((st = dev_alloc(&g->split, split_len))) break;
