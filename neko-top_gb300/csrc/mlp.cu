@@ -219,15 +219,32 @@ struct HistPtrs {
   const float* h[8];
   int nh;
 };
-// D = guess - T
+// D = combined guess (times mult when given, minus T when given)
 __global__ void k_head_diff(const float* __restrict__ Y, HistPtrs hp, int lx3, int64_t n, const float* __restrict__ T,
-                            float* __restrict__ D) {
+                            const float* __restrict__ mult, float* __restrict__ D) {
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
     const int64_t e = l / lx3;
     float g = 0.f;
     for (int f = 0; f < hp.nh; ++f) g += ((f == 0 ? 1.f : 0.f) + Y[e * hp.nh + f]) * hp.h[f][l];
-    D[l] = g - T[l];
+    if (mult) g *= mult[l];
+    D[l] = T ? g - T[l] : g;
   }
+}
+__global__ void k_sub_inplace(float* __restrict__ D, const float* __restrict__ T, int64_t n) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x)
+    D[l] -= T[l];
+}
+// AD <- ge A D + gl D, loss = sum 0.5 (ge D.AD + gl D.D) (mult-free local sums)
+__global__ void k_energy_grad_field(const float* __restrict__ D, float* __restrict__ AD, int64_t n, float ge, float gl,
+                                    double* __restrict__ part, Scalars* sc) {
+  float s = 0.f;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    const float d = D[l], ad = AD[l];
+    s += 0.5f * (ge * d * ad + gl * d * d);
+    AD[l] = ge * ad + gl * d;
+  }
+  double v[1] = {(double)s};
+  grid_reduce<1>(v, part, sc, FinLoss());
 }
 // out = guess * mult (doubles, for the averaging gs)
 __global__ void k_head_combine(const float* __restrict__ Y, HistPtrs hp, int lx3, int64_t n,
@@ -239,22 +256,18 @@ __global__ void k_head_combine(const float* __restrict__ Y, HistPtrs hp, int lx3
     out[l] = g * mult[l];
   }
 }
-// energy + L2 loss of the combined guess: loss = ge/2 (D, A D) + gl/2 (D, D);
-// dY[e][f] = sum over the element's nodes of (ge A D + gl D) * h_f.
-// One block per element (grid-stride over elements), fixed-order sums.
-__global__ void __launch_bounds__(128) k_head_grad(const float* __restrict__ D, const float* __restrict__ AD,
-                                                   HistPtrs hp, int lx3, int64_t E, float ge, float gl,
-                                                   __nv_bfloat16* __restrict__ dYb, float* __restrict__ dY,
-                                                   double* __restrict__ part, Scalars* sc) {
+// dY[e][f] = sum over the element's nodes of mult * gG * h_f, gG the
+// (gathered, masked) gradient w.r.t. the assembled guess.  One block per
+// element (grid-stride over elements), fixed-order sums.
+__global__ void __launch_bounds__(128) k_head_grad(const float* __restrict__ gG, const float* __restrict__ mult,
+                                                   HistPtrs hp, int lx3, int64_t E, __nv_bfloat16* __restrict__ dYb,
+                                                   float* __restrict__ dY) {
   __shared__ float red[8][128];
-  float loss = 0.f;
   for (int64_t e = blockIdx.x; e < E; e += gridDim.x) {
     float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int q = threadIdx.x; q < lx3; q += blockDim.x) {
       const int64_t l = e * lx3 + q;
-      const float d = D[l], ad = AD[l];
-      const float gd = ge * ad + gl * d;
-      loss += 0.5f * (ge * d * ad + gl * d * d);
+      const float gd = gG[l] * mult[l];
       for (int f = 0; f < hp.nh; ++f) acc[f] += gd * hp.h[f][l];
     }
     for (int f = 0; f < hp.nh; ++f) red[f][threadIdx.x] = acc[f];
@@ -271,8 +284,6 @@ __global__ void __launch_bounds__(128) k_head_grad(const float* __restrict__ D, 
     }
     __syncthreads();
   }
-  double v[1] = {(double)loss};
-  grid_reduce<1>(v, part, sc, FinLoss());
 }
 // (a, b) in FP32 per thread, FP64 across blocks -> red[3]
 struct FinSlot3 {
@@ -444,14 +455,25 @@ static int guess_backward(ntg_guess* g, const __nv_bfloat16* X, const float* T, 
   const int H = g->H, O = g->O;
   const int64_t len = E * O;
   if (energy) {
-    // the guess is the per-element combination of the stored solutions with
-    // weights delta_f0 + Y[e][f]; D = guess - x (T holds x), AD its local A image
+    // the guess is the per-element combination C of the stored solutions
+    // (weights delta_f0 + Y[e][f]) averaged over shared nodes and masked:
+    // G = mask(gs(mult C)).  Loss on the assembled error D = G - x, so jumps
+    // between neighbouring elements' weights are paid for; its gradient
+    // flows back through the averaging (adjoint: mult * gs).
+    ntg_plan* p = g->plan;
     HistPtrs hp = hist_ptrs(g);
-    { k_head_diff<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hp, g->lx3, g->n, T, g->D); NTG_COUNT_LAUNCH(); }
-    NTG_TRY(ax_launch_f32(g->plan, g->AD, g->D, nullptr, 0, s));
+    { k_head_diff<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hp, g->lx3, g->n, nullptr, p->multf, g->D); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(gs_launch_f32(p, g->D, NTG_GS_ADD, s));
+    NTG_TRY(mask_launch_f32(p, g->D, s));
+    { k_sub_inplace<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, T, g->n); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(ax_launch_f32(p, g->AD, g->D, nullptr, 0, s));
     const float ge = (float)(2.0 / g->tat), gl = (float)(2.0 / g->tt);
+    // AD <- ge A D + gl D (gradient w.r.t. the assembled guess), loss
+    { k_energy_grad_field<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, g->AD, g->n, ge, gl, p->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(gs_launch_f32(p, g->AD, NTG_GS_ADD, s));
+    NTG_TRY(mask_launch_f32(p, g->AD, s));
     int grid = (int)(E < 2048 ? E : 2048);
-    { k_head_grad<<<grid, 128, 0, s>>>(g->D, g->AD, hp, g->lx3, E, ge, gl, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+    { k_head_grad<<<grid, 128, 0, s>>>(g->AD, p->multf, hp, g->lx3, E, g->dYb, g->dY); NTG_COUNT_LAUNCH(); }
   } else {
     { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, 2.0f / (float)len, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
   }
