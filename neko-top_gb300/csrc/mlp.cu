@@ -592,8 +592,9 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
     fill(g->oW1, F * H, F, 11);
     fill(g->oW2, H * H, H, 12);
     fill(g->oW3, H * O, H, 13);
-    // the output layer starts small: the untrained guess is the newest solution
-    for (int64_t i = 0; i < H * O; ++i) hp[g->oW3 + i] *= 0.01f;
+    // the output layer starts at zero: the untrained guess is exactly the
+    // newest solution, with no element-to-element jumps
+    for (int64_t i = 0; i < H * O; ++i) hp[g->oW3 + i] = 0.0f;
     if (cudaMemcpy(g->P, hp.data(), sizeof(float) * g->np, cudaMemcpyHostToDevice) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     cudaMemset(g->m1, 0, sizeof(float) * g->np);
     cudaMemset(g->m2, 0, sizeof(float) * g->np);
