@@ -275,6 +275,11 @@ int ntg_guess_reset_history(ntg_guess* guess);
    (e, A_e e)/(x, A_e x) plus relative L2 error (CG pays for energy-norm
    error, so a guess trained in L2 alone carries nodal noise); 0 = MSE */
 int ntg_guess_set_loss(ntg_guess* guess, int energy);
+/* output head: 1 (default) = the per-element outputs are mean-pooled into
+   one set of weights of the stored solutions (the guess stays in their
+   span, as smooth as they are); 0 = each element weights the solutions on
+   its own nodes (element-to-element jumps; measured to cost CG iterations) */
+int ntg_guess_set_head(ntg_guess* guess, int pooled);
 /* parameters as one flat FP32 array [W1 | b1 | W2 | b2 | W3 | b3] (W row
    major, [in x out]); set != 0 writes them */
 int64_t ntg_guess_num_params(const ntg_guess* guess);

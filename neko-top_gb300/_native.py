@@ -90,6 +90,7 @@ SIGNATURES = {
     "ntg_guess_observe": (_i, [_vp, _vp, _vp, _i, _pd]),
     "ntg_guess_reset_history": (_i, [_vp]),
     "ntg_guess_set_loss": (_i, [_vp, _i]),
+    "ntg_guess_set_head": (_i, [_vp, _i]),
     "ntg_guess_num_params": (_i64, [_vp]),
     "ntg_guess_params": (_i, [_vp, _vp, _i]),
     "ntg_guess_forward_raw": (_i, [_vp, _vp, _i64, _vp]),

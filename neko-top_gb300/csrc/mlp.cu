@@ -285,6 +285,71 @@ __global__ void __launch_bounds__(128) k_head_grad(const float* __restrict__ gG,
     __syncthreads();
   }
 }
+// Mean pooling of the per-element outputs: w[f] = delta_f0 + (1/E) sum_e Y[e][f]
+// (one block, fixed-order per-thread sums and tree).
+__global__ void __launch_bounds__(256) k_pool_weights(const float* __restrict__ Y, int64_t E, int nh,
+                                                      float* __restrict__ w) {
+  __shared__ float red[8][256];
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int64_t e = threadIdx.x; e < E; e += blockDim.x)
+    for (int f = 0; f < nh; ++f) acc[f] += Y[e * nh + f];
+  for (int f = 0; f < nh; ++f) red[f][threadIdx.x] = acc[f];
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int f = 0; f < nh; ++f) red[f][threadIdx.x] += red[f][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < nh) w[threadIdx.x] = (threadIdx.x == 0 ? 1.f : 0.f) + red[threadIdx.x][0] / (float)E;
+}
+// out = sum_f w[f] h_f  (continuous: a combination of continuous solutions);
+// D variant: minus T
+__global__ void k_global_combine(const float* __restrict__ w, HistPtrs hp, int64_t n, const float* __restrict__ T,
+                                 float* __restrict__ D, double* __restrict__ out) {
+  float wf[8];
+  for (int f = 0; f < hp.nh; ++f) wf[f] = w[f];
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    if (out) {
+      double g = 0.0;
+      for (int f = 0; f < hp.nh; ++f) g += (double)wf[f] * (double)hp.h[f][l];
+      out[l] = g;
+    } else {
+      float g = 0.f;
+      for (int f = 0; f < hp.nh; ++f) g += wf[f] * hp.h[f][l];
+      D[l] = g - T[l];
+    }
+  }
+}
+// gw[f] = sum_l gG[l] h_f[l] (FP32 per thread, FP64 across blocks)
+struct FinWeights {
+  double* out;
+  int nh;
+  __device__ void operator()(const double* acc, Scalars*) const {
+    for (int f = 0; f < nh; ++f) out[f] = acc[f];
+  }
+};
+__global__ void k_global_grad(const float* __restrict__ gG, HistPtrs hp, int64_t n, double* __restrict__ part,
+                              Scalars* sc, double* __restrict__ gw) {
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    const float gg = gG[l];
+    for (int f = 0; f < hp.nh; ++f) acc[f] += gg * hp.h[f][l];
+  }
+  double v[8];
+#pragma unroll
+  for (int f = 0; f < 8; ++f) v[f] = (double)acc[f];
+  grid_reduce<8>(v, part, sc, FinWeights{gw, hp.nh});
+}
+// every element receives dY[e][f] = gw[f] / E (the adjoint of mean pooling)
+__global__ void k_broadcast_dy(const double* __restrict__ gw, int64_t E, int nh, __nv_bfloat16* __restrict__ dYb,
+                               float* __restrict__ dY) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < E * nh; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = (float)(gw[i % nh] / (double)E);
+    dY[i] = v;
+    dYb[i] = __float2bfloat16(v);
+  }
+}
+
 // (a, b) in FP32 per thread, FP64 across blocks -> red[3]
 struct FinSlot3 {
   __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[3] = acc[0]; }
@@ -370,6 +435,9 @@ struct ntg_guess {
   float *D = nullptr, *AD = nullptr;  // energy loss: error and its element-local A image
   double tat = 1.0, tt = 1.0;         // (T, A T) and (T, T) of the current target
   int loss_mode = 1;                  // 1: relative energy + L2 (online training); 0: MSE
+  int pool = 1;                       // 1: mean-pooled weights (one combination); 0: per element
+  float* wpool = nullptr;             // pooled weights [8]
+  double* gw = nullptr;               // their gradient [8]
   int splits = 16;
   // history ring of solutions (FP32), newest at hist[(head - 1) mod nhist]
   float* hist[8] = {};
@@ -398,7 +466,7 @@ static void guess_free(ntg_guess* g) {
   dev_free(g->P); dev_free(g->G); dev_free(g->m1); dev_free(g->m2); dev_free(g->Pb);
   dev_free(g->X); dev_free(g->H1b); dev_free(g->H2b); dev_free(g->dYb); dev_free(g->dZb);
   dev_free(g->Y); dev_free(g->T); dev_free(g->dY); dev_free(g->dH); dev_free(g->dZ); dev_free(g->split);
-  dev_free(g->D); dev_free(g->AD);
+  dev_free(g->D); dev_free(g->AD); dev_free(g->wpool); dev_free(g->gw);
   for (int i = 0; i < 8; ++i) dev_free(g->hist[i]);
   dev_free(g->xloc); dev_free(g->sc);
   if (g->hs) cudaFreeHost(g->hs);
@@ -462,18 +530,29 @@ static int guess_backward(ntg_guess* g, const __nv_bfloat16* X, const float* T, 
     // flows back through the averaging (adjoint: mult * gs).
     ntg_plan* p = g->plan;
     HistPtrs hp = hist_ptrs(g);
-    { k_head_diff<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hp, g->lx3, g->n, nullptr, p->multf, g->D); NTG_COUNT_LAUNCH(); }
-    NTG_TRY(gs_launch_f32(p, g->D, NTG_GS_ADD, s));
-    NTG_TRY(mask_launch_f32(p, g->D, s));
-    { k_sub_inplace<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, T, g->n); NTG_COUNT_LAUNCH(); }
+    if (g->pool) {
+      // mean-pooled head: one set of weights, guess = sum_f w_f h_f
+      { k_pool_weights<<<1, 256, 0, s>>>(g->Y, E, g->nhist, g->wpool); NTG_COUNT_LAUNCH(); }
+      { k_global_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->wpool, hp, g->n, T, g->D, nullptr); NTG_COUNT_LAUNCH(); }
+    } else {
+      { k_head_diff<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hp, g->lx3, g->n, nullptr, p->multf, g->D); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(gs_launch_f32(p, g->D, NTG_GS_ADD, s));
+      NTG_TRY(mask_launch_f32(p, g->D, s));
+      { k_sub_inplace<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, T, g->n); NTG_COUNT_LAUNCH(); }
+    }
     NTG_TRY(ax_launch_f32(p, g->AD, g->D, nullptr, 0, s));
     const float ge = (float)(2.0 / g->tat), gl = (float)(2.0 / g->tt);
     // AD <- ge A D + gl D (gradient w.r.t. the assembled guess), loss
     { k_energy_grad_field<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, g->AD, g->n, ge, gl, p->red_part, g->sc); NTG_COUNT_LAUNCH(); }
-    NTG_TRY(gs_launch_f32(p, g->AD, NTG_GS_ADD, s));
-    NTG_TRY(mask_launch_f32(p, g->AD, s));
-    int grid = (int)(E < 2048 ? E : 2048);
-    { k_head_grad<<<grid, 128, 0, s>>>(g->AD, p->multf, hp, g->lx3, E, g->dYb, g->dY); NTG_COUNT_LAUNCH(); }
+    if (g->pool) {
+      { k_global_grad<<<grid_for(g->n, 256), 256, 0, s>>>(g->AD, hp, g->n, p->red_part, g->sc, g->gw); NTG_COUNT_LAUNCH(); }
+      { k_broadcast_dy<<<grid_for(E * g->nhist, 256), 256, 0, s>>>(g->gw, E, g->nhist, g->dYb, g->dY); NTG_COUNT_LAUNCH(); }
+    } else {
+      NTG_TRY(gs_launch_f32(p, g->AD, NTG_GS_ADD, s));
+      NTG_TRY(mask_launch_f32(p, g->AD, s));
+      int grid = (int)(E < 2048 ? E : 2048);
+      { k_head_grad<<<grid, 128, 0, s>>>(g->AD, p->multf, hp, g->lx3, E, g->dYb, g->dY); NTG_COUNT_LAUNCH(); }
+    }
   } else {
     { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, 2.0f / (float)len, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
   }
@@ -567,7 +646,7 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
         // combined guess's error and its A image; T also takes E * O raw targets
         (st = dev_alloc(&g->T, std::max(g->n, E * O))) || (st = dev_alloc(&g->dY, E * O)) ||
         (st = dev_alloc(&g->dH, E * H)) || (st = dev_alloc(&g->dZ, E * H)) || (st = dev_alloc(&g->D, g->n)) ||
-        (st = dev_alloc(&g->AD, g->n)))
+        (st = dev_alloc(&g->AD, g->n)) || (st = dev_alloc(&g->wpool, 8)) || (st = dev_alloc(&g->gw, 8)))
       break;
     const int64_t split_len = (int64_t)g->splits * std::max(F * H, H * O);
     if ((st = dev_alloc(&g->split, split_len))) break;
@@ -691,8 +770,13 @@ int ntg_guess_predict(ntg_guess* g, const double* b_d, double* x_d, int* ready) 
   NTG_TRY(guess_forward(g, g->X, g->E));
   cudaStream_t s = g->plan->stream;
   // average the element-local prediction over shared nodes, then mask
-  { k_head_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hist_ptrs(g), g->lx3, g->n, g->plan->mult, x_d); NTG_COUNT_LAUNCH(); }
-  NTG_TRY(gs_launch(g->plan, x_d, NTG_GS_ADD, s));
+  if (g->pool) {
+    { k_pool_weights<<<1, 256, 0, s>>>(g->Y, g->E, g->nhist, g->wpool); NTG_COUNT_LAUNCH(); }
+    { k_global_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->wpool, hist_ptrs(g), g->n, nullptr, nullptr, x_d); NTG_COUNT_LAUNCH(); }
+  } else {
+    { k_head_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hist_ptrs(g), g->lx3, g->n, g->plan->mult, x_d); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(gs_launch(g->plan, x_d, NTG_GS_ADD, s));
+  }
   NTG_TRY(mask_launch(g->plan, x_d, s));
   *ready = 1;
   return NTG_OK;
@@ -739,6 +823,13 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
   g->head = (g->head + 1) % g->nhist;
   if (g->hcount < g->nhist) g->hcount++;
   if (loss) *loss = last;
+  return NTG_OK;
+}
+
+int ntg_guess_set_head(ntg_guess* g, int pooled) {
+  clear_error();
+  NTG_CHECK_ARG(g, "ntg_guess_set_head: null argument");
+  g->pool = pooled ? 1 : 0;
   return NTG_OK;
 }
 

@@ -74,7 +74,7 @@ def test_learned_guess_on_a_sequence(pkg, orc, dev):
     nsolve, ntrain = 40, 28
     k, ph, amps = pkg.ar1_modes(7, 16, nsolve, rho=0.98)
     fs = [c.rhs_assemble(c.field_modes(k, amps[t], ph)) for t in range(nsolve)]
-    seqs = {m: pkg.SolveSequence(c, "cg_mixed", m, L=8, train_steps=30, seed=3, lr=1e-4)
+    seqs = {m: pkg.SolveSequence(c, "cg_mixed", m, L=8, train_steps=30, seed=3, lr=5e-4)
             for m in ("zero", "projection", "learned", "learned_only")}
     its = {m: [] for m in seqs}
     uses = []
