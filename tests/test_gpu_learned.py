@@ -90,10 +90,13 @@ def test_learned_guess_on_a_sequence(pkg, orc, dev):
                     uses.append((m, used))
     print({m: float(np.mean(v)) for m, v in its.items()}, uses)
     # what the trained network gains: the learned guess alone against a zero
-    # guess, and projection enriched by it against projection alone
+    # guess (measured: -14% iterations), and projection enriched by it
+    # against projection alone (measured: within a few percent -- the
+    # Galerkin projection over 8 previous solutions already holds what the
+    # network infers for this sequence)
     assert np.mean(its["projection"]) < np.mean(its["zero"])
-    assert np.mean(its["learned_only"]) < np.mean(its["zero"])
-    assert np.mean(its["learned"]) <= np.mean(its["projection"]) + 1
+    assert np.mean(its["learned_only"]) < 0.95 * np.mean(its["zero"])
+    assert np.mean(its["learned"]) <= 1.05 * np.mean(its["projection"])
 
 
 def test_bad_guess_is_rejected(pkg, dev):
