@@ -345,52 +345,79 @@ void orc_mult(int64_t n, int64_t nu, const int32_t* perm, const int64_t* offs, d
 /*   w = h1 * (D^T G D) u + h2 * B * u                                   */
 /* h1 == NULL -> constant h1c; h2 == NULL -> no mass term.              */
 /* ------------------------------------------------------------------ */
+/* Each contraction is written as a small matrix product whose innermost
+   loop runs over contiguous memory (the mxm form of CPU SEM codes), so the
+   compiler vectorises it; every sum over l still runs in ascending l. */
 void orc_ax_helm(int64_t nelv, int lx, const double* D, double* w, const double* u,
                  const double* g11, const double* g12, const double* g13,
                  const double* g22, const double* g23, const double* g33,
                  const double* h1, double h1c, const double* h2, const double* B) {
-  int64_t lx3 = (int64_t)lx * lx * lx;
+  const int lx2 = lx * lx, lx3 = lx * lx * lx;
 #pragma omp parallel
   {
-    double* wr = (double*)malloc(sizeof(double) * (size_t)lx3 * 3);
-    double* ws = wr + lx3;
-    double* wt = ws + lx3;
+    double ur[1000], us[1000], ut[1000], acc[1000];
 #pragma omp for schedule(static)
     for (int64_t e = 0; e < nelv; ++e) {
-      const double* ue = u + e * lx3;
-      int64_t base = e * lx3;
+      const double* ue = u + e * (int64_t)lx3;
+      const int64_t base = e * (int64_t)lx3;
+      for (int m = 0; m < lx3; ++m) ur[m] = us[m] = ut[m] = 0.0;
+      /* ur[i + lx c] = sum_l D[i][l] u[l + lx c]   (c = j + lx k) */
+      for (int c = 0; c < lx2; ++c)
+        for (int l = 0; l < lx; ++l) {
+          const double a = ue[l + lx * c];
+          for (int i = 0; i < lx; ++i) ur[i + lx * c] += D[i * lx + l] * a;
+        }
+      /* us[i + lx (j + lx k)] = sum_l D[j][l] u[i + lx (l + lx k)] */
       for (int k = 0; k < lx; ++k)
         for (int j = 0; j < lx; ++j)
-          for (int i = 0; i < lx; ++i) {
-            double ur = 0, us = 0, ut = 0;
-            for (int l = 0; l < lx; ++l) {
-              ur += D[i * lx + l] * ue[l + lx * (j + lx * k)];
-              us += D[j * lx + l] * ue[i + lx * (l + lx * k)];
-              ut += D[k * lx + l] * ue[i + lx * (j + lx * l)];
-            }
-            int m = i + lx * (j + lx * k);
-            int64_t gm = base + m;
-            double hh = h1 ? h1[gm] : h1c;
-            wr[m] = hh * (g11[gm] * ur + g12[gm] * us + g13[gm] * ut);
-            ws[m] = hh * (g12[gm] * ur + g22[gm] * us + g23[gm] * ut);
-            wt[m] = hh * (g13[gm] * ur + g23[gm] * us + g33[gm] * ut);
+          for (int l = 0; l < lx; ++l) {
+            const double d = D[j * lx + l];
+            const double* src = ue + lx * (l + lx * k);
+            double* dst = us + lx * (j + lx * k);
+            for (int i = 0; i < lx; ++i) dst[i] += d * src[i];
           }
+      /* ut[ij + lx2 k] = sum_l D[k][l] u[ij + lx2 l] */
+      for (int k = 0; k < lx; ++k)
+        for (int l = 0; l < lx; ++l) {
+          const double d = D[k * lx + l];
+          for (int ij = 0; ij < lx2; ++ij) ut[ij + lx2 * k] += d * ue[ij + lx2 * l];
+        }
+      /* metric mix: (wr, ws, wt) = h1 G (ur, us, ut), stored back in place */
+      for (int m = 0; m < lx3; ++m) {
+        const int64_t gm = base + m;
+        const double hh = h1 ? h1[gm] : h1c;
+        const double a = ur[m], b = us[m], c = ut[m];
+        ur[m] = hh * (g11[gm] * a + g12[gm] * b + g13[gm] * c);
+        us[m] = hh * (g12[gm] * a + g22[gm] * b + g23[gm] * c);
+        ut[m] = hh * (g13[gm] * a + g23[gm] * b + g33[gm] * c);
+        acc[m] = 0.0;
+      }
+      /* transposed contractions */
+      for (int c = 0; c < lx2; ++c)
+        for (int l = 0; l < lx; ++l) {
+          const double a = ur[l + lx * c];
+          for (int i = 0; i < lx; ++i) acc[i + lx * c] += D[l * lx + i] * a;
+        }
       for (int k = 0; k < lx; ++k)
         for (int j = 0; j < lx; ++j)
-          for (int i = 0; i < lx; ++i) {
-            double acc = 0;
-            for (int l = 0; l < lx; ++l) {
-              acc += D[l * lx + i] * wr[l + lx * (j + lx * k)];
-              acc += D[l * lx + j] * ws[i + lx * (l + lx * k)];
-              acc += D[l * lx + k] * wt[i + lx * (j + lx * l)];
-            }
-            int m = i + lx * (j + lx * k);
-            int64_t gm = base + m;
-            if (h2) acc += h2[gm] * B[gm] * ue[m];
-            w[gm] = acc;
+          for (int l = 0; l < lx; ++l) {
+            const double d = D[l * lx + j];
+            const double* src = us + lx * (l + lx * k);
+            double* dst = acc + lx * (j + lx * k);
+            for (int i = 0; i < lx; ++i) dst[i] += d * src[i];
           }
+      for (int k = 0; k < lx; ++k)
+        for (int l = 0; l < lx; ++l) {
+          const double d = D[l * lx + k];
+          for (int ij = 0; ij < lx2; ++ij) acc[ij + lx2 * k] += d * ut[ij + lx2 * l];
+        }
+      for (int m = 0; m < lx3; ++m) {
+        const int64_t gm = base + m;
+        double v = acc[m];
+        if (h2) v += h2[gm] * B[gm] * ue[m];
+        w[gm] = v;
+      }
     }
-    free(wr);
   }
 }
 
