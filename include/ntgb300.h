@@ -68,6 +68,7 @@ typedef struct ntg_plan ntg_plan; /* mesh + coef_t + gs_t + Jacobi state */
 typedef struct ntg_ksp ntg_ksp;   /* Krylov solver workspace */
 typedef struct ntg_proj ntg_proj; /* residual projection space */
 typedef struct ntg_guess ntg_guess; /* learned initial-guess network */
+typedef struct ntg_schwarz ntg_schwarz; /* overlapping Schwarz preconditioner */
 
 /* ksp_monitor_t of the reference (iter, res_start, res_final;
    sources/mapping_functions/PDE_filter_mapping.f90:265-272), plus the
@@ -203,6 +204,22 @@ int ntg_pc_jacobi_solve(ntg_plan* plan, double* z_d, const double* r_d);
 int ntg_pc_jacobi_get(const ntg_plan* plan, double* dinv_d);
 
 /* ---------------------------------------------------------------------- */
+/* Overlapping additive Schwarz preconditioner in FP32 (fast-diagonalisation */
+/* local solves on each element extended by one node layer), the one-level */
+/* part of the Schwarz-multigrid pressure preconditioner ('hsmg') the      */
+/* reference's cases select (examples/rugby_ball/rugby_ball.case:46-52).   */
+/* Structured boxes only: ex*ey*ez elements numbered x fastest (as built by */
+/* ntg_mesh_box); lx in {4, 6, 8}.                                          */
+/* ---------------------------------------------------------------------- */
+int ntg_schwarz_create(ntg_plan* plan, int ex, int ey, int ez, const double* x_d, const double* y_d,
+                       const double* z_d, ntg_schwarz** sw);
+/* refresh the element means of h1 / h2 after ntg_coef_set */
+int ntg_schwarz_update(ntg_schwarz* sw);
+int ntg_schwarz_destroy(ntg_schwarz* sw);
+/* z = M r (FP32; assembled and masked) */
+int ntg_schwarz_apply(ntg_schwarz* sw, float* z_d, const float* r_d);
+
+/* ---------------------------------------------------------------------- */
 /* ksp_t: krylov_solver_factory(ksp, n, type, max_iter, abstol) / solve /  */
 /* krylov_solver_destroy (sources/adjoint/adjoint_scheme.f90:1046-1055,    */
 /* sources/mapping_functions/PDE_filter_mapping.f90:180-181,197,255-257). */
@@ -213,6 +230,9 @@ int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double a
 int ntg_ksp_destroy(ntg_ksp* ksp);
 /* mixed solver: inner relative tolerance and inner iteration cap */
 int ntg_ksp_set_inner(ntg_ksp* ksp, double inner_rtol, int inner_max_iter);
+/* use the Schwarz preconditioner (NULL: back to Jacobi) in the FP32
+   iteration of an NTG_KSP_CG_MIXED solver */
+int ntg_ksp_set_schwarz(ntg_ksp* ksp, ntg_schwarz* sw);
 /* change the stopping tolerances of an existing solver */
 int ntg_ksp_set_tol(ntg_ksp* ksp, double rtol, double abstol);
 /* guess guard (default off): when the initial guess's residual exceeds the

@@ -26,7 +26,7 @@ from ._native import (GS_OP_ADD, GS_OP_MAX, GS_OP_MIN, GS_OP_MUL, KSP_CG, KSP_FC
                       NTG_MAXITER, NTG_NONFINITE, NTG_OK, NtgError, library_path, lib)
 from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, ar1_modes, ax_helm_t, build_box, cadd_mask,
                   cmult_mask, coef_t, col2_mask, col3_mask, glsc2_mask, glsc3, gs_t, invcol1_mask, jacobi_t,
-                  krylov_solver_factory, ksp_monitor_t, learned_guess_t, mask_face_xmax, permeability, projection_t,
+                  krylov_solver_factory, ksp_monitor_t, learned_guess_t, mask_face_xmax, permeability, projection_t, schwarz_t,
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
 
 __all__ = [
@@ -35,5 +35,5 @@ __all__ = [
     "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
-    "learned_guess_t", "SolveSequence", "ar1_modes",
+    "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t",
 ]

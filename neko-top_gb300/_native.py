@@ -61,6 +61,11 @@ SIGNATURES = {
     "ntg_field_modes": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, _i, _pi, _pd, _pd, _vp, _vp]),
     "ntg_ksp_set_guess_guard": (_i, [_vp, _i]),
     "ntg_ksp_set_tol": (_i, [_vp, _d, _d]),
+    "ntg_ksp_set_schwarz": (_i, [_vp, _vp]),
+    "ntg_schwarz_create": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "ntg_schwarz_update": (_i, [_vp]),
+    "ntg_schwarz_destroy": (_i, [_vp]),
+    "ntg_schwarz_apply": (_i, [_vp, _vp, _vp]),
     "ntg_rhs_assemble": (_i, [_vp, _vp, _vp]),
     "ntg_ax_helm": (_i, [_vp, _vp, _vp]),
     "ntg_ax_helm_f32": (_i, [_vp, _vp, _vp]),

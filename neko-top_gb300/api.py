@@ -273,6 +273,11 @@ class _ksp:
     def set_check_every(self, k):
         check(lib().ntg_ksp_set_check_every(self._h, int(k)))
 
+    def set_schwarz(self, sw):
+        """Precondition the FP32 iteration (cg_mixed) with Schwarz; None = Jacobi."""
+        check(lib().ntg_ksp_set_schwarz(self._h, None if sw is None else sw.handle))
+        self.sw = sw
+
     def set_tol(self, rtol, abstol):
         check(lib().ntg_ksp_set_tol(self._h, float(rtol), float(abstol)))
 
@@ -298,6 +303,44 @@ class _ksp:
     def free(self):
         if self._h is not None:
             check(lib().ntg_ksp_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class schwarz_t:
+    """Overlapping additive Schwarz preconditioner (FP32, fast-diagonalisation
+    local solves) for a structured box coef_t built by coef_t.box."""
+
+    def __init__(self, coef: coef_t):
+        if not hasattr(coef, "box_dims"):
+            raise ValueError("schwarz_t needs a structured box mesh (coef_t.box)")
+        ex, ey, ez = coef.box_dims
+        h = C.c_void_p()
+        check(lib().ntg_schwarz_create(coef.handle, ex, ey, ez, _ptr(coef.x), _ptr(coef.y), _ptr(coef.z),
+                                       C.byref(h)))
+        self._h = h
+        self.coef = coef
+
+    @property
+    def handle(self):
+        return self._h
+
+    def update(self):
+        """Refresh the element means of h1/h2 after coef_t.set_coefs."""
+        check(lib().ntg_schwarz_update(self._h))
+
+    def apply(self, z, r):
+        check(lib().ntg_schwarz_apply(self._h, _ptr(z, torch.float32, self.coef.n, "z"),
+                                      _ptr(r, torch.float32, self.coef.n, "r")))
+
+    def free(self):
+        if self._h is not None:
+            check(lib().ntg_schwarz_destroy(self._h))
             self._h = None
 
     def __del__(self):

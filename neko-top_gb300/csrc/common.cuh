@@ -81,6 +81,8 @@ struct Scalars {
   double red[8];   // scratch results of generic reductions
   int ru_mode;     // 1 = FP32 iteration with FP64 reliable updates
   int need_ru;     // 1 = residual replacement due, 2 = FP32 residual converged (confirm in FP64)
+  int ext_pc;      // 1 = preconditioner applied by separate kernels: (r, z) and beta come from k_rz
+  int pad2;
   int iter;        // iterations performed
   int done;        // 1 = converged or stopped: later kernels are no-ops
   int status;      // NTG_OK / NTG_MAXITER / NTG_BREAKDOWN / NTG_NONFINITE
@@ -154,8 +156,10 @@ void count_launch();
 // off by default; enabled with ntg_timer_enable.
 enum TimerId {
   TM_AX64 = 0, TM_AX32 = 1, TM_GS64 = 2, TM_GS32 = 3, TM_UPD64 = 4, TM_UPD32 = 5, TM_DIR64 = 6,
-  TM_DIR32 = 7, TM_COUNT = 16
+  TM_DIR32 = 7, TM_PC32 = 8, TM_COUNT = 16
 };
+// z = M r with the Schwarz preconditioner (schwarz.cu); no-op once sc->done
+int schwarz_apply(ntg_schwarz* sw, float* z, const float* r, cudaStream_t s, const Scalars* sc);
 void timer_start(int id, cudaStream_t s);
 void timer_stop(int id, cudaStream_t s);
 

@@ -203,6 +203,7 @@ struct FinUpd {
       sc->done = 1;
       return;
     }
+    if (sc->ext_pc) return;  // beta and (r, z) come from k_rz
     sc->beta = acc[0] / sc->rz;
     sc->rz = acc[0];
   }
@@ -515,11 +516,80 @@ struct FinRU {
     }
     // a confirmation that failed resumes the iteration: the direction update
     // skipped at the candidate uses the replaced residual
+    sc->done = 0;
+    if (sc->ext_pc) return;  // (r, z) of the new residual comes from k_rz
     if (mode == 2) sc->beta = acc[1] / sc->rz;
     sc->rz = acc[1];
-    sc->done = 0;
   }
 };
+
+// ---------------------------------------------------------------------------
+// Explicit-preconditioner variant of the FP32 iteration (Schwarz): the
+// update forms only (r, r); z = M r is applied by its own kernels; k_rz then
+// forms (r, z) and beta; k_dir_z sets p = z + beta p.
+// ---------------------------------------------------------------------------
+__global__ void k_update_rr(float* __restrict__ y, const float* __restrict__ p, float* __restrict__ r,
+                            const float* __restrict__ w, const float* __restrict__ mult, int64_t n,
+                            double* __restrict__ part, Scalars* sc) {
+  if (sc->done) return;
+  const float alpha = (float)sc->alpha;
+  float rr = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    y[i] += alpha * p[i];
+    const float ri = r[i] - alpha * w[i];
+    r[i] = ri;
+    rr += mult[i] * ri * ri;
+  }
+  double v[2] = {0.0, (double)rr};
+  grid_reduce<2>(v, part, sc, FinUpd());
+}
+
+struct FinRz {
+  int mode;  // 0 iteration / confirmation: beta = new / rz; 1 replacement: rz only; 3 start: rz, beta = 0
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    const double rz = acc[0];
+    if (!isfinite(rz) || !(rz > 0.0)) {
+      sc->status = isfinite(rz) ? NTG_BREAKDOWN : NTG_NONFINITE;
+      sc->done = 1;
+      return;
+    }
+    if (mode == 0) sc->beta = rz / sc->rz;
+    if (mode == 3) sc->beta = 0.0;
+    sc->rz = rz;
+  }
+};
+__global__ void k_rz(const float* __restrict__ r, const float* __restrict__ z, const float* __restrict__ mult,
+                     int64_t n, int mode, double* __restrict__ part, Scalars* sc) {
+  if (sc->done) return;
+  float s = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += mult[i] * r[i] * z[i];
+  double v[1] = {(double)s};
+  grid_reduce<1>(v, part, sc, FinRz{mode});
+}
+__global__ void k_dir_z(float* __restrict__ p, const float* __restrict__ z, int64_t n, int init, const Scalars* sc) {
+  if (sc->done) return;
+  const float beta = (float)sc->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = init ? z[i] : z[i] + beta * p[i];
+}
+// start: r = f - w (w null: f); r32 = (float) r; y = 0; sums ff, rr
+__global__ void k_ru_init_pc(const double* __restrict__ f, const double* __restrict__ w, const double* __restrict__ mult,
+                             double* __restrict__ r, float* __restrict__ r32, float* __restrict__ y32, int64_t n,
+                             double* __restrict__ part, Scalars* sc) {
+  double ff = 0, rr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double fi = f[i];
+    const double ri = w ? fi - w[i] : fi;
+    r[i] = ri;
+    r32[i] = (float)ri;
+    y32[i] = 0.f;
+    ff += mult[i] * fi * fi;
+    rr += mult[i] * ri * ri;
+  }
+  double v[3] = {ff, rr, 1.0};
+  grid_reduce<3>(v, part, sc, FinRUInit());
+}
 
 // r = f - w (FP64); r32 = (float) r; sums (r, r)_mult, (r32, dinv32 r32)_mult
 __global__ void k_ru_resid(const double* __restrict__ f, const double* __restrict__ w, const float* __restrict__ dinv,
@@ -554,6 +624,8 @@ struct ntg_ksp {
   int inner_max_iter = 400;
   int check_every = 16;
   int guess_guard = 0;
+  ntg_schwarz* sw = nullptr;  // explicit FP32 preconditioner of the cg_mixed iteration
+  float* z32 = nullptr;
   // FP64 workspace
   ntg::PcgVecs<double> v64;
   double *pd = nullptr, *qd = nullptr, *pprev = nullptr, *qprev = nullptr;
@@ -572,7 +644,7 @@ static void ksp_free(ntg_ksp* k) {
   dev_free(k->v64.r); dev_free(k->v64.p); dev_free(k->v64.w);
   dev_free(k->pd); dev_free(k->qd); dev_free(k->pprev); dev_free(k->qprev);
   dev_free(k->v32.r); dev_free(k->v32.p); dev_free(k->v32.w);
-  dev_free(k->rin); dev_free(k->din);
+  dev_free(k->rin); dev_free(k->din); dev_free(k->z32);
   dev_free(k->sc); dev_free(k->sc_in);
   if (k->hs) cudaFreeHost(k->hs);
   if (k->hs_in) cudaFreeHost(k->hs_in);
@@ -800,7 +872,136 @@ static int ksp_solve_mixed_ru(ntg_ksp* k, double* x, const double* f, ntg_monito
   return NTG_OK;
 }
 
+// Reliable-update mixed CG with an explicit FP32 preconditioner (Schwarz).
+static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_monitor* mon) {
+  ntg_plan* p = k->plan;
+  cudaStream_t s = p->stream;
+  const int64_t n = p->n;
+  const int TPB = 256;
+  const int G = grid_for(n, TPB);
+  NTG_TRY(ensure_fp32(p));
+  double xx = 0.0;
+  NTG_TRY(wdot(p, x, x, nullptr, n, &xx, s));
+  int fpax = 0, nru = 0;
+  Scalars* hs = k->hs;
+  memset(hs, 0, sizeof(Scalars));
+  hs->rtol = k->rtol;
+  hs->abstol = k->abstol;
+  hs->max_iter = k->max_iter;
+  hs->ru_mode = 1;
+  hs->ext_pc = 1;
+  hs->delta = k->inner_rtol;
+  NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
+  if (xx != 0.0) {
+    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    fpax++;
+  }
+  float* y32 = k->din;
+  float* r32 = k->v32.r;
+  float* p32 = k->v32.p;
+  float* w32 = k->v32.w;
+  float* z32 = k->z32;
+  { k_ru_init_pc<<<G, TPB, 0, s>>>(f, xx != 0.0 ? k->v64.w : nullptr, p->mult, k->v64.r, r32, y32, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+  auto poll = [&]() -> int {
+    NTG_CUDA_TRY(cudaMemcpyAsync(hs, k->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
+    NTG_CUDA_TRY(cudaStreamSynchronize(s));
+    return NTG_OK;
+  };
+  // z = M r, then (r, z) in the given mode
+  auto precondition = [&](int mode) -> int {
+    NTG_TRY(schwarz_apply(k->sw, z32, r32, s, k->sc));
+    { k_rz<<<G, TPB, 0, s>>>(r32, z32, p->multf, n, mode, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+    return NTG_OK;
+  };
+  auto replace = [&](int mode) -> int {
+    { k_ru_accum<<<G, TPB, 0, s>>>(x, y32, n); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    fpax++;
+    nru++;
+    { k_ru_resid<<<G, TPB, 0, s>>>(f, k->v64.w, p->dinvf ? p->dinvf : r32, p->mult, k->v64.r, r32, n, mode, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+    NTG_CUDA_TRY(cudaGetLastError());
+    NTG_TRY(poll());
+    if (hs->done) return NTG_OK;
+    NTG_TRY(precondition(mode == 2 ? 0 : 1));
+    if (mode == 2) { k_dir_z<<<G, TPB, 0, s>>>(p32, z32, n, 0, k->sc); NTG_COUNT_LAUNCH(); }
+    return poll();
+  };
+  NTG_TRY(poll());
+  const double rr0 = hs->rr0, ff = hs->ff;
+  if (!hs->done) {
+    NTG_TRY(precondition(3));
+    { k_dir_z<<<G, TPB, 0, s>>>(p32, z32, n, 1, k->sc); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(poll());
+  }
+  bool y_dirty = false;
+  int guard = 0;
+  for (;;) {
+    if (hs->done) {
+      if (hs->need_ru == 2) {
+        NTG_TRY(replace(2));
+        y_dirty = false;
+        if (hs->done) break;
+        continue;
+      }
+      break;
+    }
+    if (hs->need_ru == 1) {
+      NTG_TRY(replace(1));
+      y_dirty = false;
+      if (hs->done) break;
+    }
+    if (++guard > k->max_iter / k->check_every + 64) break;  // defensive: the device cap ends the loop first
+    for (int c = 0; c < k->check_every; ++c) {
+      NTG_TRY(ax_launch_f32(p, w32, p32, k->sc, 0, s));
+      NTG_TRY(gs_add_guarded_f32(p, w32, s, k->sc));
+      NTG_TRY(mask_guarded_f32(p, w32, s, k->sc));
+      timer_start(TM_UPD32, s);
+      { k_update_rr<<<G, TPB, 0, s>>>(y32, p32, r32, w32, p->multf, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+      timer_stop(TM_UPD32, s);
+      timer_start(TM_PC32, s);
+      NTG_TRY(precondition(0));
+      timer_stop(TM_PC32, s);
+      timer_start(TM_DIR32, s);
+      { k_dir_z<<<G, TPB, 0, s>>>(p32, z32, n, 0, k->sc); NTG_COUNT_LAUNCH(); }
+      timer_stop(TM_DIR32, s);
+    }
+    y_dirty = true;
+    NTG_TRY(poll());
+  }
+  int status = hs->status;
+  double rr_final = hs->rr;
+  if (y_dirty) {
+    const int iters = hs->iter;
+    { k_ru_accum<<<G, TPB, 0, s>>>(x, y32, n); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    fpax++;
+    { k_resid<<<G, TPB, 0, s>>>(f, k->v64.w, p->mult, k->v64.r, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(poll());
+    rr_final = hs->rr;
+    hs->iter = iters;
+  }
+  if (mon) {
+    mon->iter = hs->iter;
+    mon->inner_iter = nru;
+    mon->res_start = sqrt(rr0);
+    mon->res_final = sqrt(rr_final);
+    mon->rhs_norm = sqrt(ff);
+    mon->status = status;
+    mon->fp64_ax = fpax;
+  }
+  return NTG_OK;
+}
+
 extern "C" {
+
+int ntg_ksp_set_schwarz(ntg_ksp* ksp, ntg_schwarz* sw_) {
+  clear_error();
+  NTG_CHECK_ARG(ksp, "ntg_ksp_set_schwarz: null argument");
+  NTG_CHECK_ARG(ksp->type == NTG_KSP_CG_MIXED, "ntg_ksp_set_schwarz: only the cg_mixed solver takes Schwarz");
+  if (sw_ && !ksp->z32) NTG_TRY(dev_alloc(&ksp->z32, ksp->plan->n));
+  ksp->sw = sw_;
+  return NTG_OK;
+}
 
 int ntg_pc_jacobi_update(ntg_plan* plan) {
   clear_error();
@@ -948,7 +1149,8 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
   }
   int st = NTG_OK;
   if (ksp->type == NTG_KSP_FCG_MIXED) st = ksp_solve_mixed(ksp, x_d, f_d, mon);
-  else if (ksp->type == NTG_KSP_CG_MIXED) st = ksp_solve_mixed_ru(ksp, x_d, f_d, mon);
+  else if (ksp->type == NTG_KSP_CG_MIXED)
+    st = ksp->sw ? ksp_solve_mixed_ru_pc(ksp, x_d, f_d, mon) : ksp_solve_mixed_ru(ksp, x_d, f_d, mon);
   else st = ksp_solve_cg(ksp, x_d, f_d, mon);
   if (mon) {
     mon->guess_rejected = rejected;

@@ -1,0 +1,105 @@
+"""numpy restatement of the overlapping additive Schwarz preconditioner.
+
+TEST INFRASTRUCTURE ONLY: the checker for neko-top_gb300/csrc/schwarz.cu.
+
+    z = sum_e R_e^T  A~_e^{-1}  R_e r
+
+on structured boxes (elements numbered x fastest).  R_e gathers the
+assembled residual on element e extended by one node layer into each
+neighbour; A~_e = h1 (Bz x By x Kx + Bz x Ky x Bx + Kz x By x Bx) + h2 Bz x By x Bx
+with 1D operators assembled from the element's and its neighbours' GLL
+intervals (Dirichlet one node beyond the extension), inverted through the
+generalised eigenvectors (numpy.linalg.eigh); R_e^T adds the extended result
+into a global structured grid (a different prolongation than the kernel's
+pull + gather-scatter).  Element lengths: mean distance between opposite faces.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle import numpy_ref
+
+
+def element_lengths(m):
+    lx = m.lx
+    X = np.stack([m.x, m.y, m.z]).reshape(3, m.nelv, lx, lx, lx)  # (d, e, k, j, i)
+    out = np.zeros((m.nelv, 3))
+    for d, (a0, a1) in enumerate(((np.s_[:, :, :, :, 0], np.s_[:, :, :, :, -1]),
+                                  (np.s_[:, :, :, 0, :], np.s_[:, :, :, -1, :]),
+                                  (np.s_[:, :, 0, :, :], np.s_[:, :, -1, :, :]))):
+        diff = X[a1] - X[a0]
+        out[:, d] = np.sqrt((diff ** 2).sum(0)).mean(axis=(1, 2))
+    return out
+
+
+def ext_1d(lx, hl, hc, hr):
+    N = lx - 1
+    _, w, D = numpy_ref.gll(lx)
+    Kh = D.T @ np.diag(w) @ D
+    ng = 3 * N + 1
+    K = np.zeros((ng, ng))
+    B = np.zeros(ng)
+    for el, h in enumerate((hl, hc, hr)):
+        s = slice(el * N, el * N + lx)
+        K[s, s] += (2.0 / h) * Kh
+        B[s] += 0.5 * h * w
+    sl = slice(N - 1, 2 * N + 2)
+    Ke, Be = K[sl, sl], B[sl]
+    bi = 1.0 / np.sqrt(Be)
+    lam, Q = np.linalg.eigh(bi[:, None] * Ke * bi[None, :])
+    return bi[:, None] * Q, lam
+
+
+def apply(m, r, box, h1=1.0, h2=None, mask=None):
+    """z = M r for an oracle Mesh `m` built as a box of `box` = (Ex, Ey, Ez)."""
+    Ex, Ey, Ez = box
+    lx = m.lx
+    N, LE = lx - 1, lx + 2
+    hl = element_lengths(m)
+    r4 = np.asarray(r).reshape(m.nelv, lx, lx, lx)  # (e, k, j, i)
+    G = np.zeros((Ex * N + 1, Ey * N + 1, Ez * N + 1))  # indexed (gx, gy, gz)
+    h2e = np.zeros(m.nelv) if h2 is None else np.asarray(h2).reshape(m.nelv, -1).mean(1)
+    dims = (Ex, Ey, Ez)
+    for e in range(m.nelv):
+        c = (e % Ex, (e // Ex) % Ey, e // (Ex * Ey))
+        strides = (1, Ex, Ex * Ey)
+        Ss, Ls = [], []
+        for d in range(3):
+            hc = hl[e, d]
+            hlft = hl[e - strides[d], d] if c[d] > 0 else hc
+            hrgt = hl[e + strides[d], d] if c[d] < dims[d] - 1 else hc
+            S, lam = ext_1d(lx, hlft, hc, hrgt)
+            Ss.append(S)
+            Ls.append(lam)
+        # gather R_e r on the extended box (index order a=x, b=y, c=z)
+        rext = np.zeros((LE, LE, LE))
+        for a in range(LE):
+            for b in range(LE):
+                for cc in range(LE):
+                    g = (c[0] * N + a - 1, c[1] * N + b - 1, c[2] * N + cc - 1)
+                    if not all(0 <= g[q] <= dims[q] * N for q in range(3)):
+                        continue
+                    # any element holding the global node: pick by clamping
+                    ec = [min(g[q] // N, dims[q] - 1) for q in range(3)]
+                    loc = [g[q] - ec[q] * N for q in range(3)]
+                    en = ec[0] + Ex * (ec[1] + Ey * ec[2])
+                    rext[a, b, cc] = r4[en, loc[2], loc[1], loc[0]]
+        Sx, Sy, Sz = Ss
+        t = np.einsum("pa,qb,sc,pqs->abc", Sx, Sy, Sz, rext)
+        t /= h1 * (Ls[0][:, None, None] + Ls[1][None, :, None] + Ls[2][None, None, :]) + h2e[e]
+        zext = np.einsum("ap,bq,cs,pqs->abc", Sx, Sy, Sz, t)
+        for a in range(LE):
+            for b in range(LE):
+                for cc in range(LE):
+                    g = (c[0] * N + a - 1, c[1] * N + b - 1, c[2] * N + cc - 1)
+                    if all(0 <= g[q] <= dims[q] * N for q in range(3)):
+                        G[g] += zext[a, b, cc]
+    # back to the local layout
+    z = np.zeros_like(r4)
+    for e in range(m.nelv):
+        c = (e % Ex, (e // Ex) % Ey, e // (Ex * Ey))
+        z[e] = G[c[0] * N:c[0] * N + lx, c[1] * N:c[1] * N + lx, c[2] * N:c[2] * N + lx].transpose(2, 1, 0)
+    z = z.ravel()
+    if mask is not None and len(mask):
+        z[np.asarray(mask) - 1] = 0.0
+    return z

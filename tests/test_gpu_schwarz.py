@@ -1,0 +1,88 @@
+"""Overlapping Schwarz preconditioner (FP32) against its numpy restatement,
+its symmetry, and the reliable-update mixed CG preconditioned by it."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import schwarz_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def T(a, dev, dtype=torch.float64):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device=dev, dtype=dtype)
+
+
+@pytest.mark.parametrize("shape", [(3, 2, 2, 8, 0.05), (2, 3, 2, 4, 0.0), (4, 1, 2, 6, 0.05)])
+def test_schwarz_apply_matches_oracle(pkg, orc, dev, shape):
+    ex, ey, ez, lx, amp = shape
+    m = orc.build_mesh(ex, ey, ez, lx, amp=amp, seed=2)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=amp, seed=2, device=dev)
+    mask = orc.mask_face_xmax(ex, ey, ez, lx)
+    c.set_mask(T(mask, dev, torch.int32), base=1)
+    rng = np.random.default_rng(1)
+    h2 = rng.uniform(0.0, 2.0, m.n)
+    c.set_coefs(h1c=0.5, h2=T(h2, dev), ifh2=True)
+    sw = pkg.schwarz_t(c)
+    r = orc.apply_mask_zero(orc.gs_op(m, rng.standard_normal(m.n)) * m.mult, mask).astype(np.float32)
+    z = torch.empty(m.n, dtype=torch.float32, device=dev)
+    sw.apply(z, T(r, dev, torch.float32))
+    torch.cuda.synchronize()
+    ref = schwarz_ref.apply(m, r.astype(np.float64), (ex, ey, ez), h1=0.5, h2=h2, mask=mask)
+    zz = z.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(zz - ref) <= 2e-5 * np.linalg.norm(ref)
+
+
+def test_schwarz_is_symmetric(pkg, orc, dev):
+    ex, ey, ez, lx = 4, 3, 2, 8
+    m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=3)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.05, seed=3, device=dev)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    sw = pkg.schwarz_t(c)
+    rng = np.random.default_rng(4)
+    u = (orc.gs_op(m, rng.standard_normal(m.n)) * m.mult).astype(np.float32)
+    v = (orc.gs_op(m, rng.standard_normal(m.n)) * m.mult).astype(np.float32)
+    Mu = torch.empty(m.n, dtype=torch.float32, device=dev)
+    Mv = torch.empty_like(Mu)
+    sw.apply(Mu, T(u, dev, torch.float32))
+    sw.apply(Mv, T(v, dev, torch.float32))
+    torch.cuda.synchronize()
+    a = float(np.sum(m.mult * v * Mu.cpu().numpy()))
+    b = float(np.sum(m.mult * u * Mv.cpu().numpy()))
+    assert abs(a - b) <= 1e-5 * max(abs(a), abs(b))
+    assert float(np.sum(m.mult * u * Mu.cpu().numpy())) > 0
+
+
+@pytest.mark.parametrize("case", ["poisson", "brinkman"])
+def test_cg_mixed_with_schwarz(pkg, orc, dev, case):
+    ex, ey, ez, lx = 6, 4, 4, 8
+    m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=21)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.05, seed=21, device=dev)
+    mask = orc.mask_face_xmax(ex, ey, ez, lx)
+    c.set_mask(T(mask, dev, torch.int32), base=1)
+    h1c, h2 = 1.0, None
+    if case == "brinkman":
+        rho = orc.field_blobs(m, 5, 12, 0.1)
+        h2 = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
+        h1c = 0.01
+        c.set_coefs(h1c=h1c, h2=T(h2, dev), ifh2=True)
+    else:
+        c.set_coefs(h1c=1.0, ifh2=False)
+    k, a, ph = orc.fourier_params(21, 16)
+    f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+    ksp_j = pkg.krylov_solver_factory(c, "cg_mixed", 20000, 1e-10)
+    xj = torch.zeros(m.n, dtype=torch.float64, device=dev)
+    mon_j = ksp_j.solve(xj, T(f, dev))
+    sw = pkg.schwarz_t(c)
+    ksp = pkg.krylov_solver_factory(c, "cg_mixed", 20000, 1e-10)
+    ksp.set_schwarz(sw)
+    x = torch.zeros(m.n, dtype=torch.float64, device=dev)
+    mon = ksp.solve(x, T(f, dev))
+    torch.cuda.synchronize()
+    assert mon.status == pkg.NTG_OK, mon
+    xn = x.cpu().numpy()
+    r = f - orc.op_apply(m, xn, h1c=h1c, h2=h2, mask=mask)
+    assert np.sqrt(orc.glsc3(r, r, m.mult)) <= 1.5e-10 * np.sqrt(orc.glsc3(f, f, m.mult))
+    assert np.linalg.norm(xn - xj.cpu().numpy()) <= 1e-7 * np.linalg.norm(xn)
+    print(case, "jacobi", mon_j.iter, "schwarz", mon.iter)
+    assert mon.iter < 0.6 * mon_j.iter
