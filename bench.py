@@ -235,9 +235,17 @@ def run_ours(args, ws, rank, local):
     if args.kernels_only:
         return run_kernels_only(args, pkg, coef, f, dev)
     n = coef.n
+    pc = args.pc
+    if pc == "auto":  # Schwarz for the pressure-Poisson cases, Jacobi under Brinkman penalisation
+        pc = "schwarz" if cfg["case"] == "poisson_fourier" else "jacobi"
+    args.pc_used = pc
+    sw = None
     if args.method == "cg_mixed":
         ksp_mx = pkg.krylov_solver_factory(coef, "cg_mixed", 50000, RTOL)
         ksp_mx.set_inner(args.delta, 1)
+        if pc == "schwarz":
+            sw = pkg.schwarz_t(coef)
+            ksp_mx.set_schwarz(sw)
     else:
         ksp_mx = pkg.krylov_solver_factory(coef, "fcg_mixed", 200, RTOL)
         ksp_mx.set_inner(args.inner_rtol, args.inner_max)
@@ -295,7 +303,7 @@ def run_ours(args, ws, rank, local):
     L.ntg_timer_enable(0)
     import ctypes as C
     names = {0: "ax_fp64", 1: "ax_fp32", 2: "gs_fp64", 3: "gs_fp32", 4: "cg_update_fp64", 5: "cg_update_fp32",
-             6: "cg_dir_fp64", 7: "cg_dir_fp32"}
+             6: "cg_dir_fp64", 7: "cg_dir_fp32", 8: "schwarz_fp32"}
     ktimes = {}
     for i, nm in names.items():
         ms, cnt = C.c_double(), C.c_longlong()
@@ -356,7 +364,8 @@ def run_ours(args, ws, rank, local):
         "dtype": "f32 inner / f64 outer",
         "data": "synthetic (seeded generators; no dataset)",
         "config": {"workload": f"{args.config}: {cfg['desc']}", "n_local_dofs": n, "n_unique_dofs": coef.nu,
-                   "method": (f"cg_mixed (Jacobi-PCG in FP32, FP64 reliable updates at delta={args.delta:g})"
+                   "method": (f"cg_mixed (PCG in FP32 with the {args.pc_used} preconditioner, FP64 reliable "
+                              f"updates at delta={args.delta:g})"
                               if args.method == "cg_mixed" else
                               f"fcg_mixed (inner Jacobi-PCG FP32 to {args.inner_rtol:g}, outer FCG(1) FP64)"),
                    "l2": "inputs larger than L2 (FP64 G 805 MB, FP32 G 403 MB at c2)",
@@ -484,6 +493,8 @@ def main(argv=None):
     p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     p.add_argument("--method", choices=["cg_mixed", "fcg_mixed"], default="cg_mixed")
     p.add_argument("--delta", type=float, default=0.1, help="reliable-update threshold of cg_mixed")
+    p.add_argument("--pc", choices=["auto", "jacobi", "schwarz"], default="auto",
+                   help="FP32 preconditioner of cg_mixed (auto: Schwarz for Poisson, Jacobi for Brinkman)")
     p.add_argument("--inner-rtol", type=float, default=1e-4)
     p.add_argument("--inner-max", type=int, default=2000)
     p.add_argument("--fp64-steps", type=int, default=2)
