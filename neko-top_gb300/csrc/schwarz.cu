@@ -74,125 +74,209 @@ struct Ext {
   static constexpr int N = LX - 1, LE = LX + 2, LE2 = LE * LE, LE3 = LE * LE * LE;
 };
 
-// extended residual -> FDM solve -> extended result (one block per element)
+// Extended residual -> FDM solve -> extended result for a batch of EPB
+// elements per block, one thread per 1D line of an element's extended box.
+// Each direction pass loads the thread's line from shared memory, applies
+// the 1D eigenvector matrix two outputs at a time with packed FP32 FMAs
+// (__ffma2_rn: operator rows f, f+1 interleaved, the line value duplicated)
+// and writes the line back in place, so a pass needs one buffer and one
+// barrier.  Shared memory per element slot:
+//   P[3][LE/2][LE][2]   forward pairs   P[d][f/2][p][f&1] = S_d[p][f]
+//   Q[3][LE/2][LE][2]   backward pairs  Q[d][a/2][f][a&1] = S_d[a][f]
+//   lam[3][LE], (h1, h2), tile A[a + RS b + PS c]
 template <int LX>
-__global__ void __launch_bounds__(128)
+struct FdmCfg {
+  static constexpr int LE = LX + 2, LE2 = LE * LE, LE3 = LE2 * LE;
+  static constexpr int RS = LE + 1, PS = RS * LE + 1;  // odd tile strides (fewer bank conflicts)
+  static constexpr int POFF = 0, QOFF = 3 * LE2, LOFF = 6 * LE2, HOFF = LOFF + 3 * LE, AOFF = (HOFF + 2 + 3) & ~3;
+  static constexpr int PER = (AOFF + PS * LE + 3) & ~3;  // floats per element slot
+  static constexpr int EPB = LX == 8 ? 4 : 8, THREADS = EPB * LE2, MINB = LX == 8 ? 3 : 4;
+  static constexpr size_t SMEM = (size_t)EPB * PER * sizeof(float);
+};
+
+// dst[f * ST] = sum_p M[f][p] in[p] for the interleaved pair rows of M
+template <int LE, int ST>
+__device__ __forceinline__ void fdm_line(const float* __restrict__ M, const float2 (&in)[LE], float* dst) {
+#pragma unroll
+  for (int fp = 0; fp < LE / 2; ++fp) {
+    const float* row = M + fp * 2 * LE;
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < LE; p += 2) {
+      const float4 m4 = *reinterpret_cast<const float4*>(row + 2 * p);
+      acc = __ffma2_rn(make_float2(m4.x, m4.y), in[p], acc);
+      acc = __ffma2_rn(make_float2(m4.z, m4.w), in[p + 1], acc);
+    }
+    dst[(2 * fp) * ST] = acc.x;
+    dst[(2 * fp + 1) * ST] = acc.y;
+  }
+}
+
+template <int LX>
+__global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
     k_fdm(const float* __restrict__ r, float* __restrict__ ze, const float* __restrict__ S,
-          const float* __restrict__ lam, const float* __restrict__ hc, int Ex, int Ey, int Ez, const Scalars* sc) {
-  using X = Ext<LX>;
-  constexpr int LE = X::LE, LE2 = X::LE2, LE3 = X::LE3, N = X::N;
-  constexpr int LX2 = LX * LX, LX3 = LX * LX * LX;
+          const float* __restrict__ lam, const float* __restrict__ hc, int Ex, int Ey, int Ez,
+          const Scalars* sc) {
+  using C = FdmCfg<LX>;
+  constexpr int LE = C::LE, LE2 = C::LE2, LE3 = C::LE3, N = LX - 1, RS = C::RS, PS = C::PS;
+  constexpr int EPB = C::EPB, PER = C::PER, LX2 = LX * LX, LX3 = LX2 * LX;
+  static_assert(LE % 2 == 0 && C::THREADS <= 1024, "pairs of outputs; one thread per line");
   if (sc && sc->done) return;
-  __shared__ float A[LE3], Bt[LE3], sS[3][LE2], sL[3][LE];
-  const int64_t nelv = (int64_t)Ex * Ey * Ez;
-  for (int64_t e = blockIdx.x; e < nelv; e += gridDim.x) {
-    const int ex = (int)(e % Ex), ey = (int)((e / Ex) % Ey), ez = (int)(e / ((int64_t)Ex * Ey));
-    for (int q = threadIdx.x; q < 3 * LE2; q += blockDim.x) sS[q / LE2][q % LE2] = S[e * 3 * LE2 + q];
-    for (int q = threadIdx.x; q < 3 * LE; q += blockDim.x) sL[q / LE][q % LE] = lam[e * 3 * LE + q];
-    const float h1 = hc[2 * e], h2 = hc[2 * e + 1];
-    // gather R_e r
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, b = (q / LE) % LE, c = q / LE2;
-      int i = a - 1, j = b - 1, k = c - 1;
-      int dx = 0, dy = 0, dz = 0;
+  extern __shared__ __align__(16) float smem[];
+  const int nelv = Ex * Ey * Ez;
+  const int tid = threadIdx.x, el = tid / LE2, line = tid - el * LE2;
+  const int lu = line % LE, lv = line / LE;
+  float* sl = smem + el * PER;
+  float* A = sl + C::AOFF;
+  float2 in[LE];
+  for (int e0 = blockIdx.x * EPB; e0 < nelv; e0 += gridDim.x * EPB) {
+    // operators of the batch: the thread's entry (a, f) = (lv, lu) of
+    // S[e][d] (coalesced over lines) -> pair rows P and Q
+    const int e = e0 + el;
+    {
+      const int aa = lv, ff = lu;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float v = e < nelv ? S[(int64_t)e * 3 * LE2 + d * LE2 + line] : 0.f;
+        sl[C::POFF + d * LE2 + (ff >> 1) * 2 * LE + 2 * aa + (ff & 1)] = v;
+        sl[C::QOFF + d * LE2 + (aa >> 1) * 2 * LE + 2 * ff + (aa & 1)] = v;
+      }
+      if (line < 3 * LE) sl[C::LOFF + line] = e < nelv ? lam[(int64_t)e * 3 * LE + line] : 0.f;
+      if (line < 2) sl[C::HOFF + line] = e < nelv ? hc[2 * (int64_t)e + line] : 1.f;
+    }
+    // gather R_e r: the thread's column (a, b) = (lu, lv) over c
+    if (e < nelv) {
+      const int exy = e / Ex, ex = e - exy * Ex, ez = exy / Ey, ey = exy - ez * Ey;
+      int i = lu - 1, j = lv - 1, dx = 0, dy = 0;
       if (i < 0) { dx = -1; i = N - 1; } else if (i > N) { dx = 1; i = 1; }
       if (j < 0) { dy = -1; j = N - 1; } else if (j > N) { dy = 1; j = 1; }
-      if (k < 0) { dz = -1; k = N - 1; } else if (k > N) { dz = 1; k = 1; }
-      const int nx = ex + dx, ny = ey + dy, nz = ez + dz;
-      float v = 0.f;
-      if (nx >= 0 && nx < Ex && ny >= 0 && ny < Ey && nz >= 0 && nz < Ez) {
-        const int64_t en = nx + (int64_t)Ex * (ny + (int64_t)Ey * nz);
-        v = r[en * LX3 + i + LX * j + LX2 * k];
+      const int nx = ex + dx, ny = ey + dy;
+      const bool okxy = nx >= 0 && nx < Ex && ny >= 0 && ny < Ey;
+      const float* rc = r + (int64_t)(nx + Ex * (ny + Ey * ez)) * LX3 + i + LX * j;
+      const int64_t zs = (int64_t)Ex * Ey * LX3;
+      float* Ac = A + lu + RS * lv;
+      Ac[0] = okxy && ez > 0 ? rc[(N - 1) * LX2 - zs] : 0.f;
+#pragma unroll
+      for (int c = 1; c < LE - 1; ++c) Ac[PS * c] = okxy ? rc[(c - 1) * LX2] : 0.f;
+      Ac[PS * (LE - 1)] = okxy && ez < Ez - 1 ? rc[LX2 + zs] : 0.f;
+    }
+    __syncthreads();
+    const float* P = sl + C::POFF;
+    const float* Q = sl + C::QOFF;
+    // r forward: line (b, c) = (lu, lv), along a
+#pragma unroll
+    for (int p = 0; p < LE; ++p) { const float v = A[p + RS * lu + PS * lv]; in[p] = make_float2(v, v); }
+    fdm_line<LE, 1>(P, in, A + RS * lu + PS * lv);
+    __syncthreads();
+    // s forward: line (a, c) = (lu, lv), along b
+#pragma unroll
+    for (int p = 0; p < LE; ++p) { const float v = A[lu + RS * p + PS * lv]; in[p] = make_float2(v, v); }
+    fdm_line<LE, RS>(P + LE2, in, A + lu + PS * lv);
+    __syncthreads();
+    // t forward, scale by the inverse eigenvalue sum, t back: line (a, b) = (lu, lv)
+    {
+      const float* L = sl + C::LOFF;
+      const float h1 = sl[C::HOFF], h2 = sl[C::HOFF + 1];
+      const float lab = L[lu] + L[LE + lv];
+      float* At = A + lu + RS * lv;
+#pragma unroll
+      for (int p = 0; p < LE; ++p) { const float v = At[PS * p]; in[p] = make_float2(v, v); }
+      float t[LE];
+      fdm_line<LE, 1>(P + 2 * LE2, in, t);
+#pragma unroll
+      for (int f = 0; f < LE; ++f) {
+        const float v = __fdividef(t[f], h1 * (lab + L[2 * LE + f]) + h2);
+        in[f] = make_float2(v, v);
       }
-      A[q] = v;
+      fdm_line<LE, PS>(Q + 2 * LE2, in, At);
     }
     __syncthreads();
-    // transform: Bt = (Sz x Sy x Sx)^T A   (three passes, A <-> Bt)
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, rest = q - a;
-      float s = 0.f;
+    // s back
 #pragma unroll
-      for (int p = 0; p < LE; ++p) s = fmaf(sS[0][p * LE + a], A[rest + p], s);
-      Bt[q] = s;
-    }
+    for (int p = 0; p < LE; ++p) { const float v = A[lu + RS * p + PS * lv]; in[p] = make_float2(v, v); }
+    fdm_line<LE, RS>(Q + LE2, in, A + lu + PS * lv);
     __syncthreads();
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, b = (q / LE) % LE, c = q / LE2;
-      float s = 0.f;
+    // r back
 #pragma unroll
-      for (int p = 0; p < LE; ++p) s = fmaf(sS[1][p * LE + b], Bt[a + LE * p + LE2 * c], s);
-      A[q] = s;
-    }
+    for (int p = 0; p < LE; ++p) { const float v = A[p + RS * lu + PS * lv]; in[p] = make_float2(v, v); }
+    fdm_line<LE, 1>(Q, in, A + RS * lu + PS * lv);
     __syncthreads();
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, b = (q / LE) % LE, c = q / LE2;
-      float s = 0.f;
+    // copy-out: the thread's column (a, b) = (lu, lv) of ze[e][a + LE b + LE2 c]
+    // (consecutive lines -> consecutive addresses)
+    if (e < nelv) {
 #pragma unroll
-      for (int p = 0; p < LE; ++p) s = fmaf(sS[2][p * LE + c], A[a + LE * b + LE2 * p], s);
-      Bt[q] = s / (h1 * (sL[0][a] + sL[1][b] + sL[2][c]) + h2);
-    }
-    __syncthreads();
-    // back: A = (Sz x Sy x Sx) Bt
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, b = (q / LE) % LE, c = q / LE2;
-      float s = 0.f;
-#pragma unroll
-      for (int p = 0; p < LE; ++p) s = fmaf(sS[2][c * LE + p], Bt[a + LE * b + LE2 * p], s);
-      A[q] = s;
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, b = (q / LE) % LE, c = q / LE2;
-      float s = 0.f;
-#pragma unroll
-      for (int p = 0; p < LE; ++p) s = fmaf(sS[1][b * LE + p], A[a + LE * p + LE2 * c], s);
-      Bt[q] = s;
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < LE3; q += blockDim.x) {
-      const int a = q % LE, rest = q - a;
-      float s = 0.f;
-#pragma unroll
-      for (int p = 0; p < LE; ++p) s = fmaf(sS[0][a * LE + p], Bt[rest + p], s);
-      ze[e * LE3 + q] = s;
+      for (int c = 0; c < LE; ++c) ze[(int64_t)e * LE3 + line + LE2 * c] = A[lu + RS * lv + PS * c];
     }
     __syncthreads();
   }
 }
 
-// prolongation: every local node sums the extended results covering it
+// Assembling prolongation: each local node sums the extended results of ALL
+// elements whose extended box covers its global node, in ascending element
+// order, so every copy of a shared node gets the bit-identical sum and no
+// gather-scatter pass is needed.  Per direction a node has one covering
+// element (its own) or two (own and the lower or upper neighbour); the
+// 2x2x2 combinations are summed z-major, y, x (= ascending element index).
+// A thread handles VW consecutive nodes of one row (i = VW h .. VW h + VW-1).
+template <int LX>
+struct PullVec {
+  static constexpr int VW = LX % 4 == 0 ? 4 : 2;  // nodes per thread (one aligned vector store)
+};
+
 template <int LX>
 __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
                        const Scalars* sc) {
   using X = Ext<LX>;
   constexpr int LE = X::LE, LE2 = X::LE2, LE3 = X::LE3, N = X::N;
-  constexpr int LX2 = LX * LX, LX3 = LX * LX * LX;
+  constexpr int LX2 = LX * LX, LX3 = LX * LX * LX, VW = PullVec<LX>::VW, Q = LX / VW;
+  static_assert(N >= 3, "one neighbour per direction");
   if (sc && sc->done) return;
-  const int64_t n = (int64_t)Ex * Ey * Ez * LX3;
-  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = l / LX3;
-    const int m = (int)(l - e * LX3);
-    const int i = m % LX, j = (m / LX) % LX, k = m / LX2;
-    const int ex = (int)(e % Ex), ey = (int)((e / Ex) % Ey), ez = (int)(e / ((int64_t)Ex * Ey));
-    // per dimension: (element offset, extended index) of the covering elements
-    int ox[3], ax[3], nxc = 1, oy[3], ay[3], nyc = 1, oz[3], az[3], nzc = 1;
-    ox[0] = 0; ax[0] = i + 1;
-    oy[0] = 0; ay[0] = j + 1;
-    oz[0] = 0; az[0] = k + 1;
-    if (i == 1 && ex > 0) { ox[nxc] = -1; ax[nxc++] = N + 2; }
-    if (i == N - 1 && ex < Ex - 1) { ox[nxc] = 1; ax[nxc++] = 0; }
-    if (j == 1 && ey > 0) { oy[nyc] = -1; ay[nyc++] = N + 2; }
-    if (j == N - 1 && ey < Ey - 1) { oy[nyc] = 1; ay[nyc++] = 0; }
-    if (k == 1 && ez > 0) { oz[nzc] = -1; az[nzc++] = N + 2; }
-    if (k == N - 1 && ez < Ez - 1) { oz[nzc] = 1; az[nzc++] = 0; }
-    float acc = 0.f;
-    for (int c = 0; c < nzc; ++c)
-      for (int b = 0; b < nyc; ++b)
-        for (int a = 0; a < nxc; ++a) {
-          const int64_t en = (ex + ox[a]) + (int64_t)Ex * ((ey + oy[b]) + (int64_t)Ey * (ez + oz[c]));
-          acc += ze[en * LE3 + ax[a] + LE * ay[b] + LE2 * az[c]];
+  const int64_t nq = (int64_t)Ex * Ey * Ez * (LX3 / VW);
+  const int64_t sy = (int64_t)Ex * LE3, sz = (int64_t)Ex * Ey * LE3;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq; t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t / (LX3 / VW));
+    const int m = (int)(t - (int64_t)e * (LX3 / VW));
+    const int h = m % Q, j = (m / Q) % LX, k = m / (Q * LX);
+    const int exy = e / Ex, cx = e - exy * Ex, cz = exy / Ey, cy = exy - cz * Ey;
+    const bool ly = j <= 1 && cy > 0, hy = j >= N - 1 && cy < Ey - 1;
+    const bool lz = k <= 1 && cz > 0, hz = k >= N - 1 && cz < Ez - 1;
+    const int64_t y0 = ly ? (cy - 1) * sy + LE * (N + 1 + j) : cy * sy + LE * (j + 1);
+    const int64_t y1 = ly ? cy * sy + LE * (j + 1) : (cy + 1) * sy + LE * (j + 1 - N);
+    const int64_t z0 = lz ? (cz - 1) * sz + LE2 * (N + 1 + k) : cz * sz + LE2 * (k + 1);
+    const int64_t z1 = lz ? cz * sz + LE2 * (k + 1) : (cz + 1) * sz + LE2 * (k + 1 - N);
+    const bool ty = ly || hy, tz = lz || hz;
+    const float* p00 = ze + z0 + y0;
+    const float* p10 = ze + z0 + y1;
+    const float* p01 = ze + z1 + y0;
+    const float* p11 = ze + z1 + y1;
+    float out[VW];
+#pragma unroll
+    for (int q = 0; q < VW; ++q) {
+      const int i = VW * h + q;
+      const bool lx_ = i <= 1 && cx > 0, hx = i >= N - 1 && cx < Ex - 1, tx = lx_ || hx;
+      const int64_t x0 = lx_ ? (int64_t)(cx - 1) * LE3 + (N + 1 + i) : (int64_t)cx * LE3 + (i + 1);
+      const int64_t x1 = lx_ ? (int64_t)cx * LE3 + (i + 1) : (int64_t)(cx + 1) * LE3 + (i + 1 - N);
+      float acc = p00[x0];
+      if (tx) acc += p00[x1];
+      if (ty) {
+        acc += p10[x0];
+        if (tx) acc += p10[x1];
+      }
+      if (tz) {
+        acc += p01[x0];
+        if (tx) acc += p01[x1];
+        if (ty) {
+          acc += p11[x0];
+          if (tx) acc += p11[x1];
         }
-    z[l] = acc;
+      }
+      out[q] = acc;
+    }
+    float* zo = z + (int64_t)e * LX3 + k * LX2 + j * LX + VW * h;
+    if constexpr (VW == 4)
+      *reinterpret_cast<float4*>(zo) = make_float4(out[0], out[1], out[2], out[3]);
+    else
+      *reinterpret_cast<float2*>(zo) = make_float2(out[0], out[1]);
   }
 }
 
@@ -243,6 +327,7 @@ struct ntg_schwarz {
   float* lam = nullptr;  // E x 3 x LE
   float* hc = nullptr;   // E x 2 (h1, h2 element means)
   float* ze = nullptr;   // E x LE^3 extended results
+  int fdm_grid = 0;      // persistent grid of the FDM kernel (blocks resident on all SMs)
   std::vector<double> hl;  // element lengths (host)
 };
 
@@ -281,29 +366,53 @@ static void schwarz_free(ntg_schwarz* s) {
   dev_free(s->S); dev_free(s->lam); dev_free(s->hc); dev_free(s->ze);
 }
 
+namespace ntg {
+namespace sw {
+
+template <int LX>
+int fdm_prepare(ntg_schwarz* w) {
+  using C = FdmCfg<LX>;
+  NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  int per_sm = 0;
+  NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX>, C::THREADS, C::SMEM));
+  const int64_t batches = (w->plan->nelv + C::EPB - 1) / C::EPB;
+  const int64_t cap = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);
+  w->fdm_grid = (int)(batches < cap ? batches : cap);
+  return NTG_OK;
+}
+
+template <int LX>
+int fdm_launch(ntg_schwarz* w, const float* r, cudaStream_t s, const Scalars* sc) {
+  using C = FdmCfg<LX>;
+  k_fdm<LX><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc);
+  NTG_COUNT_LAUNCH();
+  return NTG_OK;
+}
+
+}  // namespace sw
+}  // namespace ntg
+
 int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, const Scalars* sc) {
   ntg_plan* p = w->plan;
-  const int64_t nelv = p->nelv;
-  int grid = (int)(nelv < (int64_t)num_sms() * 16 ? nelv : (int64_t)num_sms() * 16);
   switch (p->lx) {
     case 4:
-      { sw::k_fdm<4><<<grid, 128, 0, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
-      { sw::k_pull<4><<<grid_for(p->n, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(sw::fdm_launch<4>(w, r, s, sc));
+      { sw::k_pull<4><<<grid_for(p->n / sw::PullVec<4>::VW, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
       break;
     case 6:
-      { sw::k_fdm<6><<<grid, 128, 0, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
-      { sw::k_pull<6><<<grid_for(p->n, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(sw::fdm_launch<6>(w, r, s, sc));
+      { sw::k_pull<6><<<grid_for(p->n / sw::PullVec<6>::VW, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
       break;
     case 8:
-      { sw::k_fdm<8><<<grid, 128, 0, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
-      { sw::k_pull<8><<<grid_for(p->n, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(sw::fdm_launch<8>(w, r, s, sc));
+      { sw::k_pull<8><<<grid_for(p->n / sw::PullVec<8>::VW, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
       break;
     default:
       set_error("schwarz: lx=%d not compiled (4, 6, 8)", p->lx);
       return NTG_ERR_UNSUPPORTED;
   }
   NTG_CUDA_TRY(cudaGetLastError());
-  NTG_TRY(gs_add_guarded_f32(p, z, s, sc));
+  // the pull assembles (identical sums on every copy): only the mask remains
   return mask_guarded_f32(p, z, s, sc);
 }
 
@@ -316,6 +425,7 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
   NTG_CHECK_ARG(ex > 0 && ey > 0 && ez > 0 && (int64_t)ex * ey * ez == p->nelv,
                 "ntg_schwarz_create: ex*ey*ez must equal the plan's element count (structured box, x fastest)");
   NTG_CHECK_ARG(p->lx == 4 || p->lx == 6 || p->lx == 8, "ntg_schwarz_create: lx must be 4, 6 or 8");
+  NTG_CHECK_ARG(p->nelv < (int64_t)1 << 30, "ntg_schwarz_create: element count must be below 2^30");
   *out = nullptr;
   ntg_schwarz* s = new ntg_schwarz();
   s->plan = p;
@@ -369,6 +479,8 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
       set_error("ntg_schwarz_create: upload");
       break;
     }
+    st = p->lx == 4 ? sw::fdm_prepare<4>(s) : p->lx == 6 ? sw::fdm_prepare<6>(s) : sw::fdm_prepare<8>(s);
+    if (st) break;
     st = ntg_schwarz_update(s);
   } while (0);
   dev_free(dl);
