@@ -159,7 +159,9 @@ enum TimerId {
   TM_DIR32 = 7, TM_PC32 = 8, TM_COUNT = 16
 };
 // z = M r with the Schwarz preconditioner (schwarz.cu); no-op once sc->done
-int schwarz_apply(ntg_schwarz* sw, float* z, const float* r, cudaStream_t s, const Scalars* sc);
+// z = M r (FP32).  With mult non-null also (r, z)_mult into sc (FinRz{rz_mode}).
+int schwarz_apply(ntg_schwarz* sw, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult = nullptr,
+                  double* part = nullptr, int rz_mode = 0);
 void timer_start(int id, cudaStream_t s);
 void timer_stop(int id, cudaStream_t s);
 

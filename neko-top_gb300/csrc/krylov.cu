@@ -203,7 +203,7 @@ struct FinUpd {
       sc->done = 1;
       return;
     }
-    if (sc->ext_pc) return;  // beta and (r, z) come from k_rz
+    if (sc->ext_pc) return;  // beta and (r, z) come with the preconditioner application
     sc->beta = acc[0] / sc->rz;
     sc->rz = acc[0];
   }
@@ -517,7 +517,7 @@ struct FinRU {
     // a confirmation that failed resumes the iteration: the direction update
     // skipped at the candidate uses the replaced residual
     sc->done = 0;
-    if (sc->ext_pc) return;  // (r, z) of the new residual comes from k_rz
+    if (sc->ext_pc) return;  // (r, z) of the new residual comes with the preconditioner application
     if (mode == 2) sc->beta = acc[1] / sc->rz;
     sc->rz = acc[1];
   }
@@ -525,8 +525,9 @@ struct FinRU {
 
 // ---------------------------------------------------------------------------
 // Explicit-preconditioner variant of the FP32 iteration (Schwarz): the
-// update forms only (r, r); z = M r is applied by its own kernels; k_rz then
-// forms (r, z) and beta; k_dir_z sets p = z + beta p.
+// update forms only (r, r); z = M r is applied by its own kernels, the last
+// of which also forms (r, z) and beta; k_dir_z sets p = z + beta p.
+// Both stream float4s (a scalar tail covers n % 4).
 // ---------------------------------------------------------------------------
 __global__ void k_update_rr(float* __restrict__ y, const float* __restrict__ p, float* __restrict__ r,
                             const float* __restrict__ w, const float* __restrict__ mult, int64_t n,
@@ -534,7 +535,19 @@ __global__ void k_update_rr(float* __restrict__ y, const float* __restrict__ p, 
   if (sc->done) return;
   const float alpha = (float)sc->alpha;
   float rr = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t n4 = n >> 2, g0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = g0; i < n4; i += gs) {
+    float4 y4 = reinterpret_cast<float4*>(y)[i];
+    const float4 p4 = reinterpret_cast<const float4*>(p)[i], w4 = reinterpret_cast<const float4*>(w)[i];
+    const float4 m4 = reinterpret_cast<const float4*>(mult)[i];
+    float4 r4 = reinterpret_cast<float4*>(r)[i];
+    y4.x += alpha * p4.x; y4.y += alpha * p4.y; y4.z += alpha * p4.z; y4.w += alpha * p4.w;
+    r4.x -= alpha * w4.x; r4.y -= alpha * w4.y; r4.z -= alpha * w4.z; r4.w -= alpha * w4.w;
+    reinterpret_cast<float4*>(y)[i] = y4;
+    reinterpret_cast<float4*>(r)[i] = r4;
+    rr += m4.x * r4.x * r4.x + m4.y * r4.y * r4.y + m4.z * r4.z * r4.z + m4.w * r4.w * r4.w;
+  }
+  for (int64_t i = 4 * n4 + g0; i < n; i += gs) {
     y[i] += alpha * p[i];
     const float ri = r[i] - alpha * w[i];
     r[i] = ri;
@@ -544,34 +557,17 @@ __global__ void k_update_rr(float* __restrict__ y, const float* __restrict__ p, 
   grid_reduce<2>(v, part, sc, FinUpd());
 }
 
-struct FinRz {
-  int mode;  // 0 iteration / confirmation: beta = new / rz; 1 replacement: rz only; 3 start: rz, beta = 0
-  __device__ void operator()(const double* acc, Scalars* sc) const {
-    const double rz = acc[0];
-    if (!isfinite(rz) || !(rz > 0.0)) {
-      sc->status = isfinite(rz) ? NTG_BREAKDOWN : NTG_NONFINITE;
-      sc->done = 1;
-      return;
-    }
-    if (mode == 0) sc->beta = rz / sc->rz;
-    if (mode == 3) sc->beta = 0.0;
-    sc->rz = rz;
-  }
-};
-__global__ void k_rz(const float* __restrict__ r, const float* __restrict__ z, const float* __restrict__ mult,
-                     int64_t n, int mode, double* __restrict__ part, Scalars* sc) {
-  if (sc->done) return;
-  float s = 0.f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s += mult[i] * r[i] * z[i];
-  double v[1] = {(double)s};
-  grid_reduce<1>(v, part, sc, FinRz{mode});
-}
 __global__ void k_dir_z(float* __restrict__ p, const float* __restrict__ z, int64_t n, int init, const Scalars* sc) {
   if (sc->done) return;
-  const float beta = (float)sc->beta;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = init ? z[i] : z[i] + beta * p[i];
+  const float beta = init ? 0.f : (float)sc->beta;
+  const int64_t n4 = n >> 2, g0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = g0; i < n4; i += gs) {
+    const float4 z4 = reinterpret_cast<const float4*>(z)[i];
+    float4 p4 = init ? make_float4(0.f, 0.f, 0.f, 0.f) : reinterpret_cast<const float4*>(p)[i];
+    p4.x = z4.x + beta * p4.x; p4.y = z4.y + beta * p4.y; p4.z = z4.z + beta * p4.z; p4.w = z4.w + beta * p4.w;
+    reinterpret_cast<float4*>(p)[i] = p4;
+  }
+  for (int64_t i = 4 * n4 + g0; i < n; i += gs) p[i] = init ? z[i] : z[i] + beta * p[i];
 }
 // start: r = f - w (w null: f); r32 = (float) r; y = 0; sums ff, rr
 __global__ void k_ru_init_pc(const double* __restrict__ f, const double* __restrict__ w, const double* __restrict__ mult,
@@ -909,9 +905,7 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
   };
   // z = M r, then (r, z) in the given mode
   auto precondition = [&](int mode) -> int {
-    NTG_TRY(schwarz_apply(k->sw, z32, r32, s, k->sc));
-    { k_rz<<<G, TPB, 0, s>>>(r32, z32, p->multf, n, mode, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
-    return NTG_OK;
+    return schwarz_apply(k->sw, z32, r32, s, k->sc, p->multf, p->red_part, mode);
   };
   auto replace = [&](int mode) -> int {
     { k_ru_accum<<<G, TPB, 0, s>>>(x, y32, n); NTG_COUNT_LAUNCH(); }

@@ -85,4 +85,20 @@ struct FinPap {
   }
 };
 
+// (r, z) finaliser of a preconditioned CG step.
+struct FinRz {
+  int mode;  // 0 iteration / confirmation: beta = new / rz; 1 replacement: rz only; 3 start: rz, beta = 0
+  __device__ void operator()(const double* acc, Scalars* sc) const {
+    const double rz = acc[0];
+    if (!isfinite(rz) || !(rz > 0.0)) {
+      sc->status = isfinite(rz) ? NTG_BREAKDOWN : NTG_NONFINITE;
+      sc->done = 1;
+      return;
+    }
+    if (mode == 0) sc->beta = rz / sc->rz;
+    if (mode == 3) sc->beta = 0.0;
+    sc->rz = rz;
+  }
+};
+
 }  // namespace ntg

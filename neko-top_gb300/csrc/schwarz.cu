@@ -75,40 +75,76 @@ struct Ext {
 };
 
 // Extended residual -> FDM solve -> extended result for a batch of EPB
-// elements per block, one thread per 1D line of an element's extended box.
-// Each direction pass loads the thread's line from shared memory, applies
-// the 1D eigenvector matrix two outputs at a time with packed FP32 FMAs
-// (__ffma2_rn: operator rows f, f+1 interleaved, the line value duplicated)
-// and writes the line back in place, so a pass needs one buffer and one
-// barrier.  Shared memory per element slot:
-//   P[3][LE/2][LE][2]   forward pairs   P[d][f/2][p][f&1] = S_d[p][f]
-//   Q[3][LE/2][LE][2]   backward pairs  Q[d][a/2][f][a&1] = S_d[a][f]
-//   lam[3][LE], (h1, h2), tile A[a + RS b + PS c]
+// elements per block.  A thread owns two 1D lines of an element's extended
+// box, (u, v) and (u, v + LE/2), in the two halves of packed FP32 FMAs
+// (__ffma2_rn): each direction pass loads the pair of lines from shared
+// memory, applies the 1D eigenvector matrix (rows f, f+1 interleaved, read
+// as float4 broadcasts and shared by both lines) and writes them back in
+// place, so a pass needs one buffer and one barrier.
+//   operator region, per element:  P[3][LE/2][LE][2]  P[d][f/2][p][f&1] = S_d[p][f]
+//                                  Q[3][LE/2][LE][2]  Q[d][a/2][f][a&1] = S_d[a][f]
+//                                  lam[3][LE], (h1, h2)
+//   tile region, per element:      A[a + RS b + PS c]
+// Tile strides: lines of a warp are consecutive (u fastest).  (RS, PS) make
+// the r and s passes (two each) free of bank conflicts and the tile stride
+// TPER keeps warps that span two elements free as well; the single t pass
+// takes two-way conflicts (no stride choice avoids all three passes).
 template <int LX>
 struct FdmCfg {
-  static constexpr int LE = LX + 2, LE2 = LE * LE, LE3 = LE2 * LE;
-  static constexpr int RS = LE + 1, PS = RS * LE + 1;  // odd tile strides (fewer bank conflicts)
-  static constexpr int POFF = 0, QOFF = 3 * LE2, LOFF = 6 * LE2, HOFF = LOFF + 3 * LE, AOFF = (HOFF + 2 + 3) & ~3;
-  static constexpr int PER = (AOFF + PS * LE + 3) & ~3;  // floats per element slot
-  static constexpr int EPB = LX == 8 ? 4 : 8, THREADS = EPB * LE2, MINB = LX == 8 ? 3 : 4;
-  static constexpr size_t SMEM = (size_t)EPB * PER * sizeof(float);
+  static constexpr int LE = LX + 2, LE2 = LE * LE, LE3 = LE2 * LE, TPE = LE2 / 2;
+  static constexpr int RS = LX == 8 ? 17 : LX == 6 ? 9 : 7;
+  static constexpr int PS = LX == 8 ? 170 : LX == 6 ? 72 : 43;
+  static constexpr int SPAN = (LE - 1) * (1 + RS + PS) + 1;
+  static constexpr int TPER = LX == 8 ? 1714 : LX == 6 ? 576 : 257;
+  static constexpr int POFF = 0, QOFF = 3 * LE2, LOFF = 6 * LE2, HOFF = LOFF + 3 * LE;
+  static constexpr int MPER = (HOFF + 2 + 3) & ~3;  // 16-byte aligned operator slots
+  static constexpr int EPB = LX == 4 ? 16 : 8, THREADS = EPB * TPE, MINB = LX == 8 ? 3 : 4;
+  static constexpr size_t SMEM = (size_t)EPB * (MPER + TPER) * sizeof(float);
+  static_assert(LE % 2 == 0 && TPER >= SPAN && THREADS <= 1024, "layout");
 };
 
-// dst[f * ST] = sum_p M[f][p] in[p] for the interleaved pair rows of M
+template <int LE>
+__device__ __forceinline__ float2 dup(float v) { return make_float2(v, v); }
+
+// out(line1, line2)[f * ST] = sum_p M[f][p] in2[p] for both lines of the thread
 template <int LE, int ST>
-__device__ __forceinline__ void fdm_line(const float* __restrict__ M, const float2 (&in)[LE], float* dst) {
+__device__ __forceinline__ void fdm_pair(const float* __restrict__ M, const float2 (&in)[LE], float* d1, float* d2) {
 #pragma unroll
   for (int fp = 0; fp < LE / 2; ++fp) {
     const float* row = M + fp * 2 * LE;
-    float2 acc = make_float2(0.f, 0.f);
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
 #pragma unroll
     for (int p = 0; p < LE; p += 2) {
       const float4 m4 = *reinterpret_cast<const float4*>(row + 2 * p);
-      acc = __ffma2_rn(make_float2(m4.x, m4.y), in[p], acc);
-      acc = __ffma2_rn(make_float2(m4.z, m4.w), in[p + 1], acc);
+      a0 = __ffma2_rn(dup<LE>(m4.x), in[p], a0);
+      a1 = __ffma2_rn(dup<LE>(m4.y), in[p], a1);
+      a0 = __ffma2_rn(dup<LE>(m4.z), in[p + 1], a0);
+      a1 = __ffma2_rn(dup<LE>(m4.w), in[p + 1], a1);
     }
-    dst[(2 * fp) * ST] = acc.x;
-    dst[(2 * fp + 1) * ST] = acc.y;
+    d1[(2 * fp) * ST] = a0.x;
+    d2[(2 * fp) * ST] = a0.y;
+    d1[(2 * fp + 1) * ST] = a1.x;
+    d2[(2 * fp + 1) * ST] = a1.y;
+  }
+}
+
+// the same into registers
+template <int LE>
+__device__ __forceinline__ void fdm_pair_reg(const float* __restrict__ M, const float2 (&in)[LE], float2 (&out)[LE]) {
+#pragma unroll
+  for (int fp = 0; fp < LE / 2; ++fp) {
+    const float* row = M + fp * 2 * LE;
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < LE; p += 2) {
+      const float4 m4 = *reinterpret_cast<const float4*>(row + 2 * p);
+      a0 = __ffma2_rn(dup<LE>(m4.x), in[p], a0);
+      a1 = __ffma2_rn(dup<LE>(m4.y), in[p], a1);
+      a0 = __ffma2_rn(dup<LE>(m4.z), in[p + 1], a0);
+      a1 = __ffma2_rn(dup<LE>(m4.w), in[p + 1], a1);
+    }
+    out[2 * fp] = a0;
+    out[2 * fp + 1] = a1;
   }
 }
 
@@ -118,94 +154,119 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
           const float* __restrict__ lam, const float* __restrict__ hc, int Ex, int Ey, int Ez,
           const Scalars* sc) {
   using C = FdmCfg<LX>;
-  constexpr int LE = C::LE, LE2 = C::LE2, LE3 = C::LE3, N = LX - 1, RS = C::RS, PS = C::PS;
-  constexpr int EPB = C::EPB, PER = C::PER, LX2 = LX * LX, LX3 = LX2 * LX;
-  static_assert(LE % 2 == 0 && C::THREADS <= 1024, "pairs of outputs; one thread per line");
+  constexpr int LE = C::LE, LE2 = C::LE2, LE3 = C::LE3, N = LX - 1, RS = C::RS, PS = C::PS, TPE = C::TPE;
+  constexpr int EPB = C::EPB, LX2 = LX * LX, LX3 = LX2 * LX, H = LE / 2;
   if (sc && sc->done) return;
   extern __shared__ __align__(16) float smem[];
   const int nelv = Ex * Ey * Ez;
-  const int tid = threadIdx.x, el = tid / LE2, line = tid - el * LE2;
-  const int lu = line % LE, lv = line / LE;
-  float* sl = smem + el * PER;
-  float* A = sl + C::AOFF;
+  const int tid = threadIdx.x, el = tid / TPE, tl = tid - el * TPE;
+  const int u = tl % LE, v1 = tl / LE, v2 = v1 + H;  // lines (u, v1) and (u, v2); tl + TPE = u + LE v2
+  float* ms = smem + el * C::MPER;
+  float* A = smem + EPB * C::MPER + el * C::TPER;
   float2 in[LE];
   for (int e0 = blockIdx.x * EPB; e0 < nelv; e0 += gridDim.x * EPB) {
-    // operators of the batch: the thread's entry (a, f) = (lv, lu) of
-    // S[e][d] (coalesced over lines) -> pair rows P and Q
     const int e = e0 + el;
-    {
-      const int aa = lv, ff = lu;
+    const bool live = e < nelv;
+    // operators: entries (a, f) = (v, u) of S[e][d] for both lines (coalesced over lines)
 #pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const float v = e < nelv ? S[(int64_t)e * 3 * LE2 + d * LE2 + line] : 0.f;
-        sl[C::POFF + d * LE2 + (ff >> 1) * 2 * LE + 2 * aa + (ff & 1)] = v;
-        sl[C::QOFF + d * LE2 + (aa >> 1) * 2 * LE + 2 * ff + (aa & 1)] = v;
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int aa = q ? v2 : v1, ff = u;
+        const float val = live ? S[(int64_t)e * 3 * LE2 + d * LE2 + tl + q * TPE] : 0.f;
+        ms[C::POFF + d * LE2 + (ff >> 1) * 2 * LE + 2 * aa + (ff & 1)] = val;
+        ms[C::QOFF + d * LE2 + (aa >> 1) * 2 * LE + 2 * ff + (aa & 1)] = val;
       }
-      if (line < 3 * LE) sl[C::LOFF + line] = e < nelv ? lam[(int64_t)e * 3 * LE + line] : 0.f;
-      if (line < 2) sl[C::HOFF + line] = e < nelv ? hc[2 * (int64_t)e + line] : 1.f;
     }
-    // gather R_e r: the thread's column (a, b) = (lu, lv) over c
-    if (e < nelv) {
+    if (tl < 3 * LE) ms[C::LOFF + tl] = live ? lam[(int64_t)e * 3 * LE + tl] : 0.f;
+    if (tl < 2) ms[C::HOFF + tl] = live ? hc[2 * (int64_t)e + tl] : 1.f;
+    // gather R_e r: columns (a, b) = (u, v1), (u, v2) over c
+    if (live) {
       const int exy = e / Ex, ex = e - exy * Ex, ez = exy / Ey, ey = exy - ez * Ey;
-      int i = lu - 1, j = lv - 1, dx = 0, dy = 0;
+      int i = u - 1, dx = 0;
       if (i < 0) { dx = -1; i = N - 1; } else if (i > N) { dx = 1; i = 1; }
-      if (j < 0) { dy = -1; j = N - 1; } else if (j > N) { dy = 1; j = 1; }
-      const int nx = ex + dx, ny = ey + dy;
-      const bool okxy = nx >= 0 && nx < Ex && ny >= 0 && ny < Ey;
-      const float* rc = r + (int64_t)(nx + Ex * (ny + Ey * ez)) * LX3 + i + LX * j;
+      const int nx = ex + dx;
       const int64_t zs = (int64_t)Ex * Ey * LX3;
-      float* Ac = A + lu + RS * lv;
-      Ac[0] = okxy && ez > 0 ? rc[(N - 1) * LX2 - zs] : 0.f;
 #pragma unroll
-      for (int c = 1; c < LE - 1; ++c) Ac[PS * c] = okxy ? rc[(c - 1) * LX2] : 0.f;
-      Ac[PS * (LE - 1)] = okxy && ez < Ez - 1 ? rc[LX2 + zs] : 0.f;
+      for (int q = 0; q < 2; ++q) {
+        const int vb = q ? v2 : v1;
+        int j = vb - 1, dy = 0;
+        if (j < 0) { dy = -1; j = N - 1; } else if (j > N) { dy = 1; j = 1; }
+        const int ny = ey + dy;
+        const bool okxy = nx >= 0 && nx < Ex && ny >= 0 && ny < Ey;
+        const float* rc = r + (int64_t)(nx + Ex * (ny + Ey * ez)) * LX3 + i + LX * j;
+        float* Ac = A + u + RS * vb;
+        Ac[0] = okxy && ez > 0 ? rc[(N - 1) * LX2 - zs] : 0.f;
+#pragma unroll
+        for (int c = 1; c < LE - 1; ++c) Ac[PS * c] = okxy ? rc[(c - 1) * LX2] : 0.f;
+        Ac[PS * (LE - 1)] = okxy && ez < Ez - 1 ? rc[LX2 + zs] : 0.f;
+      }
     }
     __syncthreads();
-    const float* P = sl + C::POFF;
-    const float* Q = sl + C::QOFF;
-    // r forward: line (b, c) = (lu, lv), along a
-#pragma unroll
-    for (int p = 0; p < LE; ++p) { const float v = A[p + RS * lu + PS * lv]; in[p] = make_float2(v, v); }
-    fdm_line<LE, 1>(P, in, A + RS * lu + PS * lv);
-    __syncthreads();
-    // s forward: line (a, c) = (lu, lv), along b
-#pragma unroll
-    for (int p = 0; p < LE; ++p) { const float v = A[lu + RS * p + PS * lv]; in[p] = make_float2(v, v); }
-    fdm_line<LE, RS>(P + LE2, in, A + lu + PS * lv);
-    __syncthreads();
-    // t forward, scale by the inverse eigenvalue sum, t back: line (a, b) = (lu, lv)
+    const float* P = ms + C::POFF;
+    const float* Q = ms + C::QOFF;
+    // r forward: lines (b, c) = (u, v) along a
     {
-      const float* L = sl + C::LOFF;
-      const float h1 = sl[C::HOFF], h2 = sl[C::HOFF + 1];
-      const float lab = L[lu] + L[LE + lv];
-      float* At = A + lu + RS * lv;
+      float* l1 = A + RS * u + PS * v1;
+      float* l2 = A + RS * u + PS * v2;
 #pragma unroll
-      for (int p = 0; p < LE; ++p) { const float v = At[PS * p]; in[p] = make_float2(v, v); }
-      float t[LE];
-      fdm_line<LE, 1>(P + 2 * LE2, in, t);
+      for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[p], l2[p]);
+      fdm_pair<LE, 1>(P, in, l1, l2);
+    }
+    __syncthreads();
+    // s forward: lines (a, c) = (u, v) along b
+    {
+      float* l1 = A + u + PS * v1;
+      float* l2 = A + u + PS * v2;
+#pragma unroll
+      for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[RS * p], l2[RS * p]);
+      fdm_pair<LE, RS>(P + LE2, in, l1, l2);
+    }
+    __syncthreads();
+    // t forward, scale by the inverse eigenvalue sums, t back: lines (a, b) = (u, v)
+    {
+      float* l1 = A + u + RS * v1;
+      float* l2 = A + u + RS * v2;
+      const float* L = ms + C::LOFF;
+      const float h1 = ms[C::HOFF], h2 = ms[C::HOFF + 1];
+      const float la1 = L[u] + L[LE + v1], la2 = L[u] + L[LE + v2];
+#pragma unroll
+      for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[PS * p], l2[PS * p]);
+      float2 t[LE];
+      fdm_pair_reg<LE>(P + 2 * LE2, in, t);
 #pragma unroll
       for (int f = 0; f < LE; ++f) {
-        const float v = __fdividef(t[f], h1 * (lab + L[2 * LE + f]) + h2);
-        in[f] = make_float2(v, v);
+        const float lf = L[2 * LE + f];
+        in[f] = make_float2(__fdividef(t[f].x, h1 * (la1 + lf) + h2), __fdividef(t[f].y, h1 * (la2 + lf) + h2));
       }
-      fdm_line<LE, PS>(Q + 2 * LE2, in, At);
+      fdm_pair<LE, PS>(Q + 2 * LE2, in, l1, l2);
     }
     __syncthreads();
     // s back
+    {
+      float* l1 = A + u + PS * v1;
+      float* l2 = A + u + PS * v2;
 #pragma unroll
-    for (int p = 0; p < LE; ++p) { const float v = A[lu + RS * p + PS * lv]; in[p] = make_float2(v, v); }
-    fdm_line<LE, RS>(Q + LE2, in, A + lu + PS * lv);
+      for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[RS * p], l2[RS * p]);
+      fdm_pair<LE, RS>(Q + LE2, in, l1, l2);
+    }
     __syncthreads();
     // r back
+    {
+      float* l1 = A + RS * u + PS * v1;
+      float* l2 = A + RS * u + PS * v2;
 #pragma unroll
-    for (int p = 0; p < LE; ++p) { const float v = A[p + RS * lu + PS * lv]; in[p] = make_float2(v, v); }
-    fdm_line<LE, 1>(Q, in, A + RS * lu + PS * lv);
+      for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[p], l2[p]);
+      fdm_pair<LE, 1>(Q, in, l1, l2);
+    }
     __syncthreads();
-    // copy-out: the thread's column (a, b) = (lu, lv) of ze[e][a + LE b + LE2 c]
-    // (consecutive lines -> consecutive addresses)
-    if (e < nelv) {
+    // copy-out: columns (a, b) of ze[e][a + LE b + LE2 c] (consecutive lines -> consecutive addresses)
+    if (live) {
 #pragma unroll
-      for (int c = 0; c < LE; ++c) ze[(int64_t)e * LE3 + line + LE2 * c] = A[lu + RS * lv + PS * c];
+      for (int c = 0; c < LE; ++c) {
+        ze[(int64_t)e * LE3 + tl + LE2 * c] = A[u + RS * v1 + PS * c];
+        ze[(int64_t)e * LE3 + tl + TPE + LE2 * c] = A[u + RS * v2 + PS * c];
+      }
     }
     __syncthreads();
   }
@@ -223,9 +284,12 @@ struct PullVec {
   static constexpr int VW = LX % 4 == 0 ? 4 : 2;  // nodes per thread (one aligned vector store)
 };
 
-template <int LX>
+// DOT: also (r, z)_mult, reduced deterministically and finalised by FinRz
+// (the mask applied afterwards does not change it: r vanishes on masked nodes).
+template <int LX, bool DOT>
 __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
-                       const Scalars* sc) {
+                       const float* __restrict__ r, const float* __restrict__ mult, int mode,
+                       double* __restrict__ part, Scalars* sc) {
   using X = Ext<LX>;
   constexpr int LE = X::LE, LE2 = X::LE2, LE3 = X::LE3, N = X::N;
   constexpr int LX2 = LX * LX, LX3 = LX * LX * LX, VW = PullVec<LX>::VW, Q = LX / VW;
@@ -233,10 +297,25 @@ __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int 
   if (sc && sc->done) return;
   const int64_t nq = (int64_t)Ex * Ey * Ez * (LX3 / VW);
   const int64_t sy = (int64_t)Ex * LE3, sz = (int64_t)Ex * Ey * LE3;
+  float rz = 0.f;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq; t += (int64_t)gridDim.x * blockDim.x) {
     const int e = (int)(t / (LX3 / VW));
     const int m = (int)(t - (int64_t)e * (LX3 / VW));
     const int h = m % Q, j = (m / Q) % LX, k = m / (Q * LX);
+    const int64_t o = (int64_t)e * LX3 + k * LX2 + j * LX + VW * h;
+    // the dot's operands first: their loads overlap the gather below
+    float rv[VW], mv[VW];
+    if constexpr (DOT) {
+      if constexpr (VW == 4) {
+        const float4 r4 = *reinterpret_cast<const float4*>(r + o), m4 = *reinterpret_cast<const float4*>(mult + o);
+        rv[0] = r4.x; rv[1] = r4.y; rv[2] = r4.z; rv[3] = r4.w;
+        mv[0] = m4.x; mv[1] = m4.y; mv[2] = m4.z; mv[3] = m4.w;
+      } else {
+        const float2 r2 = *reinterpret_cast<const float2*>(r + o), m2 = *reinterpret_cast<const float2*>(mult + o);
+        rv[0] = r2.x; rv[1] = r2.y;
+        mv[0] = m2.x; mv[1] = m2.y;
+      }
+    }
     const int exy = e / Ex, cx = e - exy * Ex, cz = exy / Ey, cy = exy - cz * Ey;
     const bool ly = j <= 1 && cy > 0, hy = j >= N - 1 && cy < Ey - 1;
     const bool lz = k <= 1 && cz > 0, hz = k >= N - 1 && cz < Ez - 1;
@@ -272,11 +351,18 @@ __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int 
       }
       out[q] = acc;
     }
-    float* zo = z + (int64_t)e * LX3 + k * LX2 + j * LX + VW * h;
     if constexpr (VW == 4)
-      *reinterpret_cast<float4*>(zo) = make_float4(out[0], out[1], out[2], out[3]);
+      *reinterpret_cast<float4*>(z + o) = make_float4(out[0], out[1], out[2], out[3]);
     else
-      *reinterpret_cast<float2*>(zo) = make_float2(out[0], out[1]);
+      *reinterpret_cast<float2*>(z + o) = make_float2(out[0], out[1]);
+    if constexpr (DOT) {
+#pragma unroll
+      for (int q = 0; q < VW; ++q) rz += mv[q] * rv[q] * out[q];
+    }
+  }
+  if constexpr (DOT) {
+    double v[1] = {(double)rz};
+    grid_reduce<1>(v, part, sc, FinRz{mode});
   }
 }
 
@@ -392,20 +478,39 @@ int fdm_launch(ntg_schwarz* w, const float* r, cudaStream_t s, const Scalars* sc
 }  // namespace sw
 }  // namespace ntg
 
-int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, const Scalars* sc) {
+namespace ntg {
+namespace sw {
+
+template <int LX>
+int pull_launch(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
+                double* part, int mode) {
+  const int g = grid_for(w->plan->n / PullVec<LX>::VW, 256);
+  if (mult)
+    k_pull<LX, true><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, r, mult, mode, part, sc);
+  else
+    k_pull<LX, false><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, nullptr, nullptr, 0, nullptr, sc);
+  NTG_COUNT_LAUNCH();
+  return NTG_OK;
+}
+
+}  // namespace sw
+}  // namespace ntg
+
+int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
+                       double* part, int rz_mode) {
   ntg_plan* p = w->plan;
   switch (p->lx) {
     case 4:
       NTG_TRY(sw::fdm_launch<4>(w, r, s, sc));
-      { sw::k_pull<4><<<grid_for(p->n / sw::PullVec<4>::VW, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(sw::pull_launch<4>(w, z, r, s, sc, mult, part, rz_mode));
       break;
     case 6:
       NTG_TRY(sw::fdm_launch<6>(w, r, s, sc));
-      { sw::k_pull<6><<<grid_for(p->n / sw::PullVec<6>::VW, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(sw::pull_launch<6>(w, z, r, s, sc, mult, part, rz_mode));
       break;
     case 8:
       NTG_TRY(sw::fdm_launch<8>(w, r, s, sc));
-      { sw::k_pull<8><<<grid_for(p->n / sw::PullVec<8>::VW, 256), 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, sc); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(sw::pull_launch<8>(w, z, r, s, sc, mult, part, rz_mode));
       break;
     default:
       set_error("schwarz: lx=%d not compiled (4, 6, 8)", p->lx);
