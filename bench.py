@@ -236,15 +236,15 @@ def run_ours(args, ws, rank, local):
         return run_kernels_only(args, pkg, coef, f, dev)
     n = coef.n
     pc = args.pc
-    if pc == "auto":  # Schwarz for the pressure-Poisson cases, Jacobi under Brinkman penalisation
-        pc = "schwarz" if cfg["case"] == "poisson_fourier" else "jacobi"
+    if pc == "auto":  # two-level Schwarz for the pressure-Poisson cases, Jacobi under Brinkman penalisation
+        pc = "schwarz2" if cfg["case"] == "poisson_fourier" else "jacobi"
     args.pc_used = pc
     sw = None
     if args.method == "cg_mixed":
         ksp_mx = pkg.krylov_solver_factory(coef, "cg_mixed", 50000, RTOL)
         ksp_mx.set_inner(args.delta, 1)
-        if pc == "schwarz":
-            sw = pkg.schwarz_t(coef)
+        if pc in ("schwarz", "schwarz2"):
+            sw = pkg.schwarz_t(coef, coarse=pc == "schwarz2")
             ksp_mx.set_schwarz(sw)
     else:
         ksp_mx = pkg.krylov_solver_factory(coef, "fcg_mixed", 200, RTOL)
@@ -493,8 +493,8 @@ def main(argv=None):
     p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     p.add_argument("--method", choices=["cg_mixed", "fcg_mixed"], default="cg_mixed")
     p.add_argument("--delta", type=float, default=0.1, help="reliable-update threshold of cg_mixed")
-    p.add_argument("--pc", choices=["auto", "jacobi", "schwarz"], default="auto",
-                   help="FP32 preconditioner of cg_mixed (auto: Schwarz for Poisson, Jacobi for Brinkman)")
+    p.add_argument("--pc", choices=["auto", "jacobi", "schwarz", "schwarz2"], default="auto",
+                   help="FP32 preconditioner of cg_mixed (auto: two-level Schwarz for Poisson, Jacobi for Brinkman)")
     p.add_argument("--inner-rtol", type=float, default=1e-4)
     p.add_argument("--inner-max", type=int, default=2000)
     p.add_argument("--fp64-steps", type=int, default=2)

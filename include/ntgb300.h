@@ -213,8 +213,15 @@ int ntg_pc_jacobi_get(const ntg_plan* plan, double* dinv_d);
 /* ---------------------------------------------------------------------- */
 int ntg_schwarz_create(ntg_plan* plan, int ex, int ey, int ez, const double* x_d, const double* y_d,
                        const double* z_d, ntg_schwarz** sw);
-/* refresh the element means of h1 / h2 after ntg_coef_set */
+/* refresh the element means of h1 / h2 after ntg_coef_set (and, with the  */
+/* coarse level on, its Dirichlet faces from the plan's mask and h1/h2)    */
 int ntg_schwarz_update(ntg_schwarz* sw);
+/* Coarse level on/off: adds P A_c^-1 P^T r, A_c the separable Q1 operator */
+/* on the (ex+1)(ey+1)(ez+1) element vertices (fast diagonalisation),     */
+/* P trilinear interpolation to the GLL nodes -- the coarse-grid part of   */
+/* the Schwarz-multigrid preconditioner, here solved directly.  A face     */
+/* whose nodes are all masked is Dirichlet on the coarse grid.             */
+int ntg_schwarz_set_coarse(ntg_schwarz* sw, int enable);
 int ntg_schwarz_destroy(ntg_schwarz* sw);
 /* z = M r (FP32; assembled and masked) */
 int ntg_schwarz_apply(ntg_schwarz* sw, float* z_d, const float* r_d);

@@ -314,9 +314,11 @@ class _ksp:
 
 class schwarz_t:
     """Overlapping additive Schwarz preconditioner (FP32, fast-diagonalisation
-    local solves) for a structured box coef_t built by coef_t.box."""
+    local solves) for a structured box coef_t built by coef_t.box.  With
+    ``coarse=True`` it adds the coarse-grid correction on the element
+    vertices (two-level Schwarz; the coarse part of Neko's 'hsmg')."""
 
-    def __init__(self, coef: coef_t):
+    def __init__(self, coef: coef_t, coarse: bool = False):
         if not hasattr(coef, "box_dims"):
             raise ValueError("schwarz_t needs a structured box mesh (coef_t.box)")
         ex, ey, ez = coef.box_dims
@@ -325,13 +327,17 @@ class schwarz_t:
                                        C.byref(h)))
         self._h = h
         self.coef = coef
+        self.coarse = bool(coarse)
+        if coarse:
+            check(lib().ntg_schwarz_set_coarse(self._h, 1))
 
     @property
     def handle(self):
         return self._h
 
     def update(self):
-        """Refresh the element means of h1/h2 after coef_t.set_coefs."""
+        """Refresh the element means of h1/h2 after coef_t.set_coefs (and the
+        coarse level's Dirichlet faces after coef_t.set_mask)."""
         check(lib().ntg_schwarz_update(self._h))
 
     def apply(self, z, r):

@@ -187,5 +187,7 @@ int build_gs_classes(ntg_plan* p);
 template <typename T>
 int gs_cls_launch(ntg_plan* p, T* u, int op, cudaStream_t s, const Scalars* sc);
 int grid_for(int64_t work, int threads);
+// GLL nodes, weights and differentiation matrix of lx points
+void gll_basis(int lx, double* xi, double* w, double* D);
 int num_sms();
 }  // namespace ntg

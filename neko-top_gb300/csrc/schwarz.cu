@@ -89,6 +89,11 @@ struct Ext {
 // the r and s passes (two each) free of bank conflicts and the tile stride
 // TPER keeps warps that span two elements free as well; the single t pass
 // takes two-way conflicts (no stride choice avoids all three passes).
+// linear (Q1) basis at the GLL nodes, for the coarse level
+struct CoarsePhi {
+  float p[2][NTG_LXMAX];  // p[0][i] = (1 - xi_i) / 2, p[1][i] = (1 + xi_i) / 2
+};
+
 template <int LX>
 struct FdmCfg {
   static constexpr int LE = LX + 2, LE2 = LE * LE, LE3 = LE2 * LE, TPE = LE2 / 2;
@@ -99,9 +104,27 @@ struct FdmCfg {
   static constexpr int POFF = 0, QOFF = 3 * LE2, LOFF = 6 * LE2, HOFF = LOFF + 3 * LE;
   static constexpr int MPER = (HOFF + 2 + 3) & ~3;  // 16-byte aligned operator slots
   static constexpr int EPB = LX == 4 ? 16 : 8, THREADS = EPB * TPE, MINB = LX == 8 ? 3 : 4;
-  static constexpr size_t SMEM = (size_t)EPB * (MPER + TPER) * sizeof(float);
+  // coarse restriction partials (8 per thread): in the tile rows' padding
+  // (a in [LE, RS), two rows per thread) when it is wide enough, else after the tiles
+  static constexpr bool HOLES = 2 * (RS - LE) >= 8;
+  static constexpr int RED = HOLES ? 0 : EPB * TPE * 8;
+  static constexpr size_t SMEM = ((size_t)EPB * (MPER + TPER) + RED) * sizeof(float);
   static_assert(LE % 2 == 0 && TPER >= SPAN && THREADS <= 1024, "layout");
 };
+
+// slot v of thread tl's coarse partials (A: the element's tile, red: the
+// block's partial region, el: element slot)
+template <int LX>
+__device__ __forceinline__ float* crs_slot(float* A, float* red, int el, int tl, int v) {
+  using C = FdmCfg<LX>;
+  if constexpr (C::HOLES) {
+    constexpr int W = C::RS - C::LE;
+    const int b = tl % C::LE, c = tl / C::LE + (v < W ? 0 : C::LE / 2);
+    return A + C::LE + (v < W ? v : v - W) + C::RS * b + C::PS * c;
+  } else {
+    return red + (el * C::TPE + tl) * 8 + v;
+  }
+}
 
 template <int LE>
 __device__ __forceinline__ float2 dup(float v) { return make_float2(v, v); }
@@ -152,7 +175,7 @@ template <int LX>
 __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
     k_fdm(const float* __restrict__ r, float* __restrict__ ze, const float* __restrict__ S,
           const float* __restrict__ lam, const float* __restrict__ hc, int Ex, int Ey, int Ez,
-          const Scalars* sc) {
+          const Scalars* sc, float* __restrict__ corner, CoarsePhi ph) {
   using C = FdmCfg<LX>;
   constexpr int LE = C::LE, LE2 = C::LE2, LE3 = C::LE3, N = LX - 1, RS = C::RS, PS = C::PS, TPE = C::TPE;
   constexpr int EPB = C::EPB, LX2 = LX * LX, LX3 = LX2 * LX, H = LE / 2;
@@ -163,6 +186,13 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
   const int u = tl % LE, v1 = tl / LE, v2 = v1 + H;  // lines (u, v1) and (u, v2); tl + TPE = u + LE v2
   float* ms = smem + el * C::MPER;
   float* A = smem + EPB * C::MPER + el * C::TPER;
+  float* red = smem + EPB * (C::MPER + C::TPER);
+  __shared__ float sp[2][LX];  // Q1 basis at the GLL nodes
+  if (tid == 0) {
+#pragma unroll
+    for (int t = 0; t < 2 * LX; ++t) sp[t / LX][t % LX] = ph.p[t / LX][t % LX];  // constant indices
+  }
+  __syncthreads();
   float2 in[LE];
   for (int e0 = blockIdx.x * EPB; e0 < nelv; e0 += gridDim.x * EPB) {
     const int e = e0 + el;
@@ -187,6 +217,9 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       if (i < 0) { dx = -1; i = N - 1; } else if (i > N) { dx = 1; i = 1; }
       const int nx = ex + dx;
       const int64_t zs = (int64_t)Ex * Ey * LX3;
+      float part[8];
+#pragma unroll
+      for (int v = 0; v < 8; ++v) part[v] = 0.f;
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         const int vb = q ? v2 : v1;
@@ -197,9 +230,30 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
         const float* rc = r + (int64_t)(nx + Ex * (ny + Ey * ez)) * LX3 + i + LX * j;
         float* Ac = A + u + RS * vb;
         Ac[0] = okxy && ez > 0 ? rc[(N - 1) * LX2 - zs] : 0.f;
+        // own-element columns also feed the coarse restriction:
+        // sum_k phi_vz(k) r / multiplicity, per column, then x / y weights
+        float s0 = 0.f, s1 = 0.f;
 #pragma unroll
-        for (int c = 1; c < LE - 1; ++c) Ac[PS * c] = okxy ? rc[(c - 1) * LX2] : 0.f;
+        for (int c = 1; c < LE - 1; ++c) {
+          const float val = okxy ? rc[(c - 1) * LX2] : 0.f;
+          Ac[PS * c] = val;
+          const int k = c - 1;
+          const float wz = ((k == 0 && ez > 0) || (k == N && ez < Ez - 1)) ? 0.5f : 1.f;
+          s0 = fmaf(sp[0][k] * wz, val, s0);
+          s1 = fmaf(sp[1][k] * wz, val, s1);
+        }
         Ac[PS * (LE - 1)] = okxy && ez < Ez - 1 ? rc[LX2 + zs] : 0.f;
+        if (corner && dx == 0 && dy == 0) {
+          const float wx = ((i == 0 && ex > 0) || (i == N && ex < Ex - 1)) ? 0.5f : 1.f;
+          const float wy = ((j == 0 && ey > 0) || (j == N && ey < Ey - 1)) ? 0.5f : 1.f;
+#pragma unroll
+          for (int v = 0; v < 8; ++v)
+            part[v] = fmaf(sp[v & 1][i] * wx * (sp[(v >> 1) & 1][j] * wy), (v >> 2) ? s1 : s0, part[v]);
+        }
+      }
+      if (corner) {
+#pragma unroll
+        for (int v = 0; v < 8; ++v) *crs_slot<LX>(A, red, el, tl, v) = part[v];
       }
     }
     __syncthreads();
@@ -260,6 +314,12 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       fdm_pair<LE, 1>(Q, in, l1, l2);
     }
     __syncthreads();
+    // coarse restriction of the element: 8 threads sum the partials in order
+    if (corner && live && tl < 8) {
+      float acc = 0.f;
+      for (int t = 0; t < TPE; ++t) acc += *crs_slot<LX>(A, red, el, t, tl);
+      corner[(int64_t)e * 8 + tl] = acc;
+    }
     // copy-out: columns (a, b) of ze[e][a + LE b + LE2 c] (consecutive lines -> consecutive addresses)
     if (live) {
 #pragma unroll
@@ -271,6 +331,146 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
     __syncthreads();
   }
 }
+
+// ---------------------------------------------------------------------------
+// Coarse level: Q1 on the element vertices of the box.
+//
+//   z += P A_c^{-1} P^T r
+//
+// P interpolates vertex values trilinearly (in reference coordinates) to the
+// GLL nodes; P^T r sums, per vertex, phi_v(node) r(node) / multiplicity over
+// the local nodes of the adjacent elements (each global node once).  A_c is
+// the separable Q1 operator on the vertex grid,
+//   h1 (Mz x My x Kx + Mz x Ky x Mx + Kz x My x Mx) + h2 (Mz x My x Mx),
+// with 1D linear-element stiffness K and consistent mass M assembled from the
+// mean element length of each slab -- the Galerkin operator P^T A P itself on
+// an undeformed box with constant h1, h2 -- and Dirichlet vertices removed on
+// fully masked faces.  It is inverted by fast diagonalisation (three 1D
+// generalised eigenproblems); a singular (all-Neumann) mode gets zero.
+// ---------------------------------------------------------------------------
+struct CoarseDims {
+  int Ex, Ey, Ez;         // elements per direction (vertex grid (Ex+1) x (Ey+1) x (Ez+1))
+  int lo[3], m[3];        // first active vertex and active count per direction
+  float h1, h2, dmin;     // coefficients; eigenvalue sums below dmin are the null mode
+};
+
+// x then y forward transforms on one active z-plane; the plane's residual is
+// gathered from the corner sums of the adjacent elements (ascending element order)
+__global__ void __launch_bounds__(256)
+    k_crs_xy(const float* __restrict__ corner, const float* __restrict__ Sx, const float* __restrict__ Sy,
+             float* __restrict__ work, CoarseDims d, const Scalars* sc) {
+  if (sc && sc->done) return;
+  extern __shared__ __align__(16) float sm[];
+  const int m0 = d.m[0], m1 = d.m[1], zi = blockIdx.x, gz = d.lo[2] + zi;
+  float* T = sm;
+  float* U = T + m0 * m1;
+  float* sx = U + m0 * m1;
+  float* sy = sx + m0 * m0;
+  for (int q = threadIdx.x; q < m0 * m0; q += blockDim.x) sx[q] = Sx[q];
+  for (int q = threadIdx.x; q < m1 * m1; q += blockDim.x) sy[q] = Sy[q];
+  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
+    const int gx = d.lo[0] + q % m0, gy = d.lo[1] + q / m0;
+    float acc = 0.f;
+    for (int ez = gz - 1; ez <= gz; ++ez) {
+      if (ez < 0 || ez >= d.Ez) continue;
+      for (int ey = gy - 1; ey <= gy; ++ey) {
+        if (ey < 0 || ey >= d.Ey) continue;
+        for (int ex = gx - 1; ex <= gx; ++ex) {
+          if (ex < 0 || ex >= d.Ex) continue;
+          const int64_t e = ex + (int64_t)d.Ex * (ey + (int64_t)d.Ey * ez);
+          acc += corner[e * 8 + (gx - ex) + 2 * (gy - ey) + 4 * (gz - ez)];
+        }
+      }
+    }
+    T[q] = acc;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
+    const int f = q % m0, y = q / m0;
+    float s = 0.f;
+    for (int x = 0; x < m0; ++x) s = fmaf(sx[x * m0 + f], T[y * m0 + x], s);
+    U[q] = s;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
+    const int f = q % m0, g = q / m0;
+    float s = 0.f;
+    for (int y = 0; y < m1; ++y) s = fmaf(sy[y * m1 + g], U[y * m0 + f], s);
+    work[f + (int64_t)m0 * (g + (int64_t)m1 * zi)] = s;
+  }
+}
+
+// z forward, scale by the inverse eigenvalue sums, z back, on one y-index g
+__global__ void __launch_bounds__(256)
+    k_crs_z(float* __restrict__ work, const float* __restrict__ Sz, const float* __restrict__ lam, CoarseDims d,
+            const Scalars* sc) {
+  if (sc && sc->done) return;
+  extern __shared__ __align__(16) float sm[];
+  const int m0 = d.m[0], m1 = d.m[1], m2 = d.m[2], g = blockIdx.x;
+  float* V = sm;
+  float* W = V + m2 * m0;
+  float* sz = W + m2 * m0;
+  for (int q = threadIdx.x; q < m2 * m2; q += blockDim.x) sz[q] = Sz[q];
+  for (int q = threadIdx.x; q < m2 * m0; q += blockDim.x) {
+    const int f = q % m0, z = q / m0;
+    V[q] = work[f + (int64_t)m0 * (g + (int64_t)m1 * z)];
+  }
+  __syncthreads();
+  const float* lx = lam;
+  const float* ly = lam + m0;
+  const float* lz = lam + m0 + m1;
+  for (int q = threadIdx.x; q < m2 * m0; q += blockDim.x) {
+    const int f = q % m0, h = q / m0;
+    float s = 0.f;
+    for (int z = 0; z < m2; ++z) s = fmaf(sz[z * m2 + h], V[z * m0 + f], s);
+    const float D = d.h1 * (lx[f] + ly[g] + lz[h]) + d.h2;
+    W[q] = D > d.dmin ? s / D : 0.f;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < m2 * m0; q += blockDim.x) {
+    const int f = q % m0, z = q / m0;
+    float s = 0.f;
+    for (int h = 0; h < m2; ++h) s = fmaf(sz[z * m2 + h], W[h * m0 + f], s);
+    work[f + (int64_t)m0 * (g + (int64_t)m1 * z)] = s;
+  }
+}
+
+// y then x back transforms on one active z-plane, into the full vertex grid uc
+__global__ void __launch_bounds__(256)
+    k_crs_yx(const float* __restrict__ work, const float* __restrict__ Sx, const float* __restrict__ Sy,
+             float* __restrict__ uc, CoarseDims d, const Scalars* sc) {
+  if (sc && sc->done) return;
+  extern __shared__ __align__(16) float sm[];
+  const int m0 = d.m[0], m1 = d.m[1], zi = blockIdx.x;
+  float* T = sm;
+  float* U = T + m0 * m1;
+  float* sx = U + m0 * m1;
+  float* sy = sx + m0 * m0;
+  for (int q = threadIdx.x; q < m0 * m0; q += blockDim.x) sx[q] = Sx[q];
+  for (int q = threadIdx.x; q < m1 * m1; q += blockDim.x) sy[q] = Sy[q];
+  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) T[q] = work[q + (int64_t)m0 * m1 * zi];
+  __syncthreads();
+  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
+    const int f = q % m0, y = q / m0;
+    float s = 0.f;
+    for (int g = 0; g < m1; ++g) s = fmaf(sy[y * m1 + g], T[g * m0 + f], s);
+    U[q] = s;
+  }
+  __syncthreads();
+  const int nx = d.Ex + 1, ny = d.Ey + 1;
+  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
+    const int x = q % m0, y = q / m0;
+    float s = 0.f;
+    for (int f = 0; f < m0; ++f) s = fmaf(sx[x * m0 + f], U[y * m0 + f], s);
+    uc[(d.lo[0] + x) + (int64_t)nx * ((d.lo[1] + y) + (int64_t)ny * (d.lo[2] + zi))] = s;
+  }
+}
+
+// what the pull needs to add the prolongated coarse correction
+struct CoarseView {
+  const float* uc;  // full vertex grid, Dirichlet vertices zero; null: no coarse level
+  CoarsePhi ph;
+};
 
 // Assembling prolongation: each local node sums the extended results of ALL
 // elements whose extended box covers its global node, in ascending element
@@ -289,7 +489,7 @@ struct PullVec {
 template <int LX, bool DOT>
 __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
                        const float* __restrict__ r, const float* __restrict__ mult, int mode,
-                       double* __restrict__ part, Scalars* sc) {
+                       double* __restrict__ part, Scalars* sc, CoarseView cv) {
   using X = Ext<LX>;
   constexpr int LE = X::LE, LE2 = X::LE2, LE3 = X::LE3, N = X::N;
   constexpr int LX2 = LX * LX, LX3 = LX * LX * LX, VW = PullVec<LX>::VW, Q = LX / VW;
@@ -297,6 +497,12 @@ __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int 
   if (sc && sc->done) return;
   const int64_t nq = (int64_t)Ex * Ey * Ez * (LX3 / VW);
   const int64_t sy = (int64_t)Ex * LE3, sz = (int64_t)Ex * Ey * LE3;
+  __shared__ float sp[2][LX];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int t = 0; t < 2 * LX; ++t) sp[t / LX][t % LX] = cv.ph.p[t / LX][t % LX];  // constant indices
+  }
+  __syncthreads();
   float rz = 0.f;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq; t += (int64_t)gridDim.x * blockDim.x) {
     const int e = (int)(t / (LX3 / VW));
@@ -350,6 +556,33 @@ __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int 
         }
       }
       out[q] = acc;
+    }
+    if (cv.uc) {
+      // + P u_c: trilinear in the element's eight vertices (z-, y-, x-major);
+      // on a shared face the other element's vertices have weight exactly 0,
+      // so every copy of a node sums the same terms in the same order
+      const int nx = Ex + 1, ny = Ey + 1;
+      const float* u0 = cv.uc + cx + (int64_t)nx * (cy + (int64_t)ny * cz);
+      float cvz[2][2][2];
+#pragma unroll
+      for (int vz = 0; vz < 2; ++vz)
+#pragma unroll
+        for (int vy = 0; vy < 2; ++vy)
+#pragma unroll
+          for (int vx = 0; vx < 2; ++vx) cvz[vz][vy][vx] = u0[vx + (int64_t)nx * (vy + (int64_t)ny * vz)];
+#pragma unroll
+      for (int q = 0; q < VW; ++q) {
+        const int i = VW * h + q;
+        float c = 0.f;
+#pragma unroll
+        for (int vz = 0; vz < 2; ++vz)
+#pragma unroll
+          for (int vy = 0; vy < 2; ++vy)
+#pragma unroll
+            for (int vx = 0; vx < 2; ++vx)
+              c += (sp[vx][i] * sp[vy][j] * sp[vz][k]) * cvz[vz][vy][vx];
+        out[q] += c;
+      }
     }
     if constexpr (VW == 4)
       *reinterpret_cast<float4*>(z + o) = make_float4(out[0], out[1], out[2], out[3]);
@@ -415,6 +648,16 @@ struct ntg_schwarz {
   float* ze = nullptr;   // E x LE^3 extended results
   int fdm_grid = 0;      // persistent grid of the FDM kernel (blocks resident on all SMs)
   std::vector<double> hl;  // element lengths (host)
+  // coarse level (Q1 on the vertex grid); the FDM kernel writes its restriction
+  int coarse = 0, coarse_ready = 0;
+  ntg::sw::CoarseDims cd{};
+  ntg::sw::CoarsePhi ph{};
+  float* cS[3] = {nullptr, nullptr, nullptr};  // m_d x m_d eigenvectors (S[x][f])
+  float* clam = nullptr;                       // m0 + m1 + m2 eigenvalues
+  float* corner = nullptr;                     // E x 8 restricted corner sums
+  float* cwork = nullptr;                      // m0 m1 m2 transformed coarse residual
+  float* uc = nullptr;                         // (Ex+1)(Ey+1)(Ez+1) coarse correction
+  size_t smem_xy = 0, smem_z = 0;
 };
 
 using namespace ntg;
@@ -450,6 +693,177 @@ static void fdm_1d(const ntg_plan* p, double hl, double hc, double hr, double* S
 
 static void schwarz_free(ntg_schwarz* s) {
   dev_free(s->S); dev_free(s->lam); dev_free(s->hc); dev_free(s->ze);
+  for (int d = 0; d < 3; ++d) dev_free(s->cS[d]);
+  dev_free(s->clam); dev_free(s->corner); dev_free(s->cwork); dev_free(s->uc);
+}
+
+// Generalised symmetric eigenproblem K s = lam M s (M SPD, n small): with
+// M = L L^T, C = L^-1 K L^-T = V diag(lam) V^T and S = L^-T V, so that
+// S^T M S = I and S^T K S = diag(lam).  S row-major (S[i * n + f]).
+static void gen_eig(int n, const std::vector<double>& K, const std::vector<double>& M, std::vector<double>& S,
+                    std::vector<double>& lam) {
+  std::vector<double> L(n * n, 0.0);
+  for (int j = 0; j < n; ++j) {
+    double d = M[j * n + j];
+    for (int k = 0; k < j; ++k) d -= L[j * n + k] * L[j * n + k];
+    L[j * n + j] = std::sqrt(d);
+    for (int i = j + 1; i < n; ++i) {
+      double v = M[i * n + j];
+      for (int k = 0; k < j; ++k) v -= L[i * n + k] * L[j * n + k];
+      L[i * n + j] = v / L[j * n + j];
+    }
+  }
+  // X = L^-1 K (forward substitution per column), C = X L^-T = (L^-1 X^T)^T
+  std::vector<double> X(n * n), C(n * n), V(n * n), w(n);
+  for (int c = 0; c < n; ++c)
+    for (int i = 0; i < n; ++i) {
+      double v = K[i * n + c];
+      for (int k = 0; k < i; ++k) v -= L[i * n + k] * X[k * n + c];
+      X[i * n + c] = v / L[i * n + i];
+    }
+  for (int r = 0; r < n; ++r)  // row r of C: solve L y = X[r, :]^T
+    for (int i = 0; i < n; ++i) {
+      double v = X[r * n + i];
+      for (int k = 0; k < i; ++k) v -= L[i * n + k] * C[r * n + k];
+      C[r * n + i] = v / L[i * n + i];
+    }
+  for (int i = 0; i < n; ++i)  // symmetrise against rounding
+    for (int j = i + 1; j < n; ++j) C[i * n + j] = C[j * n + i] = 0.5 * (C[i * n + j] + C[j * n + i]);
+  sw::jacobi_eig(n, C.data(), V.data(), w.data());
+  // S = L^-T V: back substitution per column
+  S.assign(n * n, 0.0);
+  for (int f = 0; f < n; ++f)
+    for (int i = n - 1; i >= 0; --i) {
+      double v = V[i * n + f];
+      for (int k = i + 1; k < n; ++k) v -= L[k * n + i] * S[k * n + f];
+      S[i * n + f] = v / L[i * n + i];
+    }
+  lam = w;
+}
+
+// (Re)build the coarse level: Dirichlet faces from the plan's mask, slab
+// lengths, 1D operators and their eigenvectors, h1/h2 means of the element means.
+static int coarse_setup(ntg_schwarz* s) {
+  ntg_plan* p = s->plan;
+  const int lx = p->lx, N = lx - 1, lx3 = lx * lx * lx;
+  const int E[3] = {s->Ex, s->Ey, s->Ez};
+  const int64_t nelv = p->nelv;
+  s->coarse_ready = 0;
+  // Dirichlet faces: a face is Dirichlet when all its local nodes are masked
+  int64_t cnt[6] = {0, 0, 0, 0, 0, 0};
+  if (p->nmask > 0) {
+    std::vector<int32_t> mk((size_t)p->nmask);
+    NTG_CUDA_TRY(cudaMemcpyAsync(mk.data(), p->mask, sizeof(int32_t) * mk.size(), cudaMemcpyDeviceToHost, p->stream));
+    NTG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    for (int32_t l : mk) {
+      const int64_t e = l / lx3;
+      const int m = (int)(l - e * lx3), idx[3] = {m % lx, (m / lx) % lx, m / (lx * lx)};
+      const int c[3] = {(int)(e % E[0]), (int)((e / E[0]) % E[1]), (int)(e / ((int64_t)E[0] * E[1]))};
+      for (int d = 0; d < 3; ++d) {
+        if (idx[d] == 0 && c[d] == 0) cnt[2 * d]++;
+        if (idx[d] == N && c[d] == E[d] - 1) cnt[2 * d + 1]++;
+      }
+    }
+  }
+  bool dir[6];
+  for (int d = 0; d < 3; ++d) {
+    const int64_t face = (int64_t)E[(d + 1) % 3] * E[(d + 2) % 3] * lx * lx;
+    dir[2 * d] = cnt[2 * d] == face;
+    dir[2 * d + 1] = cnt[2 * d + 1] == face;
+  }
+  // h1, h2: means of the element means
+  std::vector<float> hch((size_t)nelv * 2);
+  NTG_CUDA_TRY(cudaMemcpyAsync(hch.data(), s->hc, sizeof(float) * hch.size(), cudaMemcpyDeviceToHost, p->stream));
+  NTG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  double h1 = 0, h2 = 0;
+  for (int64_t e = 0; e < nelv; ++e) {
+    h1 += hch[2 * e];
+    h2 += hch[2 * e + 1];
+  }
+  h1 /= (double)nelv;
+  h2 /= (double)nelv;
+  // per direction: slab lengths, K and consistent M, active vertices, eigenpairs
+  std::vector<float> lamall;
+  double lmax = 0;
+  for (int d = 0; d < 3; ++d) {
+    std::vector<double> hs(E[d], 0.0);
+    std::vector<int64_t> ns(E[d], 0);
+    for (int64_t e = 0; e < nelv; ++e) {
+      const int c = d == 0 ? (int)(e % E[0]) : d == 1 ? (int)((e / E[0]) % E[1]) : (int)(e / ((int64_t)E[0] * E[1]));
+      hs[c] += s->hl[3 * e + d];
+      ns[c]++;
+    }
+    const int nv = E[d] + 1, lo = dir[2 * d] ? 1 : 0, hi = nv - (dir[2 * d + 1] ? 1 : 0), m = hi - lo;
+    s->cd.lo[d] = lo;
+    s->cd.m[d] = m;
+    if (m <= 0) return NTG_OK;  // no active vertex in this direction: the coarse space is empty
+    std::vector<double> K(nv * nv, 0.0), M(nv * nv, 0.0);
+    for (int c = 0; c < E[d]; ++c) {
+      const double h = hs[c] / (double)ns[c];
+      K[c * nv + c] += 1.0 / h;
+      K[(c + 1) * nv + c + 1] += 1.0 / h;
+      K[c * nv + c + 1] -= 1.0 / h;
+      K[(c + 1) * nv + c] -= 1.0 / h;
+      M[c * nv + c] += h / 3.0;
+      M[(c + 1) * nv + c + 1] += h / 3.0;
+      M[c * nv + c + 1] += h / 6.0;
+      M[(c + 1) * nv + c] += h / 6.0;
+    }
+    std::vector<double> Ka(m * m), Ma(m * m), S, lam;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        Ka[i * m + j] = K[(lo + i) * nv + lo + j];
+        Ma[i * m + j] = M[(lo + i) * nv + lo + j];
+      }
+    gen_eig(m, Ka, Ma, S, lam);
+    std::vector<float> Sf(S.begin(), S.end());
+    dev_free(s->cS[d]);
+    NTG_TRY(dev_alloc(&s->cS[d], (size_t)m * m));
+    NTG_CUDA_TRY(cudaMemcpy(s->cS[d], Sf.data(), sizeof(float) * Sf.size(), cudaMemcpyHostToDevice));
+    double lm = 0;
+    for (double v : lam) {
+      lamall.push_back((float)v);
+      lm = std::max(lm, v);
+    }
+    lmax += lm;
+  }
+  const int m0 = s->cd.m[0], m1 = s->cd.m[1], m2 = s->cd.m[2];
+  s->cd.Ex = E[0];
+  s->cd.Ey = E[1];
+  s->cd.Ez = E[2];
+  s->cd.h1 = (float)h1;
+  s->cd.h2 = (float)h2;
+  s->cd.dmin = (float)(1e-6 * (h1 * lmax + h2));
+  s->smem_xy = sizeof(float) * (2 * (size_t)m0 * m1 + (size_t)m0 * m0 + (size_t)m1 * m1);
+  s->smem_z = sizeof(float) * (2 * (size_t)m2 * m0 + (size_t)m2 * m2);
+  if (s->smem_xy > 227 * 1024 || s->smem_z > 227 * 1024) {
+    set_error("schwarz coarse level: vertex grid %d x %d x %d too large for one plane per block", m0, m1, m2);
+    return NTG_ERR_UNSUPPORTED;
+  }
+  NTG_CUDA_TRY(cudaFuncSetAttribute(sw::k_crs_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_xy));
+  NTG_CUDA_TRY(cudaFuncSetAttribute(sw::k_crs_yx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_xy));
+  NTG_CUDA_TRY(cudaFuncSetAttribute(sw::k_crs_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_z));
+  dev_free(s->clam);
+  NTG_TRY(dev_alloc(&s->clam, lamall.size()));
+  NTG_CUDA_TRY(cudaMemcpy(s->clam, lamall.data(), sizeof(float) * lamall.size(), cudaMemcpyHostToDevice));
+  const size_t nv3 = (size_t)(E[0] + 1) * (E[1] + 1) * (E[2] + 1);
+  if (!s->corner) NTG_TRY(dev_alloc(&s->corner, (size_t)nelv * 8));
+  if (!s->uc) NTG_TRY(dev_alloc(&s->uc, nv3));
+  dev_free(s->cwork);
+  NTG_TRY(dev_alloc(&s->cwork, (size_t)m0 * m1 * m2));
+  NTG_CUDA_TRY(cudaMemset(s->uc, 0, sizeof(float) * nv3));
+  double xi[NTG_LXMAX], wq[NTG_LXMAX], Dm[NTG_LXMAX * NTG_LXMAX];
+  gll_basis(lx, xi, wq, Dm);
+  for (int i = 0; i < lx; ++i) {
+    s->ph.p[0][i] = (float)(0.5 * (1.0 - xi[i]));
+    s->ph.p[1][i] = (float)(0.5 * (1.0 + xi[i]));
+  }
+  s->ph.p[0][0] = 1.f;  // endpoints exact: shared faces then weigh the other element's vertices by 0
+  s->ph.p[1][0] = 0.f;
+  s->ph.p[0][N] = 0.f;
+  s->ph.p[1][N] = 1.f;
+  s->coarse_ready = 1;
+  return NTG_OK;
 }
 
 namespace ntg {
@@ -470,7 +884,8 @@ int fdm_prepare(ntg_schwarz* w) {
 template <int LX>
 int fdm_launch(ntg_schwarz* w, const float* r, cudaStream_t s, const Scalars* sc) {
   using C = FdmCfg<LX>;
-  k_fdm<LX><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc);
+  k_fdm<LX><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc,
+                                                      w->coarse_ready ? w->corner : nullptr, w->ph);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
@@ -485,10 +900,24 @@ template <int LX>
 int pull_launch(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
                 double* part, int mode) {
   const int g = grid_for(w->plan->n / PullVec<LX>::VW, 256);
+  const CoarseView cv{w->coarse_ready ? w->uc : nullptr, w->ph};
   if (mult)
-    k_pull<LX, true><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, r, mult, mode, part, sc);
+    k_pull<LX, true><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, r, mult, mode, part, sc, cv);
   else
-    k_pull<LX, false><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, nullptr, nullptr, 0, nullptr, sc);
+    k_pull<LX, false><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, nullptr, nullptr, 0, nullptr, sc, cv);
+  NTG_COUNT_LAUNCH();
+  return NTG_OK;
+}
+
+// coarse solve (after the FDM kernel has written the corner sums): xy / z / yx
+// transforms into uc
+inline int coarse_launch(ntg_schwarz* w, cudaStream_t s, const Scalars* sc) {
+  const CoarseDims& d = w->cd;
+  k_crs_xy<<<d.m[2], 256, w->smem_xy, s>>>(w->corner, w->cS[0], w->cS[1], w->cwork, d, sc);
+  NTG_COUNT_LAUNCH();
+  k_crs_z<<<d.m[1], 256, w->smem_z, s>>>(w->cwork, w->cS[2], w->clam, d, sc);
+  NTG_COUNT_LAUNCH();
+  k_crs_yx<<<d.m[2], 256, w->smem_xy, s>>>(w->cwork, w->cS[0], w->cS[1], w->uc, d, sc);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
@@ -502,14 +931,17 @@ int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s,
   switch (p->lx) {
     case 4:
       NTG_TRY(sw::fdm_launch<4>(w, r, s, sc));
+      if (w->coarse_ready) NTG_TRY(sw::coarse_launch(w, s, sc));
       NTG_TRY(sw::pull_launch<4>(w, z, r, s, sc, mult, part, rz_mode));
       break;
     case 6:
       NTG_TRY(sw::fdm_launch<6>(w, r, s, sc));
+      if (w->coarse_ready) NTG_TRY(sw::coarse_launch(w, s, sc));
       NTG_TRY(sw::pull_launch<6>(w, z, r, s, sc, mult, part, rz_mode));
       break;
     case 8:
       NTG_TRY(sw::fdm_launch<8>(w, r, s, sc));
+      if (w->coarse_ready) NTG_TRY(sw::coarse_launch(w, s, sc));
       NTG_TRY(sw::pull_launch<8>(w, z, r, s, sc, mult, part, rz_mode));
       break;
     default:
@@ -606,7 +1038,17 @@ int ntg_schwarz_update(ntg_schwarz* s) {
   const int lx3 = p->lx * p->lx * p->lx;
   { sw::k_coef_means<<<grid_for(p->nelv, 128), 128, 0, p->stream>>>(p->h1_const ? nullptr : p->h1, p->h1c, p->ifh2 ? p->hB : nullptr, p->B, p->nelv, lx3, s->hc); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
+  if (s->coarse) return coarse_setup(s);
   return NTG_OK;
+}
+
+int ntg_schwarz_set_coarse(ntg_schwarz* s, int enable) {
+  clear_error();
+  NTG_CHECK_ARG(s, "ntg_schwarz_set_coarse: null argument");
+  NTG_TRY(cudaStreamSynchronize(s->plan->stream) == cudaSuccess ? NTG_OK : NTG_ERR_CUDA);
+  s->coarse = enable ? 1 : 0;
+  s->coarse_ready = 0;
+  return s->coarse ? ntg_schwarz_update(s) : NTG_OK;
 }
 
 int ntg_schwarz_destroy(ntg_schwarz* s) {

@@ -11,7 +11,8 @@ with 1D operators assembled from the element's and its neighbours' GLL
 intervals (Dirichlet one node beyond the extension), inverted through the
 generalised eigenvectors (numpy.linalg.eigh); R_e^T adds the extended result
 into a global structured grid (a different prolongation than the kernel's
-pull + gather-scatter).  Element lengths: mean distance between opposite faces.
+assembling pull).  Element lengths: mean distance between opposite faces.
+With coarse=True it adds the vertex-grid coarse correction (coarse_apply).
 """
 from __future__ import annotations
 
@@ -50,7 +51,85 @@ def ext_1d(lx, hl, hc, hr):
     return bi[:, None] * Q, lam
 
 
-def apply(m, r, box, h1=1.0, h2=None, mask=None):
+def dirichlet_faces(m, box, mask):
+    """(x-, x+, y-, y+, z-, z+): a face is Dirichlet when all its local nodes are masked."""
+    Ex, Ey, Ez = box
+    lx, N = m.lx, m.lx - 1
+    E = (Ex, Ey, Ez)
+    cnt = [0] * 6
+    if mask is not None and len(mask):
+        l = np.asarray(mask, dtype=np.int64) - 1
+        e, q = l // lx ** 3, l % lx ** 3
+        idx = (q % lx, (q // lx) % lx, q // lx ** 2)
+        c = (e % Ex, (e // Ex) % Ey, e // (Ex * Ey))
+        for d in range(3):
+            cnt[2 * d] = int(np.sum((idx[d] == 0) & (c[d] == 0)))
+            cnt[2 * d + 1] = int(np.sum((idx[d] == N) & (c[d] == E[d] - 1)))
+    out = []
+    for d in range(3):
+        face = E[(d + 1) % 3] * E[(d + 2) % 3] * lx * lx
+        out += [cnt[2 * d] == face, cnt[2 * d + 1] == face]
+    return out
+
+
+def coarse_apply(m, r, box, h1, h2, mask):
+    """P A_c^+ P^T r: the coarse level on the element vertices.
+
+    P: trilinear interpolation (reference coordinates) of vertex values to
+    the GLL nodes; P^T r = sum over local nodes of phi * r * mult (mult =
+    1/multiplicity); A_c = h1 (Mz x My x Kx + Mz x Ky x Mx + Kz x My x Mx)
+    + h2 Mz x My x Mx assembled densely from 1D linear elements with the mean
+    element length of each slab, Dirichlet vertices removed; pseudo-inverse
+    (an all-Neumann box has the constant null mode)."""
+    Ex, Ey, Ez = box
+    E = (Ex, Ey, Ez)
+    lx = m.lx
+    xi, _, _ = numpy_ref.gll(lx)
+    phi = np.stack([0.5 * (1 - xi), 0.5 * (1 + xi)])  # (2, lx)
+    hl = element_lengths(m)
+    dirf = dirichlet_faces(m, box, mask)
+    Ks, Ms, act = [], [], []
+    for d in range(3):
+        c = (np.arange(m.nelv) // (1, Ex, Ex * Ey)[d]) % E[d]
+        hs = np.array([hl[c == s, d].mean() for s in range(E[d])])
+        nv = E[d] + 1
+        K, M = np.zeros((nv, nv)), np.zeros((nv, nv))
+        for s, h in enumerate(hs):
+            K[s:s + 2, s:s + 2] += np.array([[1, -1], [-1, 1]]) / h
+            M[s:s + 2, s:s + 2] += np.array([[2, 1], [1, 2]]) * h / 6
+        a = np.arange(1 if dirf[2 * d] else 0, nv - (1 if dirf[2 * d + 1] else 0))
+        Ks.append(K[np.ix_(a, a)])
+        Ms.append(M[np.ix_(a, a)])
+        act.append(a)
+    if any(len(a) == 0 for a in act):
+        return np.zeros(m.n)
+    Kx, Ky, Kz = Ks
+    Mx, My, Mz = Ms
+    A = h1 * (np.kron(Mz, np.kron(My, Kx)) + np.kron(Mz, np.kron(Ky, Mx)) + np.kron(Kz, np.kron(My, Mx))) \
+        + h2 * np.kron(Mz, np.kron(My, Mx))
+    # P as a dense (n_local x n_active) matrix
+    nvx, nvy = Ex + 1, Ey + 1
+    col = -np.ones((Ex + 1) * (Ey + 1) * (Ez + 1), dtype=np.int64)
+    gx, gy, gz = np.meshgrid(act[0], act[1], act[2], indexing="ij")
+    flat = (gx + nvx * (gy + nvy * gz)).transpose(2, 1, 0).ravel()  # x fastest
+    col[flat] = np.arange(flat.size)
+    P = np.zeros((m.n, flat.size))
+    for e in range(m.nelv):
+        c = (e % Ex, (e // Ex) % Ey, e // (Ex * Ey))
+        for k in range(lx):
+            for j in range(lx):
+                for i in range(lx):
+                    l = e * lx ** 3 + i + lx * j + lx * lx * k
+                    for v in range(8):
+                        vx, vy, vz = v & 1, (v >> 1) & 1, v >> 2
+                        g = (c[0] + vx) + nvx * ((c[1] + vy) + nvy * (c[2] + vz))
+                        if col[g] >= 0:
+                            P[l, col[g]] += phi[vx, i] * phi[vy, j] * phi[vz, k]
+    rc = P.T @ (np.asarray(r) * m.mult)
+    return P @ (np.linalg.pinv(A) @ rc)
+
+
+def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False):
     """z = M r for an oracle Mesh `m` built as a box of `box` = (Ex, Ey, Ez)."""
     Ex, Ey, Ez = box
     lx = m.lx
@@ -100,6 +179,9 @@ def apply(m, r, box, h1=1.0, h2=None, mask=None):
         c = (e % Ex, (e // Ex) % Ey, e // (Ex * Ey))
         z[e] = G[c[0] * N:c[0] * N + lx, c[1] * N:c[1] * N + lx, c[2] * N:c[2] * N + lx].transpose(2, 1, 0)
     z = z.ravel()
+    if coarse:
+        h2m = 0.0 if h2 is None else float(np.asarray(h2).reshape(m.nelv, -1).mean(1).mean())
+        z = z + coarse_apply(m, r, box, h1, h2m, mask)
     if mask is not None and len(mask):
         z[np.asarray(mask) - 1] = 0.0
     return z

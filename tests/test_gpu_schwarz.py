@@ -91,3 +91,82 @@ def test_cg_mixed_with_schwarz(pkg, orc, dev, case):
     # Brinkman (h2 = chi(rho) varying by 1e4 inside elements): the FDM local
     # solves see only element means of h2, so pointwise Jacobi is the better
     # preconditioner there (measured 73 vs 562); the solve still converges.
+
+
+@pytest.mark.parametrize("shape", [(3, 2, 2, 8, 0.05, True), (2, 3, 2, 4, 0.0, False), (4, 1, 2, 6, 0.05, True)])
+def test_schwarz_coarse_apply_matches_oracle(pkg, orc, dev, shape):
+    ex, ey, ez, lx, amp, dirichlet = shape
+    m = orc.build_mesh(ex, ey, ez, lx, amp=amp, seed=2)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=amp, seed=2, device=dev)
+    mask = orc.mask_face_xmax(ex, ey, ez, lx) if dirichlet else None
+    if dirichlet:
+        c.set_mask(T(mask, dev, torch.int32), base=1)
+    rng = np.random.default_rng(5)
+    h2 = rng.uniform(0.0, 2.0, m.n)
+    c.set_coefs(h1c=0.5, h2=T(h2, dev), ifh2=True)
+    sw = pkg.schwarz_t(c, coarse=True)
+    g = orc.gs_op(m, rng.standard_normal(m.n)) * m.mult
+    r = (orc.apply_mask_zero(g, mask) if dirichlet else g).astype(np.float32)
+    z = torch.empty(m.n, dtype=torch.float32, device=dev)
+    sw.apply(z, T(r, dev, torch.float32))
+    torch.cuda.synchronize()
+    ref = schwarz_ref.apply(m, r.astype(np.float64), (ex, ey, ez), h1=0.5, h2=h2, mask=mask, coarse=True)
+    zz = z.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(zz - ref) <= 2e-5 * np.linalg.norm(ref)
+    # every copy of a shared node holds the bit-identical value
+    order = np.argsort(m.gid, kind="stable")
+    gid, v = m.gid[order], zz[order]
+    starts = np.r_[0, np.nonzero(np.diff(gid))[0] + 1]
+    assert np.array_equal(np.maximum.reduceat(v, starts), np.minimum.reduceat(v, starts))
+
+
+def test_schwarz_coarse_is_symmetric(pkg, orc, dev):
+    ex, ey, ez, lx = 4, 3, 2, 8
+    m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=3)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.05, seed=3, device=dev)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    sw = pkg.schwarz_t(c, coarse=True)
+    rng = np.random.default_rng(4)
+    u = (orc.gs_op(m, rng.standard_normal(m.n)) * m.mult).astype(np.float32)
+    v = (orc.gs_op(m, rng.standard_normal(m.n)) * m.mult).astype(np.float32)
+    Mu = torch.empty(m.n, dtype=torch.float32, device=dev)
+    Mv = torch.empty_like(Mu)
+    sw.apply(Mu, T(u, dev, torch.float32))
+    sw.apply(Mv, T(v, dev, torch.float32))
+    torch.cuda.synchronize()
+    a = float(np.sum(m.mult * v * Mu.cpu().numpy()))
+    b = float(np.sum(m.mult * u * Mv.cpu().numpy()))
+    assert abs(a - b) <= 1e-5 * max(abs(a), abs(b))
+    # all-Neumann: the constant null mode is dropped, the rest stays positive
+    assert float(np.sum(m.mult * u * Mu.cpu().numpy())) > 0
+
+
+def test_cg_mixed_with_two_level_schwarz(pkg, orc, dev):
+    """The coarse level cuts the pressure-Poisson iterations further and the
+    solution is the same."""
+    ex, ey, ez, lx = 8, 8, 8, 8
+    m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=21)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.05, seed=21, device=dev)
+    mask = orc.mask_face_xmax(ex, ey, ez, lx)
+    c.set_mask(T(mask, dev, torch.int32), base=1)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    k, a, ph = orc.fourier_params(21, 16)
+    f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+    its = {}
+    xs = {}
+    for name, coarse in (("one_level", False), ("two_level", True)):
+        sw = pkg.schwarz_t(c, coarse=coarse)
+        ksp = pkg.krylov_solver_factory(c, "cg_mixed", 20000, 1e-10)
+        ksp.set_schwarz(sw)
+        x = torch.zeros(m.n, dtype=torch.float64, device=dev)
+        mon = ksp.solve(x, T(f, dev))
+        torch.cuda.synchronize()
+        assert mon.status == pkg.NTG_OK, mon
+        its[name] = mon.iter
+        xs[name] = x.cpu().numpy()
+    xn = xs["two_level"]
+    r = f - orc.op_apply(m, xn, h1c=1.0, mask=mask)
+    assert np.sqrt(orc.glsc3(r, r, m.mult)) <= 1.5e-10 * np.sqrt(orc.glsc3(f, f, m.mult))
+    assert np.linalg.norm(xn - xs["one_level"]) <= 1e-7 * np.linalg.norm(xn)
+    print("iterations", its)
+    assert its["two_level"] < 0.7 * its["one_level"]
