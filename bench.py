@@ -239,6 +239,11 @@ def run_ours(args, ws, rank, local):
     if pc == "auto":  # two-level Schwarz for the pressure-Poisson cases, Jacobi under Brinkman penalisation
         pc = "schwarz2" if cfg["case"] == "poisson_fourier" else "jacobi"
     args.pc_used = pc
+    if args.delta is None:
+        # reliable-update spacing: the FP32 recurrence drifts with the iterations
+        # between FP64 replacements, so a preconditioner that needs few
+        # iterations per decade (two-level Schwarz) affords wide spacing
+        args.delta = 1e-3 if pc == "schwarz2" else 0.1
     sw = None
     if args.method == "cg_mixed":
         ksp_mx = pkg.krylov_solver_factory(coef, "cg_mixed", 50000, RTOL)
@@ -492,7 +497,8 @@ def main(argv=None):
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
     p.add_argument("--method", choices=["cg_mixed", "fcg_mixed"], default="cg_mixed")
-    p.add_argument("--delta", type=float, default=0.1, help="reliable-update threshold of cg_mixed")
+    p.add_argument("--delta", type=float, default=None,
+                   help="reliable-update threshold of cg_mixed (default: 1e-3 with schwarz2, 0.1 otherwise)")
     p.add_argument("--pc", choices=["auto", "jacobi", "schwarz", "schwarz2"], default="auto",
                    help="FP32 preconditioner of cg_mixed (auto: two-level Schwarz for Poisson, Jacobi for Brinkman)")
     p.add_argument("--inner-rtol", type=float, default=1e-4)

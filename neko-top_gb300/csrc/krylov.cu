@@ -185,15 +185,17 @@ struct FinUpd {
     if (sc->ru_mode) {
       // FP32 residual: a converged one is only a candidate (the host
       // confirms it with an FP64 residual); a drop by delta since the last
-      // FP64 residual asks for a replacement
-      if (acc[1] <= sc->tol2) {
+      // FP64 residual asks for a replacement.  Both stop the FP32 iteration
+      // here, before the direction update, so the replacement comes at once
+      // (iterating on to the host's next poll can carry the FP32 recurrence
+      // decades past what FP32 resolves); the host completes the iteration.
+      const double rn = sqrt(acc[1]);
+      if (rn > sc->rmax) sc->rmax = rn;
+      if (acc[1] <= sc->tol2 || rn < sc->delta * sc->rmax) {
         sc->need_ru = 2;
         sc->done = 1;
         return;
       }
-      const double rn = sqrt(acc[1]);
-      if (rn > sc->rmax) sc->rmax = rn;
-      if (rn < sc->delta * sc->rmax && sc->need_ru == 0) sc->need_ru = 1;
     } else if (acc[1] <= sc->tol2) {
       sc->done = 1;
       return;
