@@ -44,6 +44,9 @@ CONFIGS = {
     "c3": dict(E=(32, 32, 32), amp=0.05, case="brinkman_blobs", dirichlet=True,
                desc="32^3 deformed hex, N=7, Brinkman Helmholtz h1=1/Re=0.01, h2=chi(12 Gaussian blobs), "
                     "Dirichlet x=1, 16 Fourier modes, solve to 1e-10 rel"),
+    "c2m": dict(E=(24, 24, 24), amp=0.05, case="poisson_fourier", dirichlet=True,
+                desc="24^3 deformed hex (0.05h sinusoid), N=7 (7.1M local DOFs), the c2 physics on a mesh sized for "
+                     "ncu captures (inputs still above L2)"),
     "c5": dict(E=(64, 64, 64), amp=0.05, case="poisson_fourier", dirichlet=True,
                desc="64^3 deformed hex, N=7 (134M local DOFs), pressure-Poisson, Dirichlet x=1, "
                     "16 Fourier modes, solve to 1e-10 rel"),
@@ -267,8 +270,10 @@ def run_ours(args, ws, rank, local):
     barrier(ws)
     torch.cuda.synchronize()
     l0 = int(L.ntg_launch_count())
+    torch.cuda.nvtx.range_push("timed_solves")  # lets ncu restrict a launch list to the timed region
     with ClockSampler(dev.index if dev.index is not None else 0) as clk:
         t_mx, mons = time_solves(ksp_mx, x, f, args.steps, ev)
+    torch.cuda.nvtx.range_pop()
     launches = int(L.ntg_launch_count()) - l0
     barrier(ws)
     t_mx = max_over_ranks(t_mx, ws)

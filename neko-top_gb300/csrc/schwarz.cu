@@ -478,48 +478,41 @@ struct CoarseView {
 // gather-scatter pass is needed.  Per direction a node has one covering
 // element (its own) or two (own and the lower or upper neighbour); the
 // 2x2x2 combinations are summed z-major, y, x (= ascending element index).
-// A thread handles VW consecutive nodes of one row (i = VW h .. VW h + VW-1).
-template <int LX>
-struct PullVec {
-  static constexpr int VW = LX % 4 == 0 ? 4 : 2;  // nodes per thread (one aligned vector store)
-};
-
-// DOT: also (r, z)_mult, reduced deterministically and finalised by FinRz
-// (the mask applied afterwards does not change it: r vanishes on masked nodes).
+// A thread handles one row (j, k) of an element: per covering (y, z) choice
+// it reads the covering element's extended row (LE values, float2 pairs) and
+// the adjacent pair of each x neighbour.  DOT: also (r, z)_mult, reduced
+// deterministically and finalised by FinRz (the mask applied afterwards does
+// not change it: r vanishes on masked nodes).  cv.uc: plus the trilinear
+// prolongation of the coarse correction.
 template <int LX, bool DOT>
-__global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
-                       const float* __restrict__ r, const float* __restrict__ mult, int mode,
-                       double* __restrict__ part, Scalars* sc, CoarseView cv) {
-  using X = Ext<LX>;
-  constexpr int LE = X::LE, LE2 = X::LE2, LE3 = X::LE3, N = X::N;
-  constexpr int LX2 = LX * LX, LX3 = LX * LX * LX, VW = PullVec<LX>::VW, Q = LX / VW;
-  static_assert(N >= 3, "one neighbour per direction");
+__global__ void __launch_bounds__(256)
+    k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
+           const float* __restrict__ r, const float* __restrict__ mult, int mode,
+           double* __restrict__ part, Scalars* sc, CoarseView cv) {
+  constexpr int N = LX - 1, LE = LX + 2, LE2 = LE * LE, LE3 = LE2 * LE, LX2 = LX * LX, LX3 = LX2 * LX;
+  static_assert(N >= 3 && LE % 2 == 0, "one neighbour per direction; rows of float2 pairs");
   if (sc && sc->done) return;
-  const int64_t nq = (int64_t)Ex * Ey * Ez * (LX3 / VW);
-  const int64_t sy = (int64_t)Ex * LE3, sz = (int64_t)Ex * Ey * LE3;
   __shared__ float sp[2][LX];
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int t = 0; t < 2 * LX; ++t) sp[t / LX][t % LX] = cv.ph.p[t / LX][t % LX];  // constant indices
   }
   __syncthreads();
+  const int64_t nrow = (int64_t)Ex * Ey * Ez * LX2;
+  const int64_t sy = (int64_t)Ex * LE3, sz = (int64_t)Ex * Ey * LE3;
   float rz = 0.f;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nq; t += (int64_t)gridDim.x * blockDim.x) {
-    const int e = (int)(t / (LX3 / VW));
-    const int m = (int)(t - (int64_t)e * (LX3 / VW));
-    const int h = m % Q, j = (m / Q) % LX, k = m / (Q * LX);
-    const int64_t o = (int64_t)e * LX3 + k * LX2 + j * LX + VW * h;
-    // the dot's operands first: their loads overlap the gather below
-    float rv[VW], mv[VW];
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nrow; t += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(t / LX2);
+    const int m = (int)(t - (int64_t)e * LX2), j = m % LX, k = m / LX;
+    const int64_t o = (int64_t)e * LX3 + (int64_t)m * LX;  // first node of the row in z / r / mult
+    float rv[LX], mv[LX];
     if constexpr (DOT) {
-      if constexpr (VW == 4) {
-        const float4 r4 = *reinterpret_cast<const float4*>(r + o), m4 = *reinterpret_cast<const float4*>(mult + o);
-        rv[0] = r4.x; rv[1] = r4.y; rv[2] = r4.z; rv[3] = r4.w;
-        mv[0] = m4.x; mv[1] = m4.y; mv[2] = m4.z; mv[3] = m4.w;
-      } else {
-        const float2 r2 = *reinterpret_cast<const float2*>(r + o), m2 = *reinterpret_cast<const float2*>(mult + o);
-        rv[0] = r2.x; rv[1] = r2.y;
-        mv[0] = m2.x; mv[1] = m2.y;
+#pragma unroll
+      for (int q = 0; q < LX; q += 2) {
+        const float2 r2 = *reinterpret_cast<const float2*>(r + o + q);
+        const float2 m2 = *reinterpret_cast<const float2*>(mult + o + q);
+        rv[q] = r2.x; rv[q + 1] = r2.y;
+        mv[q] = m2.x; mv[q + 1] = m2.y;
       }
     }
     const int exy = e / Ex, cx = e - exy * Ex, cz = exy / Ey, cy = exy - cz * Ey;
@@ -529,68 +522,65 @@ __global__ void k_pull(const float* __restrict__ ze, float* __restrict__ z, int 
     const int64_t y1 = ly ? cy * sy + LE * (j + 1) : (cy + 1) * sy + LE * (j + 1 - N);
     const int64_t z0 = lz ? (cz - 1) * sz + LE2 * (N + 1 + k) : cz * sz + LE2 * (k + 1);
     const int64_t z1 = lz ? cz * sz + LE2 * (k + 1) : (cz + 1) * sz + LE2 * (k + 1 - N);
-    const bool ty = ly || hy, tz = lz || hz;
-    const float* p00 = ze + z0 + y0;
-    const float* p10 = ze + z0 + y1;
-    const float* p01 = ze + z1 + y0;
-    const float* p11 = ze + z1 + y1;
-    float out[VW];
+    const int ny = (ly || hy) ? 2 : 1, nz = (lz || hz) ? 2 : 1;
+    const bool xl = cx > 0, xh = cx < Ex - 1;
+    float acc[LX];
 #pragma unroll
-    for (int q = 0; q < VW; ++q) {
-      const int i = VW * h + q;
-      const bool lx_ = i <= 1 && cx > 0, hx = i >= N - 1 && cx < Ex - 1, tx = lx_ || hx;
-      const int64_t x0 = lx_ ? (int64_t)(cx - 1) * LE3 + (N + 1 + i) : (int64_t)cx * LE3 + (i + 1);
-      const int64_t x1 = lx_ ? (int64_t)cx * LE3 + (i + 1) : (int64_t)(cx + 1) * LE3 + (i + 1 - N);
-      float acc = p00[x0];
-      if (tx) acc += p00[x1];
-      if (ty) {
-        acc += p10[x0];
-        if (tx) acc += p10[x1];
-      }
-      if (tz) {
-        acc += p01[x0];
-        if (tx) acc += p01[x1];
-        if (ty) {
-          acc += p11[x0];
-          if (tx) acc += p11[x1];
+    for (int i = 0; i < LX; ++i) acc[i] = 0.f;
+#pragma unroll
+    for (int vz = 0; vz < 2; ++vz) {
+      if (vz >= nz) break;
+#pragma unroll
+      for (int vy = 0; vy < 2; ++vy) {
+        if (vy >= ny) break;
+        // the covering row of element (cx, ., .) and its x neighbours' adjacent pairs
+        const float* row = ze + (vz ? z1 : z0) + (vy ? y1 : y0) + (int64_t)cx * LE3;
+        float w[LE];
+#pragma unroll
+        for (int a = 0; a < LE; a += 2) {
+          const float2 p2 = *reinterpret_cast<const float2*>(row + a);
+          w[a] = p2.x; w[a + 1] = p2.y;
         }
+        const float2 lo = xl ? *reinterpret_cast<const float2*>(row - LE3 + (LE - 2)) : make_float2(0.f, 0.f);
+        const float2 hi = xh ? *reinterpret_cast<const float2*>(row + LE3) : make_float2(0.f, 0.f);
+        // per node: lower neighbour, own, upper neighbour (ascending element order)
+        if (xl) { acc[0] += lo.x; acc[1] += lo.y; }
+#pragma unroll
+        for (int i = 0; i < LX; ++i) acc[i] += w[i + 1];
+        if (xh) { acc[N - 1] += hi.x; acc[N] += hi.y; }
       }
-      out[q] = acc;
     }
     if (cv.uc) {
       // + P u_c: trilinear in the element's eight vertices (z-, y-, x-major);
       // on a shared face the other element's vertices have weight exactly 0,
       // so every copy of a node sums the same terms in the same order
-      const int nx = Ex + 1, ny = Ey + 1;
-      const float* u0 = cv.uc + cx + (int64_t)nx * (cy + (int64_t)ny * cz);
+      const int nx = Ex + 1, nyv = Ey + 1;
+      const float* u0 = cv.uc + cx + (int64_t)nx * (cy + (int64_t)nyv * cz);
       float cvz[2][2][2];
 #pragma unroll
       for (int vz = 0; vz < 2; ++vz)
 #pragma unroll
         for (int vy = 0; vy < 2; ++vy)
 #pragma unroll
-          for (int vx = 0; vx < 2; ++vx) cvz[vz][vy][vx] = u0[vx + (int64_t)nx * (vy + (int64_t)ny * vz)];
+          for (int vx = 0; vx < 2; ++vx) cvz[vz][vy][vx] = u0[vx + (int64_t)nx * (vy + (int64_t)nyv * vz)];
+      const float pj[2] = {sp[0][j], sp[1][j]}, pk[2] = {sp[0][k], sp[1][k]};
 #pragma unroll
-      for (int q = 0; q < VW; ++q) {
-        const int i = VW * h + q;
+      for (int i = 0; i < LX; ++i) {
         float c = 0.f;
 #pragma unroll
         for (int vz = 0; vz < 2; ++vz)
 #pragma unroll
           for (int vy = 0; vy < 2; ++vy)
 #pragma unroll
-            for (int vx = 0; vx < 2; ++vx)
-              c += (sp[vx][i] * sp[vy][j] * sp[vz][k]) * cvz[vz][vy][vx];
-        out[q] += c;
+            for (int vx = 0; vx < 2; ++vx) c += (sp[vx][i] * pj[vy] * pk[vz]) * cvz[vz][vy][vx];
+        acc[i] += c;
       }
     }
-    if constexpr (VW == 4)
-      *reinterpret_cast<float4*>(z + o) = make_float4(out[0], out[1], out[2], out[3]);
-    else
-      *reinterpret_cast<float2*>(z + o) = make_float2(out[0], out[1]);
+#pragma unroll
+    for (int q = 0; q < LX; q += 2) *reinterpret_cast<float2*>(z + o + q) = make_float2(acc[q], acc[q + 1]);
     if constexpr (DOT) {
 #pragma unroll
-      for (int q = 0; q < VW; ++q) rz += mv[q] * rv[q] * out[q];
+      for (int i = 0; i < LX; ++i) rz += mv[i] * rv[i] * acc[i];
     }
   }
   if constexpr (DOT) {
@@ -899,7 +889,7 @@ namespace sw {
 template <int LX>
 int pull_launch(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
                 double* part, int mode) {
-  const int g = grid_for(w->plan->n / PullVec<LX>::VW, 256);
+  const int g = grid_for(w->plan->n / LX, 256);
   const CoarseView cv{w->coarse_ready ? w->uc : nullptr, w->ph};
   if (mult)
     k_pull<LX, true><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, r, mult, mode, part, sc, cv);
