@@ -224,6 +224,109 @@ def run_kernels_only(args, pkg, coef, f, dev):
     return {"kernels_only": True, "n_local_dofs": n, "iters": mon.iter, "status": mon.status}
 
 
+SEQUENCES = {
+    "c4": dict(E=(64, 16, 16), lo=(0.0, 0.0, 0.0), hi=(8.0, 2.0, 2.0), amp=0.05, nsolves=400, ntrain=200,
+               desc="channel 64x16x16 hex on [0,8]x[0,2]x[0,2] (0.05h sinusoid), N=7 (8.4M local DOFs); Brinkman "
+                    "Poisson h1=1, h2=chi(rho) (RAMP q=8, chimax=1e4, rho = 12 Gaussian blobs, moved by a seeded 1% "
+                    "perturbation every 20 solves); RHS = 32 Fourier modes with AR(1) amplitudes (rho=0.98); Dirichlet "
+                    "x=8; 400 solves to 1e-10, online training on 1-200, evaluation on 201-400"),
+}
+
+
+def run_sequence(args, local):
+    """A right-hand-side sequence solved with each initial-guess mode (zero,
+    projection, projection + learned direction, learned guess alone), the
+    network trained online on the first half and frozen on the second; the
+    plain FP64 drop-in (Jacobi-PCG, zero guess and projection) on a sample
+    of the evaluation half."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = SEQUENCES[args.sequence]
+    ex, ey, ez = cfg["E"]
+    coef = pkg.coef_t.box(ex, ey, ez, LX, lo=cfg["lo"], hi=cfg["hi"], amp=cfg["amp"], seed=MESH_SEED, device=dev)
+    coef.set_mask(pkg.mask_face_xmax(ex, ey, ez, LX, device=dev), base=1)
+    nsol, ntrain = cfg["nsolves"], cfg["ntrain"]
+    k, ph, amps = pkg.ar1_modes(RHS_SEED, 32, nsol, rho=0.98)
+    ramp = pkg.RAMP_mapping_t(0.0, 1e4, 8.0, False)
+    rho0 = coef.field_blobs(RHO_SEED, 12, 0.1)
+
+    def design(t):  # the design field of solve t: a 1% perturbation every 20 solves
+        rho = rho0.clone()
+        for q in range(1, t // 20 + 1):
+            d = coef.field_fourier(8, 1000 + q)
+            rho.add_(0.01 * d / d.abs().max()).clamp_(0.0, 1.0)
+        chi = torch.empty_like(rho)
+        ramp.apply_forward(chi, 1.0 - rho)
+        return chi
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    pc = "schwarz2" if args.pc in ("auto", "schwarz2") else args.pc
+    delta = args.delta if args.delta is not None else (1e-3 if pc == "schwarz2" else 0.1)
+    modes = ("zero", "projection", "learned", "learned_only")
+    res = {}
+    for mode in modes:
+        coef.set_coefs(h1c=1.0, h2=design(0), ifh2=True)
+        seq = pkg.SolveSequence(coef, "cg_mixed", mode, rtol=RTOL, L=8, train_steps=30, seed=3, lr=5e-4,
+                                pc=pc, delta=delta)
+        its, secs = [], []
+        for t in range(nsol):
+            if t > 0 and t % 20 == 0:
+                coef.set_coefs(h1c=1.0, h2=design(t), ifh2=True)
+                seq.coefficients_changed()
+            seq.training = t < ntrain
+            f = coef.rhs_assemble(coef.field_modes(k, amps[t], ph))
+            torch.cuda.synchronize()
+            e0, e1 = ev(), ev()
+            e0.record()
+            x, mon, used, fn = seq.solve(f)
+            e1.record()
+            torch.cuda.synchronize()
+            assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), (mode, t, mon)
+            if t >= ntrain:
+                its.append(mon.iter)
+                secs.append(e0.elapsed_time(e1) / 1e3)
+        res[mode] = {"iters_mean": round(statistics.mean(its), 2), "s_per_solve": round(statistics.mean(secs), 5)}
+        del seq
+    # the plain FP64 drop-in on a sample of the evaluation half
+    sample = list(range(ntrain, min(nsol, ntrain + args.fp64_sample)))  # consecutive, after 8 warm-up solves
+    for mode in ("zero", "projection"):
+        coef.set_coefs(h1c=1.0, h2=design(0), ifh2=True)
+        seq = pkg.SolveSequence(coef, "cg", mode, rtol=RTOL, L=8, pc="jacobi")
+        its, secs = [], []
+        last = 0
+        for t in sorted(set(list(range(max(0, sample[0] - 8), sample[0])) + sample)):
+            if t // 20 != last // 20:
+                coef.set_coefs(h1c=1.0, h2=design(t), ifh2=True)
+                seq.coefficients_changed()
+            last = t
+            f = coef.rhs_assemble(coef.field_modes(k, amps[t], ph))
+            torch.cuda.synchronize()
+            e0, e1 = ev(), ev()
+            e0.record()
+            x, mon, used, fn = seq.solve(f)
+            e1.record()
+            torch.cuda.synchronize()
+            assert mon.status == pkg.NTG_OK, (mode, t, mon)
+            if t in sample:
+                its.append(mon.iter)
+                secs.append(e0.elapsed_time(e1) / 1e3)
+        res["fp64_" + mode] = {"iters_mean": round(statistics.mean(its), 2),
+                               "s_per_solve": round(statistics.mean(secs), 5), "solves": len(its)}
+        del seq
+    best = min(modes, key=lambda m: res[m]["s_per_solve"])
+    return {
+        "metric": "Brinkman Poisson sequence: time per solve to 1e-10 (evaluation half)", "value":
+        res[best]["s_per_solve"], "unit": "s/solve", "higher_is_better": False, "best_mode": best,
+        "modes": res, "speedup_vs_fp64_projection": round(res["fp64_projection"]["s_per_solve"] /
+                                                          res[best]["s_per_solve"], 2),
+        "config": {"workload": cfg["desc"], "method": f"cg_mixed with {pc}, FP64 replacements at delta={delta:g}",
+                   "n_local_dofs": coef.n}, "n_gpus": 1, "data": "synthetic (seeded generators; no dataset)",
+    }
+
+
 def run_ours(args, ws, rank, local):
     import torch
     import __graft_entry__ as ge
@@ -515,9 +618,15 @@ def main(argv=None):
                    help="set up the workload and launch each hot kernel a few times (profiler captures)")
     p.add_argument("--traffic", type=float, default=None,
                    help="dram bytes per FP32 Ax launch from an ncu capture (reported as roofline.traffic)")
+    p.add_argument("--sequence", choices=sorted(SEQUENCES), default=None,
+                   help="instead of the headline line: a solve sequence with each initial-guess mode")
+    p.add_argument("--fp64-sample", type=int, default=10, help="FP64 drop-in solves sampled in --sequence")
     args = p.parse_args(argv)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
     ws, rank, local = dist_env()
+    if args.sequence:
+        print(json.dumps(run_sequence(args, local)), flush=True)
+        return 0
     if args.impl == "reference":
         res = run_reference(args, ws, rank)
         if res is not None:

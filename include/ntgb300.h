@@ -56,12 +56,19 @@ enum {
   NTG_KSP_FCG_MIXED = 1, /* FP64 flexible CG whose preconditioner is an FP32
                             Jacobi-PCG inner solve (FP32 Ax, FP32 Jacobi, FP32
                             geometric factors); FP64 residuals and dots */
-  NTG_KSP_CG_MIXED = 2   /* Jacobi-PCG iterated in FP32 with FP64 reliable
+  NTG_KSP_CG_MIXED = 2,  /* Jacobi-PCG iterated in FP32 with FP64 reliable
                             updates: the FP32 correction is folded into the
                             FP64 solution and the residual recomputed in FP64
                             (FP64 operator) whenever the FP32 residual fell by
                             delta (ntg_ksp_set_inner's first argument, default
                             0.1); convergence is confirmed on the FP64 residual */
+  NTG_KSP_GMRES = 3,      /* restarted flexible GMRES(m), FP64 (Neko's 'gmres';
+                            Jacobi or the Schwarz preconditioner) */
+  NTG_KSP_GMRES_MIXED = 4 /* FP32 flexible GMRES(m) cycles inside FP64
+                            iterative refinement: each cycle starts from the
+                            FP64 residual and reduces it by delta
+                            (ntg_ksp_set_inner's first argument, default 1e-4)
+                            or m steps; x accumulates in FP64 */
 };
 
 typedef struct ntg_plan ntg_plan; /* mesh + coef_t + gs_t + Jacobi state */
@@ -248,6 +255,8 @@ int ntg_ksp_set_tol(ntg_ksp* ksp, double rtol, double abstol);
 int ntg_ksp_set_guess_guard(ntg_ksp* ksp, int on);
 /* how many iterations run between host convergence checks (default 16) */
 int ntg_ksp_set_check_every(ntg_ksp* ksp, int every);
+/* GMRES restart length m in [1, 31] (default 30) */
+int ntg_ksp_set_restart(ntg_ksp* ksp, int m);
 /* x_d: initial guess in, solution out.  f_d: assembled, masked RHS. */
 int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon);
 /* solve_coupled for three components with one operator

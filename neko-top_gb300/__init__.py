@@ -22,7 +22,8 @@ module raises.
 """
 from __future__ import annotations
 
-from ._native import (GS_OP_ADD, GS_OP_MAX, GS_OP_MIN, GS_OP_MUL, KSP_CG, KSP_FCG_MIXED, NTG_BREAKDOWN,
+from ._native import (GS_OP_ADD, GS_OP_MAX, GS_OP_MIN, GS_OP_MUL, KSP_CG, KSP_CG_MIXED, KSP_FCG_MIXED, KSP_GMRES,
+                      KSP_GMRES_MIXED, NTG_BREAKDOWN,
                       NTG_MAXITER, NTG_NONFINITE, NTG_OK, NtgError, library_path, lib)
 from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, ar1_modes, ax_helm_t, build_box, cadd_mask,
                   cmult_mask, coef_t, col2_mask, col3_mask, glsc2_mask, glsc3, gs_t, invcol1_mask, jacobi_t,
@@ -30,7 +31,8 @@ from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, ar1_modes, ax_hel
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
 
 __all__ = [
-    "GS_OP_ADD", "GS_OP_MUL", "GS_OP_MIN", "GS_OP_MAX", "KSP_CG", "KSP_FCG_MIXED", "NTG_OK", "NTG_MAXITER",
+    "GS_OP_ADD", "GS_OP_MUL", "GS_OP_MIN", "GS_OP_MAX", "KSP_CG", "KSP_CG_MIXED", "KSP_FCG_MIXED", "KSP_GMRES",
+    "KSP_GMRES_MIXED", "NTG_OK", "NTG_MAXITER",
     "NTG_BREAKDOWN", "NTG_NONFINITE", "NtgError", "library_path", "lib", "coef_t", "gs_t", "ax_helm_t", "jacobi_t",
     "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",

@@ -10,7 +10,7 @@ _LIB = os.path.join(_HERE, "lib", "libntgb300.so")
 NTG_OK, NTG_ERR_INVALID, NTG_ERR_CUDA, NTG_ERR_ALLOC, NTG_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
 NTG_MAXITER, NTG_BREAKDOWN, NTG_NONFINITE, NTG_GUESS_REJECTED = 10, 11, 12, 13
 GS_OP_ADD, GS_OP_MUL, GS_OP_MIN, GS_OP_MAX = 1, 2, 3, 4
-KSP_CG, KSP_FCG_MIXED, KSP_CG_MIXED = 0, 1, 2
+KSP_CG, KSP_FCG_MIXED, KSP_CG_MIXED, KSP_GMRES, KSP_GMRES_MIXED = 0, 1, 2, 3, 4
 
 _vp = C.c_void_p
 _i = C.c_int
@@ -80,6 +80,7 @@ SIGNATURES = {
     "ntg_ksp_destroy": (_i, [_vp]),
     "ntg_ksp_set_inner": (_i, [_vp, _d, _i]),
     "ntg_ksp_set_check_every": (_i, [_vp, _i]),
+    "ntg_ksp_set_restart": (_i, [_vp, _i]),
     "ntg_ksp_solve": (_i, [_vp, _vp, _vp, C.POINTER(ntg_monitor)]),
     "ntg_ksp_solve_coupled": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(ntg_monitor)]),
     "ntg_proj_create": (_i, [_vp, _i, C.POINTER(_vp)]),

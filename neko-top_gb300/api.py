@@ -11,8 +11,8 @@ from dataclasses import dataclass
 
 import torch
 
-from ._native import (GS_OP_ADD, KSP_CG, KSP_CG_MIXED, KSP_FCG_MIXED, NtgError, check, check_last, lib,
-                      ntg_monitor)
+from ._native import (GS_OP_ADD, KSP_CG, KSP_CG_MIXED, KSP_FCG_MIXED, KSP_GMRES, KSP_GMRES_MIXED, NtgError, check,
+                      check_last, lib, ntg_monitor)
 
 _DT = {torch.float64: "f64", torch.float32: "f32", torch.int32: "i32", torch.int64: "i64"}
 
@@ -270,11 +270,15 @@ class _ksp:
     def set_inner(self, inner_rtol=1e-4, inner_max_iter=400):
         check(lib().ntg_ksp_set_inner(self._h, float(inner_rtol), int(inner_max_iter)))
 
+    def set_restart(self, m):
+        """GMRES restart length (1..31)."""
+        check(lib().ntg_ksp_set_restart(self._h, int(m)))
+
     def set_check_every(self, k):
         check(lib().ntg_ksp_set_check_every(self._h, int(k)))
 
     def set_schwarz(self, sw):
-        """Precondition the FP32 iteration (cg_mixed) with Schwarz; None = Jacobi."""
+        """Precondition with Schwarz (cg_mixed, gmres, gmres_mixed); None = Jacobi."""
         check(lib().ntg_ksp_set_schwarz(self._h, None if sw is None else sw.handle))
         self.sw = sw
 
@@ -360,8 +364,12 @@ def krylov_solver_factory(coef: coef_t, type_: str = "cg", max_iter: int = 800, 
                           abstol: float = 0.0) -> _ksp:
     """krylov_solver_factory(ksp, n, type, max_iter, abstol)
     (sources/adjoint/adjoint_scheme.f90:1046-1055).  type: 'cg' (FP64
-    Jacobi-PCG) or 'fcg_mixed' (FP32 inner PCG in an FP64 flexible CG)."""
-    t = {"cg": KSP_CG, "fcg_mixed": KSP_FCG_MIXED, "cg_mixed": KSP_CG_MIXED}.get(type_)
+    Jacobi-PCG), 'cg_mixed' (FP32 PCG with FP64 reliable updates),
+    'fcg_mixed' (FP32 inner PCG in an FP64 flexible CG), 'gmres' (FP64
+    restarted flexible GMRES) or 'gmres_mixed' (FP32 GMRES cycles inside FP64
+    iterative refinement)."""
+    t = {"cg": KSP_CG, "fcg_mixed": KSP_FCG_MIXED, "cg_mixed": KSP_CG_MIXED, "gmres": KSP_GMRES,
+         "gmres_mixed": KSP_GMRES_MIXED}.get(type_)
     if t is None:
         raise ValueError(f"unknown solver type {type_!r}")
     return _ksp(coef, t, max_iter, rtol, abstol)
@@ -394,6 +402,13 @@ class projection_t:
     @property
     def size(self):
         return int(lib().ntg_proj_size(self._h))
+
+    def reset(self):
+        """Empty the basis (after the operator changed)."""
+        self.free()
+        h = C.c_void_p()
+        check(lib().ntg_proj_create(self.coef.handle, int(self.L), C.byref(h)))
+        self._h = h
 
     def free(self):
         if self._h is not None:
@@ -519,11 +534,21 @@ class SolveSequence:
     right-hand side, whatever the guess."""
 
     def __init__(self, coef: coef_t, method="cg_mixed", guess="zero", rtol=1e-10, max_iter=50000, L=20,
-                 history=4, hidden=64, seed=0, lr=1e-3, train_steps=20):
+                 history=4, hidden=64, seed=0, lr=1e-3, train_steps=20, pc="jacobi", delta=None):
         if guess not in ("zero", "projection", "learned", "learned_only"):
             raise ValueError(f"unknown guess mode {guess!r}")
+        if pc not in ("jacobi", "schwarz", "schwarz2"):
+            raise ValueError(f"unknown preconditioner {pc!r}")
         self.coef, self.guess, self.rtol = coef, guess, rtol
         self.ksp = krylov_solver_factory(coef, method, max_iter, rtol)
+        self.sw = None
+        if pc != "jacobi":
+            if method != "cg_mixed":
+                raise ValueError("the Schwarz preconditioner drives the cg_mixed solver")
+            self.sw = schwarz_t(coef, coarse=pc == "schwarz2")
+            self.ksp.set_schwarz(self.sw)
+        if delta is not None:
+            self.ksp.set_inner(delta, 1)
         self.proj = projection_t(coef, L) if guess in ("projection", "learned") else None
         self.net = learned_guess_t(coef, history, hidden, seed, lr) if guess.startswith("learned") else None
         if guess == "learned_only":
@@ -560,6 +585,15 @@ class SolveSequence:
         if self.net is not None:
             self.net.observe(f, x, self.train_steps if self.training else 0)
         return x, mon, used, fn
+
+    def coefficients_changed(self):
+        """Refresh what depends on h1/h2 (Jacobi diagonal, Schwarz means)
+        after coef_t.set_coefs; the projection basis is restarted, since its
+        A-conjugacy belonged to the old operator."""
+        if self.sw is not None:
+            self.sw.update()
+        if self.proj is not None:
+            self.proj.reset()
 
     def _mult(self):
         if not hasattr(self, "_mult_t"):

@@ -187,6 +187,16 @@ int build_gs_classes(ntg_plan* p);
 template <typename T>
 int gs_cls_launch(ntg_plan* p, T* u, int op, cudaStream_t s, const Scalars* sc);
 int grid_for(int64_t work, int threads);
+int jacobi_update(ntg_plan* p);
+// restarted flexible GMRES (gmres.cu)
+struct GmresWork;
+struct GmresOpts {
+  int restart = 30, fp32 = 0, max_iter = 1000, check_every = 4;
+  double rtol = 1e-10, abstol = 0.0, delta = 1e-4;
+};
+int gmres_solve(ntg_plan* p, GmresWork*& g, Scalars* sc, ntg_schwarz* sw, const GmresOpts& o, double* x,
+                const double* f, ntg_monitor* mon);
+void gmres_free(GmresWork* g);
 // GLL nodes, weights and differentiation matrix of lx points
 void gll_basis(int lx, double* xi, double* w, double* D);
 int num_sms();

@@ -622,7 +622,9 @@ struct ntg_ksp {
   int inner_max_iter = 400;
   int check_every = 16;
   int guess_guard = 0;
-  ntg_schwarz* sw = nullptr;  // explicit FP32 preconditioner of the cg_mixed iteration
+  ntg_schwarz* sw = nullptr;  // explicit FP32 preconditioner of the cg_mixed / gmres iterations
+  int restart = 30;            // gmres restart length
+  ntg::GmresWork* gm = nullptr;
   float* z32 = nullptr;
   // FP64 workspace
   ntg::PcgVecs<double> v64;
@@ -644,6 +646,8 @@ static void ksp_free(ntg_ksp* k) {
   dev_free(k->v32.r); dev_free(k->v32.p); dev_free(k->v32.w);
   dev_free(k->rin); dev_free(k->din); dev_free(k->z32);
   dev_free(k->sc); dev_free(k->sc_in);
+  gmres_free(k->gm);
+  k->gm = nullptr;
   if (k->hs) cudaFreeHost(k->hs);
   if (k->hs_in) cudaFreeHost(k->hs_in);
   k->hs = nullptr;
@@ -993,8 +997,9 @@ extern "C" {
 int ntg_ksp_set_schwarz(ntg_ksp* ksp, ntg_schwarz* sw_) {
   clear_error();
   NTG_CHECK_ARG(ksp, "ntg_ksp_set_schwarz: null argument");
-  NTG_CHECK_ARG(ksp->type == NTG_KSP_CG_MIXED, "ntg_ksp_set_schwarz: only the cg_mixed solver takes Schwarz");
-  if (sw_ && !ksp->z32) NTG_TRY(dev_alloc(&ksp->z32, ksp->plan->n));
+  NTG_CHECK_ARG(ksp->type == NTG_KSP_CG_MIXED || ksp->type == NTG_KSP_GMRES || ksp->type == NTG_KSP_GMRES_MIXED,
+                "ntg_ksp_set_schwarz: the cg_mixed and gmres solvers take Schwarz");
+  if (sw_ && ksp->type == NTG_KSP_CG_MIXED && !ksp->z32) NTG_TRY(dev_alloc(&ksp->z32, ksp->plan->n));
   ksp->sw = sw_;
   return NTG_OK;
 }
@@ -1031,7 +1036,8 @@ int ntg_glsc3(ntg_plan* plan, const double* a_d, const double* b_d, const double
 int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double abstol, ntg_ksp** ksp) {
   clear_error();
   NTG_CHECK_ARG(plan && ksp, "ntg_ksp_create: null argument");
-  NTG_CHECK_ARG(type == NTG_KSP_CG || type == NTG_KSP_FCG_MIXED || type == NTG_KSP_CG_MIXED,
+  NTG_CHECK_ARG(type == NTG_KSP_CG || type == NTG_KSP_FCG_MIXED || type == NTG_KSP_CG_MIXED ||
+                    type == NTG_KSP_GMRES || type == NTG_KSP_GMRES_MIXED,
                 "ntg_ksp_create: unknown solver type");
   NTG_CHECK_ARG(max_iter >= 0 && rtol >= 0 && abstol >= 0, "ntg_ksp_create: bad tolerance or iteration cap");
   *ksp = nullptr;
@@ -1053,6 +1059,7 @@ int ntg_ksp_create(ntg_plan* plan, int type, int max_iter, double rtol, double a
     if (cudaMallocHost(&k->hs_in, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
     if (cudaMemset(k->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMemset(k->sc_in, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    if (type == NTG_KSP_GMRES_MIXED) k->inner_rtol = 1e-4;  // residual reduction per FP32 cycle
     if (type == NTG_KSP_CG_MIXED) {
       k->inner_rtol = 0.1;  // reliable-update threshold delta
       if ((st = dev_alloc(&k->v32.r, n))) break;
@@ -1095,6 +1102,13 @@ int ntg_ksp_set_inner(ntg_ksp* ksp, double inner_rtol, int inner_max_iter) {
   NTG_CHECK_ARG(ksp && inner_rtol > 0 && inner_rtol < 1 && inner_max_iter > 0, "ntg_ksp_set_inner: bad argument");
   ksp->inner_rtol = inner_rtol;
   ksp->inner_max_iter = inner_max_iter;
+  return NTG_OK;
+}
+
+int ntg_ksp_set_restart(ntg_ksp* ksp, int m) {
+  clear_error();
+  NTG_CHECK_ARG(ksp && m >= 1 && m <= 31, "ntg_ksp_set_restart: restart length must be in [1, 31]");
+  ksp->restart = m;
   return NTG_OK;
 }
 
@@ -1144,7 +1158,16 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
     }
   }
   int st = NTG_OK;
-  if (ksp->type == NTG_KSP_FCG_MIXED) st = ksp_solve_mixed(ksp, x_d, f_d, mon);
+  if (ksp->type == NTG_KSP_GMRES || ksp->type == NTG_KSP_GMRES_MIXED) {
+    GmresOpts o;
+    o.restart = ksp->restart;
+    o.fp32 = ksp->type == NTG_KSP_GMRES_MIXED;
+    o.max_iter = ksp->max_iter;
+    o.rtol = ksp->rtol;
+    o.abstol = ksp->abstol;
+    o.delta = ksp->inner_rtol;
+    st = gmres_solve(ksp->plan, ksp->gm, ksp->sc, ksp->sw, o, x_d, f_d, mon);
+  } else if (ksp->type == NTG_KSP_FCG_MIXED) st = ksp_solve_mixed(ksp, x_d, f_d, mon);
   else if (ksp->type == NTG_KSP_CG_MIXED)
     st = ksp->sw ? ksp_solve_mixed_ru_pc(ksp, x_d, f_d, mon) : ksp_solve_mixed_ru(ksp, x_d, f_d, mon);
   else st = ksp_solve_cg(ksp, x_d, f_d, mon);

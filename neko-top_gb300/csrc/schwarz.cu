@@ -485,7 +485,7 @@ struct CoarseView {
 // not change it: r vanishes on masked nodes).  cv.uc: plus the trilinear
 // prolongation of the coarse correction.
 template <int LX, bool DOT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
            const float* __restrict__ r, const float* __restrict__ mult, int mode,
            double* __restrict__ part, Scalars* sc, CoarseView cv) {
