@@ -30,6 +30,8 @@ from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, ar1_modes, ax_hel
                   krylov_solver_factory, ksp_monitor_t, learned_guess_t, mask_face_xmax, permeability, projection_t, schwarz_t,
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
 
+from . import dist  # noqa: E402  (element-partitioned solves across ranks)
+
 __all__ = [
     "GS_OP_ADD", "GS_OP_MUL", "GS_OP_MIN", "GS_OP_MAX", "KSP_CG", "KSP_CG_MIXED", "KSP_FCG_MIXED", "KSP_GMRES",
     "KSP_GMRES_MIXED", "NTG_OK", "NTG_MAXITER",
@@ -37,5 +39,5 @@ __all__ = [
     "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
-    "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t",
+    "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t", "dist",
 ]

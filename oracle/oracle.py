@@ -185,6 +185,34 @@ def build_mesh(ex, ey, ez, lx=8, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.0
     return m
 
 
+def mesh_slice(m: Mesh, e0: int, e1: int) -> Mesh:
+    """The oracle Mesh of elements [e0, e1) of `m` (coordinates and global
+    ids sliced, geometry and rank-local gather-scatter maps rebuilt): one
+    rank's part of an element partition.  ex/ey/ez keep the box's x and y
+    counts with ez = the slab's planes, so nelv = e1 - e0 for z-slabs."""
+    lx = m.lx
+    nl = lx ** 3
+    planes = (e1 - e0) // (m.ex * m.ey)
+    s = Mesh(m.ex, m.ey, planes, lx, m.lo, m.hi, m.amp, m.seed)
+    s.x, s.y, s.z = (np.ascontiguousarray(a[e0 * nl:e1 * nl]) for a in (m.x, m.y, m.z))
+    s.gid = np.ascontiguousarray(m.gid[e0 * nl:e1 * nl])
+    s.w, s.D = m.w, m.D
+    n = s.n
+    G = {k: np.zeros(n) for k in ("g11", "g12", "g13", "g22", "g23", "g33")}
+    s.B = np.zeros(n); s.jac = np.zeros(n)
+    lib().orc_geom(s.nelv, lx, s.x, s.y, s.z, G["g11"], G["g12"], G["g13"], G["g22"], G["g23"], G["g33"],
+                   s.B, _ptr(s.jac))
+    s.G = G
+    s.perm = np.zeros(n, dtype=np.int32)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    s.uid = np.zeros(n, dtype=np.int32)
+    s.nu = int(lib().orc_gs_build(n, s.gid, s.perm, offs, _ptr(s.uid)))
+    s.offs = offs[: s.nu + 1].copy()
+    s.mult = np.zeros(n)
+    lib().orc_mult(n, s.nu, s.perm, s.offs, s.mult)
+    return s
+
+
 def gs_op(m: Mesh, u: np.ndarray, op: int = 1) -> np.ndarray:
     v = np.ascontiguousarray(u, dtype=np.float64).copy()
     lib().orc_gs_op(v, m.nu, m.perm, m.offs, int(op))
