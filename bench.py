@@ -225,6 +225,11 @@ def run_kernels_only(args, pkg, coef, f, dev):
 
 
 SEQUENCES = {
+    "c5": dict(E=(64, 64, 64), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.05, nsolves=100, ntrain=50,
+               desc="64^3 deformed hex (0.05h sinusoid), N=7 (134M local DOFs); Brinkman Poisson h1=1, h2=chi(rho) "
+                    "(RAMP q=8, chimax=1e4, rho = 12 Gaussian blobs, moved by a seeded 1% perturbation every 20 "
+                    "solves); RHS = 32 Fourier modes with AR(1) amplitudes (rho=0.98); Dirichlet x=1; 100 solves to "
+                    "1e-10, online training on 1-50, evaluation on 51-100"),
     "c4": dict(E=(64, 16, 16), lo=(0.0, 0.0, 0.0), hi=(8.0, 2.0, 2.0), amp=0.05, nsolves=400, ntrain=200,
                desc="channel 64x16x16 hex on [0,8]x[0,2]x[0,2] (0.05h sinusoid), N=7 (8.4M local DOFs); Brinkman "
                     "Poisson h1=1, h2=chi(rho) (RAMP q=8, chimax=1e4, rho = 12 Gaussian blobs, moved by a seeded 1% "
@@ -265,7 +270,7 @@ def run_sequence(args, local):
     ev = lambda: torch.cuda.Event(enable_timing=True)
     pc = "schwarz2" if args.pc in ("auto", "schwarz2") else args.pc
     delta = args.delta if args.delta is not None else (1e-3 if pc == "schwarz2" else 0.1)
-    modes = ("zero", "projection", "learned", "learned_only")
+    modes = tuple(args.seq_modes.split(","))
     res = {}
     for mode in modes:
         coef.set_coefs(h1c=1.0, h2=design(0), ifh2=True)
@@ -297,7 +302,7 @@ def run_sequence(args, local):
         seq = pkg.SolveSequence(coef, "cg", mode, rtol=RTOL, L=8, pc="jacobi")
         its, secs = [], []
         last = 0
-        for t in sorted(set(list(range(max(0, sample[0] - 8), sample[0])) + sample)):
+        for t in sorted(set(list(range(max(0, sample[0] - args.fp64_warm), sample[0])) + sample)):
             if t // 20 != last // 20:
                 coef.set_coefs(h1c=1.0, h2=design(t), ifh2=True)
                 seq.coefficients_changed()
@@ -621,6 +626,9 @@ def main(argv=None):
     p.add_argument("--sequence", choices=sorted(SEQUENCES), default=None,
                    help="instead of the headline line: a solve sequence with each initial-guess mode")
     p.add_argument("--fp64-sample", type=int, default=10, help="FP64 drop-in solves sampled in --sequence")
+    p.add_argument("--fp64-warm", type=int, default=8, help="FP64 solves before the sample (fills projection)")
+    p.add_argument("--seq-modes", default="zero,projection,learned,learned_only",
+                   help="initial-guess modes of --sequence (comma separated)")
     args = p.parse_args(argv)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
     ws, rank, local = dist_env()

@@ -14,13 +14,22 @@
 // spectral element solution of the incompressible Navier-Stokes equations").
 // Element lengths come from the node coordinates; h1/h2 are element means.
 //
+// Optional coarse level (two-level Schwarz): z += P A_c^{-1} P^T r on the
+// element vertices (Q1), solved by fast diagonalisation; see the coarse-level
+// section below.
+//
 // Reference context: Neko's pressure solves use a Schwarz-multigrid
 // preconditioner ('hsmg', examples/rugby_ball/rugby_ball.case:46-52); this is
-// its one-level Schwarz part on the GLL grid.
+// its Schwarz part on the GLL grid and its coarse-grid part.
+//
+// Kernels per application: k_fdm (gather, six 1D transforms, coarse
+// restriction), k_crs_xy / k_crs_z / k_crs_yx (coarse solve), k_pull
+// (prolongation of both levels, optional (r, z)), then the Dirichlet mask.
 //
 // Determinism: the prolongation is a pull -- every local node sums, in a fixed
 // order, the extended results of the elements whose extended box covers it --
-// followed by the ordinary gather-scatter, so no atomics are involved.
+// so every copy of a shared node is bit-identical without a gather-scatter
+// pass, and no atomics are involved.
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -69,10 +78,6 @@ __global__ void k_coef_means(const double* __restrict__ h1, double h1c, const do
   }
 }
 
-template <int LX>
-struct Ext {
-  static constexpr int N = LX - 1, LE = LX + 2, LE2 = LE * LE, LE3 = LE * LE * LE;
-};
 
 // Extended residual -> FDM solve -> extended result for a batch of EPB
 // elements per block.  A thread owns two 1D lines of an element's extended
