@@ -276,6 +276,8 @@ def run_sequence(args, local):
         coef.set_coefs(h1c=1.0, h2=design(0), ifh2=True)
         seq = pkg.SolveSequence(coef, "cg_mixed", mode, rtol=RTOL, L=8, train_steps=30, seed=3, lr=5e-4,
                                 pc=pc, delta=delta)
+        if seq.sw is not None and args.mass_term:
+            seq.sw.set_mass_term(True)
         its, secs = [], []
         for t in range(nsol):
             if t > 0 and t % 20 == 0:
@@ -361,6 +363,8 @@ def run_ours(args, ws, rank, local):
         ksp_mx.set_inner(args.delta, 1)
         if pc in ("schwarz", "schwarz2"):
             sw = pkg.schwarz_t(coef, coarse=pc == "schwarz2")
+            if args.mass_term:
+                sw.set_mass_term(True)
             ksp_mx.set_schwarz(sw)
     else:
         ksp_mx = pkg.krylov_solver_factory(coef, "fcg_mixed", 200, RTOL)
@@ -614,6 +618,8 @@ def main(argv=None):
                    help="reliable-update threshold of cg_mixed (default: 1e-3 with schwarz2, 0.1 otherwise)")
     p.add_argument("--pc", choices=["auto", "jacobi", "schwarz", "schwarz2"], default="auto",
                    help="FP32 preconditioner of cg_mixed (auto: two-level Schwarz for Poisson, Jacobi for Brinkman)")
+    p.add_argument("--mass-term", action="store_true",
+                   help="Schwarz: additive diagonal term for the Brinkman mass part")
     p.add_argument("--inner-rtol", type=float, default=1e-4)
     p.add_argument("--inner-max", type=int, default=2000)
     p.add_argument("--fp64-steps", type=int, default=2)

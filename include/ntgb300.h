@@ -229,6 +229,10 @@ int ntg_schwarz_update(ntg_schwarz* sw);
 /* the Schwarz-multigrid preconditioner, here solved directly.  A face     */
 /* whose nodes are all masked is Dirichlet on the coarse grid.             */
 int ntg_schwarz_set_coarse(ntg_schwarz* sw, int enable);
+/* Additive diagonal term for a mass term varying inside elements (Brinkman */
+/* penalisation): z += w D^-1 r with D the assembled diagonal and w the     */
+/* node's mass fraction (h2 B) / D in [0, 1].                               */
+int ntg_schwarz_set_mass_term(ntg_schwarz* sw, int enable);
 int ntg_schwarz_destroy(ntg_schwarz* sw);
 /* z = M r (FP32; assembled and masked) */
 int ntg_schwarz_apply(ntg_schwarz* sw, float* z_d, const float* r_d);

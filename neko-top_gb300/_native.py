@@ -65,6 +65,7 @@ SIGNATURES = {
     "ntg_schwarz_create": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, C.POINTER(_vp)]),
     "ntg_schwarz_update": (_i, [_vp]),
     "ntg_schwarz_set_coarse": (_i, [_vp, _i]),
+    "ntg_schwarz_set_mass_term": (_i, [_vp, _i]),
     "ntg_schwarz_destroy": (_i, [_vp]),
     "ntg_schwarz_apply": (_i, [_vp, _vp, _vp]),
     "ntg_rhs_assemble": (_i, [_vp, _vp, _vp]),

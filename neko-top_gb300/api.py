@@ -344,6 +344,11 @@ class schwarz_t:
         coarse level's Dirichlet faces after coef_t.set_mask)."""
         check(lib().ntg_schwarz_update(self._h))
 
+    def set_mass_term(self, enable: bool = True):
+        """Add w D^-1 r (D the assembled diagonal, w the node's mass fraction):
+        for mass terms varying inside elements (Brinkman penalisation)."""
+        check(lib().ntg_schwarz_set_mass_term(self._h, int(bool(enable))))
+
     def apply(self, z, r):
         check(lib().ntg_schwarz_apply(self._h, _ptr(z, torch.float32, self.coef.n, "z"),
                                       _ptr(r, torch.float32, self.coef.n, "r")))

@@ -475,7 +475,19 @@ __global__ void __launch_bounds__(256)
 struct CoarseView {
   const float* uc;  // full vertex grid, Dirichlet vertices zero; null: no coarse level
   CoarsePhi ph;
+  const float* dw;  // additive diagonal term (mass fraction / diagonal); null: none
 };
+
+// dw = (h2 B)_assembled / diag(A)^2: the node's mass-dominance fraction
+// w = (h2 B) / diag(A) in [0, 1] times the inverse diagonal (dinv = 1 on
+// masked nodes, whose result the mask zeroes anyway)
+__global__ void k_mass_term(const double* __restrict__ hBa, const double* __restrict__ dinv, float* __restrict__ dw,
+                            int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double w = fmin(fmax(hBa[i] * dinv[i], 0.0), 1.0);
+    dw[i] = (float)(w * dinv[i]);
+  }
+}
 
 // Assembling prolongation: each local node sums the extended results of ALL
 // elements whose extended box covers its global node, in ascending element
@@ -511,12 +523,17 @@ __global__ void __launch_bounds__(256, 4)
     const int m = (int)(t - (int64_t)e * LX2), j = m % LX, k = m / LX;
     const int64_t o = (int64_t)e * LX3 + (int64_t)m * LX;  // first node of the row in z / r / mult
     float rv[LX], mv[LX];
-    if constexpr (DOT) {
+    if (DOT || cv.dw) {
 #pragma unroll
       for (int q = 0; q < LX; q += 2) {
         const float2 r2 = *reinterpret_cast<const float2*>(r + o + q);
-        const float2 m2 = *reinterpret_cast<const float2*>(mult + o + q);
         rv[q] = r2.x; rv[q + 1] = r2.y;
+      }
+    }
+    if constexpr (DOT) {
+#pragma unroll
+      for (int q = 0; q < LX; q += 2) {
+        const float2 m2 = *reinterpret_cast<const float2*>(mult + o + q);
         mv[q] = m2.x; mv[q + 1] = m2.y;
       }
     }
@@ -579,6 +596,14 @@ __global__ void __launch_bounds__(256, 4)
 #pragma unroll
             for (int vx = 0; vx < 2; ++vx) c += (sp[vx][i] * pj[vy] * pk[vz]) * cvz[vz][vy][vx];
         acc[i] += c;
+      }
+    }
+    if (cv.dw) {
+#pragma unroll
+      for (int q = 0; q < LX; q += 2) {
+        const float2 d2 = *reinterpret_cast<const float2*>(cv.dw + o + q);
+        acc[q] += d2.x * rv[q];
+        acc[q + 1] += d2.y * rv[q + 1];
       }
     }
 #pragma unroll
@@ -653,6 +678,8 @@ struct ntg_schwarz {
   float* cwork = nullptr;                      // m0 m1 m2 transformed coarse residual
   float* uc = nullptr;                         // (Ex+1)(Ey+1)(Ez+1) coarse correction
   size_t smem_xy = 0, smem_z = 0;
+  int mass_term = 0;
+  float* dw = nullptr;  // additive diagonal term of the Brinkman mass part (n)
 };
 
 using namespace ntg;
@@ -689,7 +716,7 @@ static void fdm_1d(const ntg_plan* p, double hl, double hc, double hr, double* S
 static void schwarz_free(ntg_schwarz* s) {
   dev_free(s->S); dev_free(s->lam); dev_free(s->hc); dev_free(s->ze);
   for (int d = 0; d < 3; ++d) dev_free(s->cS[d]);
-  dev_free(s->clam); dev_free(s->corner); dev_free(s->cwork); dev_free(s->uc);
+  dev_free(s->clam); dev_free(s->corner); dev_free(s->cwork); dev_free(s->uc); dev_free(s->dw);
 }
 
 // Generalised symmetric eigenproblem K s = lam M s (M SPD, n small): with
@@ -895,11 +922,11 @@ template <int LX>
 int pull_launch(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
                 double* part, int mode) {
   const int g = grid_for(w->plan->n / LX, 256);
-  const CoarseView cv{w->coarse_ready ? w->uc : nullptr, w->ph};
+  const CoarseView cv{w->coarse_ready ? w->uc : nullptr, w->ph, w->dw};
   if (mult)
     k_pull<LX, true><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, r, mult, mode, part, sc, cv);
   else
-    k_pull<LX, false><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, nullptr, nullptr, 0, nullptr, sc, cv);
+    k_pull<LX, false><<<g, 256, 0, s>>>(w->ze, z, w->Ex, w->Ey, w->Ez, r, nullptr, 0, nullptr, sc, cv);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
@@ -1033,8 +1060,28 @@ int ntg_schwarz_update(ntg_schwarz* s) {
   const int lx3 = p->lx * p->lx * p->lx;
   { sw::k_coef_means<<<grid_for(p->nelv, 128), 128, 0, p->stream>>>(p->h1_const ? nullptr : p->h1, p->h1c, p->ifh2 ? p->hB : nullptr, p->B, p->nelv, lx3, s->hc); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
+  dev_free(s->dw);
+  s->dw = nullptr;
+  if (s->mass_term && p->ifh2) {
+    NTG_TRY(jacobi_update(p));
+    double* hBa = nullptr;
+    NTG_TRY(dev_alloc(&hBa, (size_t)p->n));
+    NTG_TRY(dev_alloc(&s->dw, (size_t)p->n));
+    NTG_CUDA_TRY(cudaMemcpyAsync(hBa, p->hB, sizeof(double) * p->n, cudaMemcpyDeviceToDevice, p->stream));
+    NTG_TRY(gs_launch(p, hBa, NTG_GS_ADD, p->stream));
+    { sw::k_mass_term<<<grid_for(p->n, 256), 256, 0, p->stream>>>(hBa, p->dinv, s->dw, p->n); NTG_COUNT_LAUNCH(); }
+    NTG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    dev_free(hBa);
+  }
   if (s->coarse) return coarse_setup(s);
   return NTG_OK;
+}
+
+int ntg_schwarz_set_mass_term(ntg_schwarz* s, int enable) {
+  clear_error();
+  NTG_CHECK_ARG(s, "ntg_schwarz_set_mass_term: null argument");
+  s->mass_term = enable ? 1 : 0;
+  return ntg_schwarz_update(s);
 }
 
 int ntg_schwarz_set_coarse(ntg_schwarz* s, int enable) {

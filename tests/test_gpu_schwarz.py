@@ -170,3 +170,42 @@ def test_cg_mixed_with_two_level_schwarz(pkg, orc, dev):
     assert np.linalg.norm(xn - xs["one_level"]) <= 1e-7 * np.linalg.norm(xn)
     print("iterations", its)
     assert its["two_level"] < 0.7 * its["one_level"]
+
+
+def test_mass_term_keeps_symmetry_and_converges(pkg, orc, dev):
+    """The optional additive diagonal term for a Brinkman mass part: the
+    preconditioner stays symmetric and the mixed CG reaches the tolerance
+    with the same solution."""
+    ex, ey, ez, lx = 6, 4, 4, 8
+    m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=23)
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.05, seed=23, device=dev)
+    mask = orc.mask_face_xmax(ex, ey, ez, lx)
+    c.set_mask(T(mask, dev, torch.int32), base=1)
+    rho = orc.field_blobs(m, 5, 12, 0.1)
+    h2 = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
+    c.set_coefs(h1c=1.0, h2=T(h2, dev), ifh2=True)
+    sw = pkg.schwarz_t(c, coarse=True)
+    sw.set_mass_term(True)
+    rng = np.random.default_rng(8)
+    u = orc.apply_mask_zero(orc.gs_op(m, rng.standard_normal(m.n)) * m.mult, mask).astype(np.float32)
+    v = orc.apply_mask_zero(orc.gs_op(m, rng.standard_normal(m.n)) * m.mult, mask).astype(np.float32)
+    Mu = torch.empty(m.n, dtype=torch.float32, device=dev)
+    Mv = torch.empty_like(Mu)
+    sw.apply(Mu, T(u, dev, torch.float32))
+    sw.apply(Mv, T(v, dev, torch.float32))
+    torch.cuda.synchronize()
+    a = float(np.sum(m.mult * v * Mu.cpu().numpy()))
+    b = float(np.sum(m.mult * u * Mv.cpu().numpy()))
+    assert abs(a - b) <= 1e-5 * max(abs(a), abs(b))
+    k, am, ph = orc.fourier_params(23, 16)
+    f = orc.assemble_rhs(m, orc.field_fourier(m, k, am, ph), mask)
+    ksp = pkg.krylov_solver_factory(c, "cg_mixed", 20000, 1e-10)
+    ksp.set_inner(1e-3, 1)
+    ksp.set_schwarz(sw)
+    x = torch.zeros(m.n, dtype=torch.float64, device=dev)
+    mon = ksp.solve(x, T(f, dev))
+    torch.cuda.synchronize()
+    assert mon.status == pkg.NTG_OK, mon
+    xn = x.cpu().numpy()
+    r = f - orc.op_apply(m, xn, h1c=1.0, h2=h2, mask=mask)
+    assert np.sqrt(orc.glsc3(r, r, m.mult)) <= 1.5e-10 * np.sqrt(orc.glsc3(f, f, m.mult))
