@@ -381,27 +381,44 @@ def krylov_solver_factory(coef: coef_t, type_: str = "cg", max_iter: int = 800, 
 
 
 class projection_t:
-    """Residual projection: init(n, L), pre_solving(b), post_solving(x)
-    (sources/adjoint/adjoint_pnpn.f90:365-374,729-741)."""
+    """Residual projection: init(n, L, activ_step), pre_solving(b, tstep),
+    post_solving(x, tstep) (sources/adjoint/adjoint_pnpn.f90:365-374,729-741;
+    projection_space_size 20 and projection_hold_steps 5 are the defaults at
+    sources/adjoint/adjoint_scheme.f90:386-403).  With tstep given, steps up
+    to activ_step neither project nor enter the basis; without it the
+    projection is always active."""
 
-    def __init__(self, coef: coef_t, L: int = 20):
+    def __init__(self, coef: coef_t, L: int = 20, activ_step: int = 0):
         self.coef = coef
         h = C.c_void_p()
         check(lib().ntg_proj_create(coef.handle, int(L), C.byref(h)))
         self._h = h
         self.L = L
+        self.activ_step = int(activ_step)
+        self._active = True
 
-    def pre_solving(self, b):
+    def _set_step(self, tstep):
+        self._active = tstep is None or tstep > self.activ_step
+        return self._active
+
+    def pre_solving(self, b, tstep=None):
+        if not self._set_step(tstep):
+            return
         check(lib().ntg_proj_pre_solving(self._h, _ptr(b, n=self.coef.n, name="b")))
 
     def pre_solving_with(self, b, g):
         """pre_solving plus the extra direction g for this solve (learned guess)."""
+        self._active = True
         used = C.c_int()
         check(lib().ntg_proj_pre_solving_with(self._h, _ptr(b, n=self.coef.n, name="b"),
                                               _ptr(g, n=self.coef.n, name="g"), C.byref(used)))
         return bool(used.value)
 
-    def post_solving(self, x):
+    def post_solving(self, x, tstep=None):
+        if tstep is not None and tstep <= self.activ_step:
+            return
+        if not self._active:  # pre_solving was skipped for this solve
+            return
         check(lib().ntg_proj_post_solving(self._h, _ptr(x, n=self.coef.n, name="x")))
 
     @property

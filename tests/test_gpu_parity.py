@@ -252,6 +252,38 @@ def test_projection_sequence(pkg, orc, dev):
     assert iters[-1] < iters[0]
 
 
+def test_projection_activ_step(pkg, orc, dev):
+    """projection_t(L, activ_step): steps up to activ_step run from a zero
+    guess and leave the basis empty; later steps project."""
+    m, c, mask, f0 = poisson_deformed(pkg, orc, dev, E=(3, 3, 2))
+    rng = np.random.default_rng(9)
+    fp = orc.assemble_rhs(m, rng.uniform(-1, 1, m.n), mask)
+    proj = pkg.projection_t(c, 4, activ_step=2)
+    plain = []
+    for tstep in range(1, 6):
+        f = f0 + 0.02 * tstep * fp
+        fn = np.sqrt(orc.glsc3(f, f, m.mult))
+        b = T(f, dev)
+        proj.pre_solving(b, tstep)
+        ksp = pkg.krylov_solver_factory(c, "cg", 1000, 0.0, 1e-10 * fn)
+        x = torch.zeros(m.n, dtype=torch.float64, device=dev)
+        mon = ksp.solve(x, b)
+        proj.post_solving(x, tstep)
+        torch.cuda.synchronize()
+        ref = pkg.krylov_solver_factory(c, "cg", 1000, 0.0, 1e-10 * fn)
+        x0 = torch.zeros_like(x)
+        mon0 = ref.solve(x0, T(f, dev))
+        if tstep <= 2:
+            assert proj.size == 0 and mon.iter == mon0.iter
+        else:
+            # the first active step still starts from an empty basis
+            assert proj.size == tstep - 2
+            assert mon.iter == mon0.iter if tstep == 3 else mon.iter < mon0.iter
+        xn = x.cpu().numpy()
+        r = f - orc.op_apply(m, xn, mask=mask)
+        assert np.sqrt(orc.glsc3(r, r, m.mult)) <= 1.5e-10 * fn
+
+
 def test_masked_kernels_bitexact(pkg, orc, dev):
     rng = np.random.default_rng(9)
     n = 5000
