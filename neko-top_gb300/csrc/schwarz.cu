@@ -7,12 +7,15 @@
 // into each neighbour ((lx+2)^3 nodes); A~_e is the separable approximation of
 // the local operator on that extended box,
 //   h1 (Bz x By x Kx + Bz x Ky x Bx + Kz x By x Bx) + h2 (Bz x By x Bx),
-// with 1D stiffness/mass matrices assembled from the element and the adjacent
-// GLL interval of each neighbour (homogeneous Dirichlet one node further out),
-// inverted through the generalised eigenvectors of each 1D pair
-// (Lynch, Rice & Thomas 1964; Fischer 1997, "An overlapping Schwarz method for
-// spectral element solution of the incompressible Navier-Stokes equations").
-// Element lengths come from the node coordinates; h1/h2 are element means.
+// with 1D stiffness/mass matrices assembled from the element's GLL interval
+// and one interval of the element's own length on each side (homogeneous
+// Dirichlet one node further out), inverted through the generalised
+// eigenvectors of each 1D pair (Lynch, Rice & Thomas 1964; Fischer 1997, "An
+// overlapping Schwarz method for spectral element solution of the
+// incompressible Navier-Stokes equations").  With the element's own length on
+// all three intervals every element shares the reference pair (S^, lam^),
+// scaled by its lengths.  Element lengths come from the node coordinates;
+// h1/h2 are element means.
 //
 // Optional coarse level (two-level Schwarz): z += P A_c^{-1} P^T r on the
 // element vertices (Q1), solved by fast diagonalisation; see the coarse-level
@@ -80,16 +83,27 @@ __global__ void k_coef_means(const double* __restrict__ h1, double h1c, const do
 
 
 // Extended residual -> FDM solve -> extended result for a batch of EPB
-// elements per block.  A thread owns two 1D lines of an element's extended
-// box, (u, v) and (u, v + LE/2), in the two halves of packed FP32 FMAs
-// (__ffma2_rn): each direction pass loads the pair of lines from shared
-// memory, applies the 1D eigenvector matrix (rows f, f+1 interleaved, read
-// as float4 broadcasts and shared by both lines) and writes them back in
-// place, so a pass needs one buffer and one barrier.
-//   operator region, per element:  P[3][LE/2][LE][2]  P[d][f/2][p][f&1] = S_d[p][f]
-//                                  Q[3][LE/2][LE][2]  Q[d][a/2][f][a&1] = S_d[a][f]
-//                                  lam[3][LE], (h1, h2)
-//   tile region, per element:      A[a + RS b + PS c]
+// elements per block.
+//
+// The local model of element e is the separable operator on its extended
+// box with the element's own length h_d in each direction for the adjacent
+// intervals too.  Then every element shares one pair of 1D generalised
+// eigenvectors and eigenvalues, those of the reference interval (h = 2):
+// S_d = S^ sqrt(2 / h_d) and lam_d = (4 / h_d^2) lam^, so
+//   A_e^-1 = 8 / (hx hy hz) (S^ x S^ x S^) D_e^-1 (S^ x S^ x S^)^T,
+//   D_e(a, b, c) = h1 (4 lam^_a / hx^2 + 4 lam^_b / hy^2 + 4 lam^_c / hz^2) + h2.
+// (Using the neighbours' own lengths instead changed no iteration count on
+// the deformed boxes measured.)  S^ sits in the kernel-parameter bank and is
+// read at compile-time indices, so the transforms load no operator from
+// memory; an element brings only its six scalars.
+//
+// A thread owns two 1D lines of an element's extended box, (u, v) and
+// (u, v + LE/2).  Each direction pass loads a line from the shared tile,
+// applies S^ (or its transpose) two outputs at a time with packed FP32 FMAs
+// (__ffma2_rn: rows f, f+1 of S^ against the duplicated line value) and
+// writes the line back in place, so a pass needs one buffer and one barrier.
+//   per element: scalars (sx, sy, sz, c, h1, h2) = (4/hx^2, 4/hy^2, 4/hz^2,
+//                8/(hx hy hz), h1, h2); tile A[a + RS b + PS c]
 // Tile strides: lines of a warp are consecutive (u fastest).  (RS, PS) make
 // the r and s passes (two each) free of bank conflicts and the tile stride
 // TPER keeps warps that span two elements free as well; the single t pass
@@ -99,6 +113,14 @@ struct CoarsePhi {
   float p[2][NTG_LXMAX];  // p[0][i] = (1 - xi_i) / 2, p[1][i] = (1 + xi_i) / 2
 };
 
+// the reference interval's extended 1D eigenvectors, as output pairs
+template <int LE>
+struct FdmRef {
+  float P[LE / 2][LE][2];  // forward:  P[f/2][p][f&1] = S^[p][f]
+  float Q[LE / 2][LE][2];  // backward: Q[a/2][f][a&1] = S^[a][f]
+  float lam[LE];
+};
+
 template <int LX>
 struct FdmCfg {
   static constexpr int LE = LX + 2, LE2 = LE * LE, LE3 = LE2 * LE, TPE = LE2 / 2;
@@ -106,14 +128,13 @@ struct FdmCfg {
   static constexpr int PS = LX == 8 ? 170 : LX == 6 ? 72 : 43;
   static constexpr int SPAN = (LE - 1) * (1 + RS + PS) + 1;
   static constexpr int TPER = LX == 8 ? 1714 : LX == 6 ? 576 : 257;
-  static constexpr int POFF = 0, QOFF = 3 * LE2, LOFF = 6 * LE2, HOFF = LOFF + 3 * LE;
-  static constexpr int MPER = (HOFF + 2 + 3) & ~3;  // 16-byte aligned operator slots
+  static constexpr int NSC = 8;  // per-element scalars (six used)
   static constexpr int EPB = LX == 4 ? 16 : 8, THREADS = EPB * TPE, MINB = LX == 8 ? 3 : 4;
   // coarse restriction partials (8 per thread): in the tile rows' padding
   // (a in [LE, RS), two rows per thread) when it is wide enough, else after the tiles
   static constexpr bool HOLES = 2 * (RS - LE) >= 8;
   static constexpr int RED = HOLES ? 0 : EPB * TPE * 8;
-  static constexpr size_t SMEM = ((size_t)EPB * (MPER + TPER) + RED) * sizeof(float);
+  static constexpr size_t SMEM = ((size_t)EPB * (NSC + TPER) + RED) * sizeof(float);
   static_assert(LE % 2 == 0 && TPER >= SPAN && THREADS <= 1024, "layout");
 };
 
@@ -134,7 +155,9 @@ __device__ __forceinline__ float* crs_slot(float* A, float* red, int el, int tl,
 template <int LE>
 __device__ __forceinline__ float2 dup(float v) { return make_float2(v, v); }
 
-// out(line1, line2)[f * ST] = sum_p M[f][p] in2[p] for both lines of the thread
+// out(line1, line2)[f * ST] = sum_p M[f][p] in2[p] for both lines of the
+// thread; M as interleaved output pairs in shared memory (row pair fp:
+// M[fp*2LE + 2p + k] = M[2fp + k][p]), read as float4 broadcasts
 template <int LE, int ST>
 __device__ __forceinline__ void fdm_pair(const float* __restrict__ M, const float2 (&in)[LE], float* d1, float* d2) {
 #pragma unroll
@@ -178,43 +201,38 @@ __device__ __forceinline__ void fdm_pair_reg(const float* __restrict__ M, const 
 
 template <int LX>
 __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
-    k_fdm(const float* __restrict__ r, float* __restrict__ ze, const float* __restrict__ S,
-          const float* __restrict__ lam, const float* __restrict__ hc, int Ex, int Ey, int Ez,
-          const Scalars* sc, float* __restrict__ corner, CoarsePhi ph) {
+    k_fdm(const float* __restrict__ r, float* __restrict__ ze, const float* __restrict__ esc, int Ex, int Ey,
+          int Ez, const Scalars* sc, float* __restrict__ corner, CoarsePhi ph,
+          const __grid_constant__ FdmRef<LX + 2> R) {
   using C = FdmCfg<LX>;
   constexpr int LE = C::LE, LE2 = C::LE2, LE3 = C::LE3, N = LX - 1, RS = C::RS, PS = C::PS, TPE = C::TPE;
-  constexpr int EPB = C::EPB, LX2 = LX * LX, LX3 = LX2 * LX, H = LE / 2;
+  constexpr int EPB = C::EPB, NSC = C::NSC, LX2 = LX * LX, LX3 = LX2 * LX, H = LE / 2;
   if (sc && sc->done) return;
   extern __shared__ __align__(16) float smem[];
   const int nelv = Ex * Ey * Ez;
   const int tid = threadIdx.x, el = tid / TPE, tl = tid - el * TPE;
   const int u = tl % LE, v1 = tl / LE, v2 = v1 + H;  // lines (u, v1) and (u, v2); tl + TPE = u + LE v2
-  float* ms = smem + el * C::MPER;
-  float* A = smem + EPB * C::MPER + el * C::TPER;
-  float* red = smem + EPB * (C::MPER + C::TPER);
+  float* es = smem + el * NSC;
+  float* A = smem + EPB * NSC + el * C::TPER;
+  float* red = smem + EPB * (NSC + C::TPER);
   __shared__ float sp[2][LX];  // Q1 basis at the GLL nodes
+  __shared__ __align__(16) float sP[LE2], sQ[LE2];  // reference pairs (forward, backward)
+  __shared__ float slam[LE];                        // reference eigenvalues
   if (tid == 0) {
 #pragma unroll
     for (int t = 0; t < 2 * LX; ++t) sp[t / LX][t % LX] = ph.p[t / LX][t % LX];  // constant indices
   }
+  for (int t = tid; t < LE2; t += blockDim.x) {
+    sP[t] = (&R.P[0][0][0])[t];
+    sQ[t] = (&R.Q[0][0][0])[t];
+  }
+  if (tid < LE) slam[tid] = R.lam[tid];
   __syncthreads();
   float2 in[LE];
   for (int e0 = blockIdx.x * EPB; e0 < nelv; e0 += gridDim.x * EPB) {
     const int e = e0 + el;
     const bool live = e < nelv;
-    // operators: entries (a, f) = (v, u) of S[e][d] for both lines (coalesced over lines)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const int aa = q ? v2 : v1, ff = u;
-        const float val = live ? S[(int64_t)e * 3 * LE2 + d * LE2 + tl + q * TPE] : 0.f;
-        ms[C::POFF + d * LE2 + (ff >> 1) * 2 * LE + 2 * aa + (ff & 1)] = val;
-        ms[C::QOFF + d * LE2 + (aa >> 1) * 2 * LE + 2 * ff + (aa & 1)] = val;
-      }
-    }
-    if (tl < 3 * LE) ms[C::LOFF + tl] = live ? lam[(int64_t)e * 3 * LE + tl] : 0.f;
-    if (tl < 2) ms[C::HOFF + tl] = live ? hc[2 * (int64_t)e + tl] : 1.f;
+    if (tl < NSC) es[tl] = live ? esc[(int64_t)e * NSC + tl] : 1.f;
     // gather R_e r: columns (a, b) = (u, v1), (u, v2) over c
     if (live) {
       const int exy = e / Ex, ex = e - exy * Ex, ez = exy / Ey, ey = exy - ez * Ey;
@@ -262,15 +280,13 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       }
     }
     __syncthreads();
-    const float* P = ms + C::POFF;
-    const float* Q = ms + C::QOFF;
     // r forward: lines (b, c) = (u, v) along a
     {
       float* l1 = A + RS * u + PS * v1;
       float* l2 = A + RS * u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[p], l2[p]);
-      fdm_pair<LE, 1>(P, in, l1, l2);
+      fdm_pair<LE, 1>(sP, in, l1, l2);
     }
     __syncthreads();
     // s forward: lines (a, c) = (u, v) along b
@@ -279,26 +295,25 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[RS * p], l2[RS * p]);
-      fdm_pair<LE, RS>(P + LE2, in, l1, l2);
+      fdm_pair<LE, RS>(sP, in, l1, l2);
     }
     __syncthreads();
-    // t forward, scale by the inverse eigenvalue sums, t back: lines (a, b) = (u, v)
+    // t forward, scale (c_e / D_e), t back: lines (a, b) = (u, v) along c
     {
       float* l1 = A + u + RS * v1;
       float* l2 = A + u + RS * v2;
-      const float* L = ms + C::LOFF;
-      const float h1 = ms[C::HOFF], h2 = ms[C::HOFF + 1];
-      const float la1 = L[u] + L[LE + v1], la2 = L[u] + L[LE + v2];
+      const float sx = es[0], sy = es[1], sz = es[2], ce = es[3], h1 = es[4], h2 = es[5];
+      const float la1 = h1 * (sx * slam[u] + sy * slam[v1]) + h2, la2 = h1 * (sx * slam[u] + sy * slam[v2]) + h2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[PS * p], l2[PS * p]);
       float2 t[LE];
-      fdm_pair_reg<LE>(P + 2 * LE2, in, t);
+      fdm_pair_reg<LE>(sP, in, t);
 #pragma unroll
       for (int f = 0; f < LE; ++f) {
-        const float lf = L[2 * LE + f];
-        in[f] = make_float2(__fdividef(t[f].x, h1 * (la1 + lf) + h2), __fdividef(t[f].y, h1 * (la2 + lf) + h2));
+        const float lf = h1 * sz * slam[f];
+        in[f] = make_float2(__fdividef(ce * t[f].x, la1 + lf), __fdividef(ce * t[f].y, la2 + lf));
       }
-      fdm_pair<LE, PS>(Q + 2 * LE2, in, l1, l2);
+      fdm_pair<LE, PS>(sQ, in, l1, l2);
     }
     __syncthreads();
     // s back
@@ -307,7 +322,7 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[RS * p], l2[RS * p]);
-      fdm_pair<LE, RS>(Q + LE2, in, l1, l2);
+      fdm_pair<LE, RS>(sQ, in, l1, l2);
     }
     __syncthreads();
     // r back
@@ -316,7 +331,7 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + RS * u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[p], l2[p]);
-      fdm_pair<LE, 1>(Q, in, l1, l2);
+      fdm_pair<LE, 1>(sQ, in, l1, l2);
     }
     __syncthreads();
     // coarse restriction of the element: 8 threads sum the partials in order
@@ -334,6 +349,24 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       }
     }
     __syncthreads();
+  }
+}
+
+// per-element scalars of the local model from the element lengths and the
+// h1 / h2 means: (4/hx^2, 4/hy^2, 4/hz^2, 8/(hx hy hz), h1, h2)
+__global__ void k_elem_scalars(const float* __restrict__ hl, const float* __restrict__ hc, float* __restrict__ esc,
+                               int64_t nelv) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nelv; e += (int64_t)gridDim.x * blockDim.x) {
+    const float hx = hl[3 * e], hy = hl[3 * e + 1], hz = hl[3 * e + 2];
+    float* o = esc + 8 * e;
+    o[0] = 4.f / (hx * hx);
+    o[1] = 4.f / (hy * hy);
+    o[2] = 4.f / (hz * hz);
+    o[3] = 8.f / (hx * hy * hz);
+    o[4] = hc[2 * e];
+    o[5] = hc[2 * e + 1];
+    o[6] = 0.f;
+    o[7] = 0.f;
   }
 }
 
@@ -662,9 +695,10 @@ static void jacobi_eig(int n, double* a, double* v, double* w) {
 struct ntg_schwarz {
   ntg_plan* plan = nullptr;
   int Ex = 0, Ey = 0, Ez = 0, LE = 0;
-  float* S = nullptr;    // E x 3 x LE^2 (column f = eigenvector f)
-  float* lam = nullptr;  // E x 3 x LE
+  float* hld = nullptr;  // E x 3 element lengths (device)
+  float* esc = nullptr;  // E x 8 per-element scalars of the local model
   float* hc = nullptr;   // E x 2 (h1, h2 element means)
+  std::vector<double> Sref, lamref;  // reference (h = 2) extended 1D eigenpairs
   float* ze = nullptr;   // E x LE^3 extended results
   int fdm_grid = 0;      // persistent grid of the FDM kernel (blocks resident on all SMs)
   std::vector<double> hl;  // element lengths (host)
@@ -714,7 +748,7 @@ static void fdm_1d(const ntg_plan* p, double hl, double hc, double hr, double* S
 }
 
 static void schwarz_free(ntg_schwarz* s) {
-  dev_free(s->S); dev_free(s->lam); dev_free(s->hc); dev_free(s->ze);
+  dev_free(s->hld); dev_free(s->esc); dev_free(s->hc); dev_free(s->ze);
   for (int d = 0; d < 3; ++d) dev_free(s->cS[d]);
   dev_free(s->clam); dev_free(s->corner); dev_free(s->cwork); dev_free(s->uc); dev_free(s->dw);
 }
@@ -906,8 +940,18 @@ int fdm_prepare(ntg_schwarz* w) {
 template <int LX>
 int fdm_launch(ntg_schwarz* w, const float* r, cudaStream_t s, const Scalars* sc) {
   using C = FdmCfg<LX>;
-  k_fdm<LX><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->S, w->lam, w->hc, w->Ex, w->Ey, w->Ez, sc,
-                                                      w->coarse_ready ? w->corner : nullptr, w->ph);
+  constexpr int LE = LX + 2;
+  FdmRef<LE> R;
+  for (int a = 0; a < LE; ++a) {
+    for (int f = 0; f < LE; ++f) {
+      const float v = (float)w->Sref[a * LE + f];
+      R.P[f >> 1][a][f & 1] = v;
+      R.Q[a >> 1][f][a & 1] = v;
+    }
+    R.lam[a] = (float)w->lamref[a];
+  }
+  k_fdm<LX><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
+                                                      w->coarse_ready ? w->corner : nullptr, w->ph, R);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
@@ -995,7 +1039,7 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
   int st = NTG_OK;
   double* dl = nullptr;
   do {
-    if ((st = dev_alloc(&s->S, (size_t)E * 3 * LE2)) || (st = dev_alloc(&s->lam, (size_t)E * 3 * LE)) ||
+    if ((st = dev_alloc(&s->hld, (size_t)E * 3)) || (st = dev_alloc(&s->esc, (size_t)E * 8)) ||
         (st = dev_alloc(&s->hc, (size_t)E * 2)) || (st = dev_alloc(&s->ze, (size_t)E * LE2 * LE)) ||
         (st = dev_alloc(&dl, (size_t)E * 3)))
       break;
@@ -1007,37 +1051,16 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
       set_error("ntg_schwarz_create: lengths");
       break;
     }
-    // 1D operators per element and direction; repeated length triples reuse
-    // one decomposition (lengths rounded to 6 significant digits)
-    std::vector<float> hS((size_t)E * 3 * LE2), hL((size_t)E * 3 * LE);
-    std::map<std::tuple<long long, long long, long long>, std::pair<std::vector<double>, std::vector<double>>> cache;
-    auto key = [](double v) { return (long long)std::llround(v * 1e6 / std::pow(10.0, std::floor(std::log10(v)))) +
-                                     (long long)(std::floor(std::log10(v)) + 400) * 100000000LL; };
-    const int dims[3] = {ex, ey, ez};
-    for (int64_t e = 0; e < E; ++e) {
-      const int c[3] = {(int)(e % ex), (int)((e / ex) % ey), (int)(e / ((int64_t)ex * ey))};
-      const int64_t stride[3] = {1, ex, (int64_t)ex * ey};
-      for (int d = 0; d < 3; ++d) {
-        const double hc = s->hl[3 * e + d];
-        const double hlft = c[d] > 0 ? s->hl[3 * (e - stride[d]) + d] : hc;
-        const double hrgt = c[d] < dims[d] - 1 ? s->hl[3 * (e + stride[d]) + d] : hc;
-        auto kk = std::make_tuple(key(hlft), key(hc), key(hrgt));
-        auto it = cache.find(kk);
-        if (it == cache.end()) {
-          std::vector<double> Sv(LE2), Lv(LE);
-          fdm_1d(p, hlft, hc, hrgt, Sv.data(), Lv.data());
-          it = cache.emplace(kk, std::make_pair(Sv, Lv)).first;
-        }
-        for (int q = 0; q < LE2; ++q) hS[(size_t)e * 3 * LE2 + d * LE2 + q] = (float)it->second.first[q];
-        for (int q = 0; q < LE; ++q) hL[(size_t)e * 3 * LE + d * LE + q] = (float)it->second.second[q];
-      }
-    }
-    if (cudaMemcpy(s->S, hS.data(), sizeof(float) * hS.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(s->lam, hL.data(), sizeof(float) * hL.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    std::vector<float> hlf(s->hl.begin(), s->hl.end());
+    if (cudaMemcpy(s->hld, hlf.data(), sizeof(float) * hlf.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
       st = NTG_ERR_CUDA;
       set_error("ntg_schwarz_create: upload");
       break;
     }
+    // the reference interval's extended 1D eigenpairs (h = 2 on all three intervals)
+    s->Sref.assign((size_t)LE2, 0.0);
+    s->lamref.assign((size_t)LE, 0.0);
+    fdm_1d(p, 2.0, 2.0, 2.0, s->Sref.data(), s->lamref.data());
     st = p->lx == 4 ? sw::fdm_prepare<4>(s) : p->lx == 6 ? sw::fdm_prepare<6>(s) : sw::fdm_prepare<8>(s);
     if (st) break;
     st = ntg_schwarz_update(s);
@@ -1059,6 +1082,7 @@ int ntg_schwarz_update(ntg_schwarz* s) {
   ntg_plan* p = s->plan;
   const int lx3 = p->lx * p->lx * p->lx;
   { sw::k_coef_means<<<grid_for(p->nelv, 128), 128, 0, p->stream>>>(p->h1_const ? nullptr : p->h1, p->h1c, p->ifh2 ? p->hB : nullptr, p->B, p->nelv, lx3, s->hc); NTG_COUNT_LAUNCH(); }
+  { sw::k_elem_scalars<<<grid_for(p->nelv, 128), 128, 0, p->stream>>>(s->hld, s->hc, s->esc, p->nelv); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   dev_free(s->dw);
   s->dw = nullptr;

@@ -7,8 +7,9 @@ TEST INFRASTRUCTURE ONLY: the checker for neko-top_gb300/csrc/schwarz.cu.
 on structured boxes (elements numbered x fastest).  R_e gathers the
 assembled residual on element e extended by one node layer into each
 neighbour; A~_e = h1 (Bz x By x Kx + Bz x Ky x Bx + Kz x By x Bx) + h2 Bz x By x Bx
-with 1D operators assembled from the element's and its neighbours' GLL
-intervals (Dirichlet one node beyond the extension), inverted through the
+with 1D operators assembled from the element's GLL interval and one
+interval of the element's own length on each side (Dirichlet one node
+beyond the extension), inverted through the
 generalised eigenvectors (numpy.linalg.eigh); R_e^T adds the extended result
 into a global structured grid (a different prolongation than the kernel's
 assembling pull).  Element lengths: mean distance between opposite faces.
@@ -144,10 +145,10 @@ def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False):
         strides = (1, Ex, Ex * Ey)
         Ss, Ls = [], []
         for d in range(3):
+            # the local model extends the element with intervals of its own
+            # length (the kernel's shared-reference form)
             hc = hl[e, d]
-            hlft = hl[e - strides[d], d] if c[d] > 0 else hc
-            hrgt = hl[e + strides[d], d] if c[d] < dims[d] - 1 else hc
-            S, lam = ext_1d(lx, hlft, hc, hrgt)
+            S, lam = ext_1d(lx, hc, hc, hc)
             Ss.append(S)
             Ls.append(lam)
         # gather R_e r on the extended box (index order a=x, b=y, c=z)
