@@ -394,7 +394,7 @@ struct CoarseDims {
 
 // x then y forward transforms on one active z-plane; the plane's residual is
 // gathered from the corner sums of the adjacent elements (ascending element order)
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024)
     k_crs_xy(const float* __restrict__ corner, const float* __restrict__ Sx, const float* __restrict__ Sy,
              float* __restrict__ work, CoarseDims d, const Scalars* sc) {
   if (sc && sc->done) return;
@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // z forward, scale by the inverse eigenvalue sums, z back, on one y-index g
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024)
     k_crs_z(float* __restrict__ work, const float* __restrict__ Sz, const float* __restrict__ lam, CoarseDims d,
             const Scalars* sc) {
   if (sc && sc->done) return;
@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // y then x back transforms on one active z-plane, into the full vertex grid uc
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(1024)
     k_crs_yx(const float* __restrict__ work, const float* __restrict__ Sx, const float* __restrict__ Sy,
              float* __restrict__ uc, CoarseDims d, const Scalars* sc) {
   if (sc && sc->done) return;
@@ -979,11 +979,11 @@ int pull_launch(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalar
 // transforms into uc
 inline int coarse_launch(ntg_schwarz* w, cudaStream_t s, const Scalars* sc) {
   const CoarseDims& d = w->cd;
-  k_crs_xy<<<d.m[2], 256, w->smem_xy, s>>>(w->corner, w->cS[0], w->cS[1], w->cwork, d, sc);
+  k_crs_xy<<<d.m[2], 1024, w->smem_xy, s>>>(w->corner, w->cS[0], w->cS[1], w->cwork, d, sc);
   NTG_COUNT_LAUNCH();
-  k_crs_z<<<d.m[1], 256, w->smem_z, s>>>(w->cwork, w->cS[2], w->clam, d, sc);
+  k_crs_z<<<d.m[1], 1024, w->smem_z, s>>>(w->cwork, w->cS[2], w->clam, d, sc);
   NTG_COUNT_LAUNCH();
-  k_crs_yx<<<d.m[2], 256, w->smem_xy, s>>>(w->cwork, w->cS[0], w->cS[1], w->uc, d, sc);
+  k_crs_yx<<<d.m[2], 1024, w->smem_xy, s>>>(w->cwork, w->cS[0], w->cS[1], w->uc, d, sc);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
