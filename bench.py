@@ -274,7 +274,7 @@ def run_sequence(args, local):
     res = {}
     for mode in modes:
         coef.set_coefs(h1c=1.0, h2=design(0), ifh2=True)
-        seq = pkg.SolveSequence(coef, "cg_mixed", mode, rtol=RTOL, L=8, train_steps=30, seed=3, lr=5e-4,
+        seq = pkg.SolveSequence(coef, "cg_mixed", mode, rtol=RTOL, L=args.proj_l, train_steps=30, seed=3, lr=5e-4,
                                 pc=pc, delta=delta)
         if seq.sw is not None and args.mass_term:
             seq.sw.set_mass_term(True)
@@ -301,7 +301,7 @@ def run_sequence(args, local):
     sample = list(range(ntrain, min(nsol, ntrain + args.fp64_sample)))  # consecutive, after 8 warm-up solves
     for mode in ("zero", "projection"):
         coef.set_coefs(h1c=1.0, h2=design(0), ifh2=True)
-        seq = pkg.SolveSequence(coef, "cg", mode, rtol=RTOL, L=8, pc="jacobi")
+        seq = pkg.SolveSequence(coef, "cg", mode, rtol=RTOL, L=args.proj_l, pc="jacobi")
         its, secs = [], []
         last = 0
         for t in sorted(set(list(range(max(0, sample[0] - args.fp64_warm), sample[0])) + sample)):
@@ -450,6 +450,16 @@ def run_ours(args, ws, rank, local):
             "bytes_per_dof": bytes_per_dof, "traffic": args.traffic if args.traffic is not None
             else measured_traffic("k_ax_helm_f32_tma", n, ncoef)}
 
+    # the FP64 operator against the FP64 compute roof: 116 flop per local DOF
+    # (six contractions of 2(N+1) flop each, plus the metric mix), the peak
+    # from an FMA-chain probe on GB300 (not in MEASURED_PEAKS.json)
+    ax64 = ktimes.get("ax_fp64")
+    t64 = ax64["avg_us"] * 1e-6 if ax64 else t_ax64
+    fp64_peak = 1200.0
+    roof64 = {"kernel": "k_ax_helm<double,8> (FP64 Ax, residual replacements)", "bound": "fp64",
+              "achieved": round(116.0 * n / t64 / 1e9, 1), "peak": fp64_peak, "unit": "GFLOP/s",
+              "frac": round(116.0 * n / t64 / 1e9 / fp64_peak, 4), "peak_source": "own FP64 FMA-chain probe"}
+
     # end to end through the public API: host RHS in, host solution out
     f_h = f.cpu().pin_memory()
     x_h = torch.empty(n, dtype=torch.float64).pin_memory()
@@ -500,6 +510,7 @@ def run_ours(args, ws, rank, local):
         "error_vs_fp64_solution": err_vs_fp64,
         "ax_gdof_s": {"fp64": round(n / t_ax64 / 1e9, 3), "fp32": round(n / t_ax32 / 1e9, 3)},
         "roofline": roof,
+        "roofline_fp64_ax": roof64,
         "kernels_in_one_solve": ktimes,
         "e2e": {"value": round(ws * args.steps / t_e2e, 4), "unit": "solves/s",
                 "h2d_bytes_per_step": int(f_h.numel() * 8), "d2h_bytes_per_step": int(x_h.numel() * 8),
@@ -633,6 +644,7 @@ def main(argv=None):
                    help="instead of the headline line: a solve sequence with each initial-guess mode")
     p.add_argument("--fp64-sample", type=int, default=10, help="FP64 drop-in solves sampled in --sequence")
     p.add_argument("--fp64-warm", type=int, default=8, help="FP64 solves before the sample (fills projection)")
+    p.add_argument("--proj-l", type=int, default=20, help="projection space size of --sequence (Neko's default 20)")
     p.add_argument("--seq-modes", default="zero,projection,learned,learned_only",
                    help="initial-guess modes of --sequence (comma separated)")
     args = p.parse_args(argv)
