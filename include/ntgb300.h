@@ -365,6 +365,46 @@ int ntg_filter_apply(ntg_plan* plan, ntg_ksp* ksp, double* X_out_d, const double
                      ntg_monitor* mon);
 
 /* ---------------------------------------------------------------------- */
+/* derivative operators and the adjoint-equation terms (FP64, on the plan's */
+/* stream).  The operators are Neko's (operators.f90: opgrad, dudxyz, cdtp, */
+/* conv1, curl) as the reference calls them; ntg_metrics_set must come     */
+/* first (it derives the cofactors drdx..dtdz, 1/jac and 1/gs(B) from the   */
+/* coordinates, as coef_t's generate_dxyz does).                            */
+/* ---------------------------------------------------------------------- */
+int ntg_metrics_set(ntg_plan* plan, const double* x_d, const double* y_d, const double* z_d);
+/* du = du/dx_dir, strong (dir 0..2) */
+int ntg_dudxyz(ntg_plan* plan, double* du_d, const double* u_d, int dir);
+/* (ux, uy, uz) = B grad u (weak gradient); adv_adjoint_no_dealias.f90:165-167 */
+int ntg_opgrad(ntg_plan* plan, double* ux_d, double* uy_d, double* uz_d, const double* u_d);
+/* dtx = transpose of opgrad's `dir` component applied to x;
+   adv_adjoint_no_dealias.f90:297-299 */
+int ntg_cdtp(ntg_plan* plan, double* dtx_d, const double* x_d, int dir);
+/* du = vx du/dx + vy du/dy + vz du/dz (strong); adv_adjoint_no_dealias.f90:383 */
+int ntg_conv1(ntg_plan* plan, double* du_d, const double* u_d, const double* vx_d, const double* vy_d,
+              const double* vz_d);
+/* w = Binv gs(B curl u); adjoint_minimum_dissipation_source_term.f90:231 */
+int ntg_curl(ntg_plan* plan, double* w1_d, double* w2_d, double* w3_d, const double* u1_d, const double* u2_d,
+             const double* u3_d);
+/* adjoint advection without dealiasing, f_i -= sum_j u_j opgrad_i(Ub_j) +
+   sum_d cdtp_d(u_i Ub_d) (adv_adjoint_no_dealias.f90:118-255 and 266-302, device
+   branch); (vx, vy, vz) the adjoint velocity, (vxb, vyb, vzb) the primal one */
+int ntg_adjoint_advection_no_dealias(ntg_plan* plan, double* fx_d, double* fy_d, double* fz_d,
+                                     const double* vx_d, const double* vy_d, const double* vz_d,
+                                     const double* vxb_d, const double* vyb_d, const double* vzb_d);
+/* linearised advection without dealiasing, f_i -= B conv1(u_i; Ub) +
+   B conv1(Ub_i; u) (adv_adjoint_no_dealias.f90:365-427 linear_advection_no_dealias) */
+int ntg_linear_advection_no_dealias(ntg_plan* plan, double* fx_d, double* fy_d, double* fz_d,
+                                    const double* vx_d, const double* vy_d, const double* vz_d,
+                                    const double* vxb_d, const double* vyb_d, const double* vzb_d);
+/* minimum-dissipation adjoint forcing f += scale curl(curl(u)), kept on the
+   zone's nodes only when nzone > 0 (zone_d: nzone unique indices, base
+   `base`) (adjoint_minimum_dissipation_source_term.f90:175-249).  Allocates
+   6 n doubles of scratch and synchronises the plan's stream. */
+int ntg_adjoint_min_dissipation(ntg_plan* plan, double* fx_d, double* fy_d, double* fz_d, const double* u_d,
+                                const double* v_d, const double* w_d, double scale, const int32_t* zone_d,
+                                int64_t nzone, int base);
+
+/* ---------------------------------------------------------------------- */
 /* masked vector kernels of neko-top, same names and signatures as the     */
 /* reference's extern "C" wrappers (math_ext.cu:49-108): device arrays by  */
 /* value, sizes and scalars by pointer, 1-based masks, real = double.      */

@@ -110,6 +110,15 @@ SIGNATURES = {
     "ntg_permeability": (_i, [_vp, _vp, _i64, _d, _d, _d, _vp]),
     "ntg_sens_min_dissipation": (_i, [_vp] * 7 + [_i64, _i, _d, _vp]),
     "ntg_filter_apply": (_i, [_vp, _vp, _vp, _vp, _d, C.POINTER(ntg_monitor)]),
+    "ntg_metrics_set": (_i, [_vp, _vp, _vp, _vp]),
+    "ntg_dudxyz": (_i, [_vp, _vp, _vp, _i]),
+    "ntg_opgrad": (_i, [_vp] * 5),
+    "ntg_cdtp": (_i, [_vp, _vp, _vp, _i]),
+    "ntg_conv1": (_i, [_vp] * 6),
+    "ntg_curl": (_i, [_vp] * 7),
+    "ntg_adjoint_advection_no_dealias": (_i, [_vp] * 10),
+    "ntg_linear_advection_no_dealias": (_i, [_vp] * 10),
+    "ntg_adjoint_min_dissipation": (_i, [_vp] * 7 + [_d, _vp, _i64, _i]),
     "cuda_cadd_mask": (None, [_vp, _pd, _pi, _vp, _pi]),
     "cuda_invcol1_mask": (None, [_vp, _pi, _vp, _pi]),
     "cuda_col2_mask": (None, [_vp, _vp, _pi, _vp, _pi]),

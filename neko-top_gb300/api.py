@@ -94,6 +94,8 @@ class coef_t:
         self.nelv, self.lx, self.n, self.nu, self.nshared = ne.value, l.value, nn.value, nu.value, nsh.value
         self.device = x.device
         self.mask = None
+        self._xyz = (x, y, z)  # for the derivative metrics, derived on first use
+        self._metrics = False
 
     @classmethod
     def box(cls, ex, ey, ez, lx=8, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.0, seed=0, device="cuda"):
@@ -123,6 +125,16 @@ class coef_t:
             return
         check(lib().ntg_plan_set_mask(self.handle, _ptr(mask, torch.int32, name="mask"), mask.numel(), int(base)))
         self.mask = mask
+
+    def metrics(self):
+        """The cofactors drdx..dtdz, 1/jac and 1/gs(B) for the derivative
+        operators (Neko's coef_t generate_dxyz / Binv), derived once."""
+        if not self._metrics:
+            x, y, z = self._xyz
+            check(lib().ntg_metrics_set(self.handle, _ptr(x, n=self.n, name="x"), _ptr(y, n=self.n, name="y"),
+                                        _ptr(z, n=self.n, name="z")))
+            self._metrics = True
+        return self
 
     def geometry(self):
         out = {k: torch.empty(self.n, dtype=torch.float64, device=self.device)
@@ -696,6 +708,85 @@ def permeability(kappa, phi, perm0, perm1, penalty):
 def sens_min_dissipation(s, u, v, w, ua, va, wa, if_lube=False, K_scale=0.0):
     check(lib().ntg_sens_min_dissipation(_ptr(s), _ptr(u), _ptr(v), _ptr(w), _ptr(ua), _ptr(va), _ptr(wa), u.numel(),
                                          int(bool(if_lube)), float(K_scale), _stream()))
+
+
+# derivative operators, Neko's operators.f90 as the adjoint terms call them
+# (sources/adjoint/adv_adjoint_no_dealias.f90, FP64, on the current stream)
+_DIRS = {"x": 0, "y": 1, "z": 2, 0: 0, 1: 1, 2: 2}
+
+
+def _f(coef, t, name):
+    return _ptr(t, n=coef.n, name=name)
+
+
+def opgrad(ux, uy, uz, u, coef: coef_t):
+    """(ux, uy, uz) = B grad u (weak gradient)."""
+    check(lib().ntg_opgrad(coef.metrics().handle, _f(coef, ux, "ux"), _f(coef, uy, "uy"), _f(coef, uz, "uz"),
+                           _f(coef, u, "u")))
+
+
+def dudxyz(du, u, direction, coef: coef_t):
+    """du = du/dx_direction (strong), direction "x" | "y" | "z"."""
+    check(lib().ntg_dudxyz(coef.metrics().handle, _f(coef, du, "du"), _f(coef, u, "u"), _DIRS[direction]))
+
+
+def cdtp(dtx, x, direction, coef: coef_t):
+    """dtx = transpose of opgrad's `direction` component applied to x
+    (Neko's cdtp(dtx, x, dr, ds, dt, coef) with the direction's cofactors)."""
+    check(lib().ntg_cdtp(coef.metrics().handle, _f(coef, dtx, "dtx"), _f(coef, x, "x"), _DIRS[direction]))
+
+
+def conv1(du, u, vx, vy, vz, coef: coef_t):
+    """du = (v . grad) u (strong, pointwise)."""
+    check(lib().ntg_conv1(coef.metrics().handle, _f(coef, du, "du"), _f(coef, u, "u"), _f(coef, vx, "vx"),
+                          _f(coef, vy, "vy"), _f(coef, vz, "vz")))
+
+
+def curl(w1, w2, w3, u1, u2, u3, coef: coef_t):
+    """w = Binv gs(B curl u)."""
+    check(lib().ntg_curl(coef.metrics().handle, *[_f(coef, t, f"w{i}") for i, t in enumerate((w1, w2, w3))],
+                         *[_f(coef, t, f"u{i}") for i, t in enumerate((u1, u2, u3))]))
+
+
+class adv_lin_no_dealias_t:
+    """Adjoint and linearised advection without dealiasing
+    (sources/adjoint/adv_adjoint_no_dealias.f90: adjoint_advection_no_dealias
+    :118-255 and linear_advection_no_dealias :365-427), same argument order:
+    (vx, vy, vz) the adjoint / perturbation velocity, (vxb, vyb, vzb) the
+    base flow, (fx, fy, fz) the right-hand side, updated in place."""
+
+    def __init__(self, coef: coef_t):
+        self.coef = coef.metrics()
+
+    def compute_adjoint(self, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz):
+        c = self.coef
+        check(lib().ntg_adjoint_advection_no_dealias(
+            c.handle, *[_f(c, t, "f") for t in (fx, fy, fz)], *[_f(c, t, "v") for t in (vx, vy, vz)],
+            *[_f(c, t, "vb") for t in (vxb, vyb, vzb)]))
+
+    def compute_linear(self, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz):
+        c = self.coef
+        check(lib().ntg_linear_advection_no_dealias(
+            c.handle, *[_f(c, t, "f") for t in (fx, fy, fz)], *[_f(c, t, "v") for t in (vx, vy, vz)],
+            *[_f(c, t, "vb") for t in (vxb, vyb, vzb)]))
+
+
+class adjoint_minimum_dissipation_source_term_t:
+    """f += obj_scale curl(curl(u)), optionally kept inside a zone
+    (sources/source_terms/adjoint_minimum_dissipation_source_term.f90:175-249;
+    the zone is the point-zone mask, unique 1-based indices by default)."""
+
+    def __init__(self, fields, u, v, w, coef: coef_t, obj_scale=1.0, mask=None, base=1):
+        self.fields, self.u, self.v, self.w = tuple(fields), u, v, w
+        self.coef, self.obj_scale, self.mask, self.base = coef.metrics(), float(obj_scale), mask, int(base)
+
+    def compute(self, t=0.0, tstep=0):
+        c, (fx, fy, fz) = self.coef, self.fields
+        m = self.mask
+        check(lib().ntg_adjoint_min_dissipation(
+            c.handle, _f(c, fx, "fx"), _f(c, fy, "fy"), _f(c, fz, "fz"), _f(c, self.u, "u"), _f(c, self.v, "v"),
+            _f(c, self.w, "w"), self.obj_scale, _ptr(m, torch.int32, name="mask") if m is not None else None,
+            0 if m is None else m.numel(), self.base))
 
 
 # masked ops: the reference's cuda_* entry points (math_ext.cu:49-108)

@@ -144,6 +144,10 @@ struct ntg_plan {
   double* red_part = nullptr;    // kRedSlots * kRedLanes
   ntg::Scalars* scal = nullptr;  // generic scalars for standalone dots
   double* host_red = nullptr;    // pinned
+  // derivative operators (deriv.cu): 9 metric cofactors and 1/jac
+  // (10 x n), and 1 / gs(B)
+  double* met = nullptr;
+  double* binv = nullptr;
 };
 
 namespace ntg {
