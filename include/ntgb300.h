@@ -398,11 +398,38 @@ int ntg_linear_advection_no_dealias(ntg_plan* plan, double* fx_d, double* fy_d, 
                                     const double* vxb_d, const double* vyb_d, const double* vzb_d);
 /* minimum-dissipation adjoint forcing f += scale curl(curl(u)), kept on the
    zone's nodes only when nzone > 0 (zone_d: nzone unique indices, base
-   `base`) (adjoint_minimum_dissipation_source_term.f90:175-249).  Allocates
-   6 n doubles of scratch and synchronises the plan's stream. */
+   `base`) (adjoint_minimum_dissipation_source_term.f90:175-249).  Uses the
+   plan's derivative scratch (6 n doubles, allocated on first use). */
 int ntg_adjoint_min_dissipation(ntg_plan* plan, double* fx_d, double* fy_d, double* fz_d, const double* u_d,
                                 const double* v_d, const double* w_d, double scale, const int32_t* zone_d,
                                 int64_t nzone, int base);
+
+/* Pn/Pn splitting residuals (FP64), replacing prs_res%compute and
+   vel_res%compute (sources/adjoint/adjoint_pnpn.f90:716-723, :747-753).
+   mu/rho: fields (mu_d, rho_d) or, when the pointer is NULL, the constants
+   mu_c, rho_c; bd = the first BDF coefficient, dt the step.  Results are
+   neither gs-assembled nor masked (the caller does both next, as the
+   reference does).  The plan's h1/h2 are left untouched.
+
+   p_res = -A(h1 = 1/rho) p + sum_d cdtp_d(ta_d)
+           - (bd/dt) sum_c u_c s_c over the velocity-surface entries
+           - sum_c ta_c s'_c over the symmetry-surface entries,
+   ta_d = Binv gs(f_d / rho - (mu/rho) B curl(curl(u_e))_d).
+   Surface lists: prs_idx/sym_idx (n entries, unique, base `base`) with
+   s = 3 x n doubles (all x, then all y, then all z): the outward normal
+   times the facet area at each entry.  Uses the plan's derivative
+   scratch. */
+int ntg_pnpn_prs_res(ntg_plan* plan, double* p_res_d, const double* p_d, const double* u_d, const double* v_d,
+                     const double* w_d, const double* ue_d, const double* ve_d, const double* we_d,
+                     const double* fx_d, const double* fy_d, const double* fz_d, const double* mu_d, double mu_c,
+                     const double* rho_d, double rho_c, double bd, double dt, const int32_t* prs_idx_d,
+                     const double* prs_s_d, int64_t nprs, const int32_t* sym_idx_d, const double* sym_s_d,
+                     int64_t nsym, int base);
+/* u_res_c = f_c - (mu K + rho (bd/dt) B) u_c - opgrad_c(p), one fused pass */
+int ntg_pnpn_vel_res(ntg_plan* plan, double* u_res_d, double* v_res_d, double* w_res_d, const double* u_d,
+                     const double* v_d, const double* w_d, const double* p_d, const double* fx_d, const double* fy_d,
+                     const double* fz_d, const double* mu_d, double mu_c, const double* rho_d, double rho_c,
+                     double bd, double dt);
 
 /* ---------------------------------------------------------------------- */
 /* masked vector kernels of neko-top, same names and signatures as the     */

@@ -789,6 +789,58 @@ class adjoint_minimum_dissipation_source_term_t:
             0 if m is None else m.numel(), self.base))
 
 
+def _prop(coef, v, name):
+    """(pointer, constant) of a material property given as a field or a number."""
+    if isinstance(v, torch.Tensor):
+        return _f(coef, v, name), 0.0
+    return None, float(v)
+
+
+def _surface(coef, surf, name):
+    if surf is None:
+        return None, None, 0
+    idx, sv = surf
+    if sv.shape != (3, idx.numel()):
+        raise ValueError(f"{name}: s must be 3 x {idx.numel()} (normal times area per entry)")
+    return _ptr(idx, torch.int32, name=name + " idx"), _ptr(sv.contiguous(), name=name + " s"), idx.numel()
+
+
+class pnpn_prs_res_t:
+    """Pressure residual of the Pn/Pn splitting, prs_res%compute
+    (sources/adjoint/adjoint_pnpn.f90:716-723), same argument order.  The
+    surface terms are (idx, s) pairs: unique node indices (base `base`, 1 for
+    Neko masks) and s = 3 x len(idx) outward normals times facet areas.
+    mu and rho are numbers or fields.  p_res is neither assembled nor masked."""
+
+    def compute(self, p, p_res, u, v, w, u_e, v_e, w_e, f_x, f_y, f_z, c_Xh: coef_t, bc_prs_surface=None,
+                bc_sym_surface=None, bd=1.0, dt=1.0, mu=1.0, rho=1.0, base=1):
+        c = c_Xh.metrics()
+        mp, mc = _prop(c, mu, "mu")
+        rp, rc = _prop(c, rho, "rho")
+        pi, ps, pn = _surface(c, bc_prs_surface, "bc_prs_surface")
+        si, ss, sn = _surface(c, bc_sym_surface, "bc_sym_surface")
+        check(lib().ntg_pnpn_prs_res(c.handle, _f(c, p_res, "p_res"), _f(c, p, "p"),
+                                     *[_f(c, t, "u") for t in (u, v, w)], *[_f(c, t, "u_e") for t in (u_e, v_e, w_e)],
+                                     *[_f(c, t, "f") for t in (f_x, f_y, f_z)], mp, mc, rp, rc, float(bd), float(dt),
+                                     pi, ps, pn, si, ss, sn, int(base)))
+
+
+class pnpn_vel_res_t:
+    """Velocity residual of the Pn/Pn splitting, vel_res%compute
+    (sources/adjoint/adjoint_pnpn.f90:747-753): u_res_c = f_c - (mu K +
+    rho bd/dt B) u_c - B grad_c p, all three components in one pass; the
+    coef's own h1/h2 are left as they were."""
+
+    def compute(self, u, v, w, u_res, v_res, w_res, p, f_x, f_y, f_z, c_Xh: coef_t, mu=1.0, rho=1.0, bd=1.0,
+                dt=1.0):
+        c = c_Xh.metrics()
+        mp, mc = _prop(c, mu, "mu")
+        rp, rc = _prop(c, rho, "rho")
+        check(lib().ntg_pnpn_vel_res(c.handle, *[_f(c, t, "res") for t in (u_res, v_res, w_res)],
+                                     *[_f(c, t, "u") for t in (u, v, w)], _f(c, p, "p"),
+                                     *[_f(c, t, "f") for t in (f_x, f_y, f_z)], mp, mc, rp, rc, float(bd), float(dt)))
+
+
 # masked ops: the reference's cuda_* entry points (math_ext.cu:49-108)
 def _mi(mask):
     return C.byref(C.c_int(int(mask.numel())))

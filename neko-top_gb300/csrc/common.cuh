@@ -148,6 +148,8 @@ struct ntg_plan {
   // (10 x n), and 1 / gs(B)
   double* met = nullptr;
   double* binv = nullptr;
+  double* dscr = nullptr;  // their scratch (plan_scratch)
+  int64_t dscr_n = 0;
 };
 
 namespace ntg {

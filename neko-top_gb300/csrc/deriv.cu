@@ -22,41 +22,10 @@
 // (thread (i, j) owns the column k = 0..LX-1), element tiles in shared
 // memory, D from the kernel-parameter bank.  FP64 throughout (these feed the
 // adjoint right-hand sides and sensitivities).
-#include <type_traits>
-
-#include "common.cuh"
+#include "deriv.cuh"
 
 namespace ntg {
 namespace dv {
-
-template <int LX>
-struct DMat {
-  double d[LX * LX];
-  double w[LX];  // GLL weights
-};
-
-template <int LX, int NT>
-struct Shape {
-  static constexpr int LX2 = LX * LX, LX3 = LX2 * LX;
-  static constexpr int EPB0 = 256 / LX2 < 1 ? 1 : 256 / LX2;
-  static constexpr int EPBS = 45056 / (NT * LX3 * 8) < 1 ? 1 : 45056 / (NT * LX3 * 8);
-  static constexpr int EPB = EPB0 < EPBS ? EPB0 : EPBS;
-  static constexpr int NW = EPB * LX2, THREADS = (NW + 31) / 32 * 32;
-};
-
-// reference derivatives at (i, j, k) of the tile s (s[c * LX2 + b * LX + a])
-template <int LX>
-__device__ __forceinline__ void rgrad(const double* s, const DMat<LX>& M, int i, int j, int k, double& ur, double& us,
-                                      double& ut) {
-  constexpr int LX2 = LX * LX;
-  ur = us = ut = 0.0;
-#pragma unroll
-  for (int l = 0; l < LX; ++l) {
-    ur = fma(M.d[i * LX + l], s[k * LX2 + j * LX + l], ur);
-    us = fma(M.d[j * LX + l], s[k * LX2 + l * LX + i], us);
-    ut = fma(M.d[k * LX + l], s[l * LX2 + j * LX + i], ut);
-  }
-}
 
 // 9 cofactors (drdx, drdy, drdz, dsdx, ..., dtdz) and 1/jac, stored m * n + l
 template <int LX>
@@ -307,58 +276,37 @@ __global__ void k_add_zone(double* __restrict__ f0, double* __restrict__ f1, dou
   }
 }
 
-template <int LX>
-DMat<LX> dmat(const ntg_plan* p) {
-  DMat<LX> M;
-  for (int q = 0; q < LX * LX; ++q) M.d[q] = p->D[q];
-  for (int q = 0; q < LX; ++q) M.w[q] = p->wq[q];
-  return M;
-}
-
-template <int NT, typename F>
-int dispatch(int lx, F&& f) {
-  switch (lx) {
-    case 2: return f(std::integral_constant<int, 2>{});
-    case 3: return f(std::integral_constant<int, 3>{});
-    case 4: return f(std::integral_constant<int, 4>{});
-    case 5: return f(std::integral_constant<int, 5>{});
-    case 6: return f(std::integral_constant<int, 6>{});
-    case 7: return f(std::integral_constant<int, 7>{});
-    case 8: return f(std::integral_constant<int, 8>{});
-    case 9: return f(std::integral_constant<int, 9>{});
-    case 10: return f(std::integral_constant<int, 10>{});
-    default: set_error("derivative operators: lx=%d not compiled (2..10)", lx); return NTG_ERR_UNSUPPORTED;
-  }
-}
-
-template <int LX, int NT>
-int grid_of(const ntg_plan* p) {
-  constexpr int EPB = Shape<LX, NT>::EPB;
-  const int64_t g = (p->nelv + EPB - 1) / EPB, cap = (int64_t)num_sms() * 32;
-  return (int)(g < cap ? g : cap);
-}
-
 }  // namespace dv
 
-static int need_metrics(const ntg_plan* p) {
-  if (!p->met) {
-    set_error("derivative operators: call ntg_metrics_set(plan, x, y, z) first");
-    return NTG_ERR_INVALID;
+double* plan_scratch(ntg_plan* p, int64_t count) {
+  if (p->dscr_n < count) {
+    // the stream may still use the old buffer
+    if (p->dscr && cudaStreamSynchronize(p->stream) != cudaSuccess) return nullptr;
+    dev_free(p->dscr);
+    p->dscr_n = 0;
+    if (dev_alloc(&p->dscr, (size_t)count)) return nullptr;
+    p->dscr_n = count;
   }
-  return NTG_OK;
+  return p->dscr;
 }
 
-// w = Binv gs(B curl u)
-static int curl_avg(ntg_plan* p, double* w0, double* w1, double* w2, const double* ux, const double* uy,
-                    const double* uz) {
+// w = B curl u (unassembled)
+int bcurl(ntg_plan* p, double* w0, double* w1, double* w2, const double* ux, const double* uy, const double* uz) {
   cudaStream_t s = p->stream;
-  NTG_TRY(dv::dispatch<3>(p->lx, [&](auto L) -> int {
+  return dv::dispatch<3>(p->lx, [&](auto L) -> int {
     constexpr int LX = decltype(L)::value;
     dv::k_curl<LX><<<dv::grid_of<LX, 3>(p), dv::Shape<LX, 3>::THREADS, 0, s>>>(w0, w1, w2, ux, uy, uz, p->nelv,
                                                                                  dv::dmat<LX>(p), p->met, p->n);
     NTG_COUNT_LAUNCH();
     return NTG_OK;
-  }));
+  });
+}
+
+// w = Binv gs(B curl u)
+int curl_avg(ntg_plan* p, double* w0, double* w1, double* w2, const double* ux, const double* uy,
+             const double* uz) {
+  cudaStream_t s = p->stream;
+  NTG_TRY(bcurl(p, w0, w1, w2, ux, uy, uz));
   NTG_TRY(gs_launch(p, w0, NTG_GS_ADD, s));
   NTG_TRY(gs_launch(p, w1, NTG_GS_ADD, s));
   NTG_TRY(gs_launch(p, w2, NTG_GS_ADD, s));
@@ -527,20 +475,16 @@ int ntg_adjoint_min_dissipation(ntg_plan* p, double* fx, double* fy, double* fz,
   NTG_CHECK_ARG(p && fx && fy && fz && u && v && w && (nzone == 0 || zone_d) && nzone >= 0,
                 "ntg_adjoint_min_dissipation: bad argument");
   NTG_TRY(need_metrics(p));
-  const size_t n = (size_t)p->n;
-  double* t = nullptr;
-  NTG_TRY(dev_alloc(&t, 6 * n));
-  int st = curl_avg(p, t, t + n, t + 2 * n, u, v, w);
-  if (!st) st = curl_avg(p, t + 3 * n, t + 4 * n, t + 5 * n, t, t + n, t + 2 * n);
-  if (!st) {
-    dv::k_add_zone<<<grid_for(nzone ? nzone : p->n, 256), 256, 0, p->stream>>>(
-        fx, fy, fz, t + 3 * n, t + 4 * n, t + 5 * n, scale, nzone ? zone_d : nullptr, nzone, base, p->n);
-    NTG_COUNT_LAUNCH();
-    if (cudaGetLastError() != cudaSuccess) st = NTG_ERR_CUDA;
-  }
-  cudaStreamSynchronize(p->stream);
-  dev_free(t);
-  return st;
+  const int64_t n = p->n;
+  double* t = plan_scratch(p, 6 * n);
+  if (!t) return NTG_ERR_ALLOC;
+  NTG_TRY(curl_avg(p, t, t + n, t + 2 * n, u, v, w));
+  NTG_TRY(curl_avg(p, t + 3 * n, t + 4 * n, t + 5 * n, t, t + n, t + 2 * n));
+  dv::k_add_zone<<<grid_for(nzone ? nzone : n, 256), 256, 0, p->stream>>>(
+      fx, fy, fz, t + 3 * n, t + 4 * n, t + 5 * n, scale, nzone ? zone_d : nullptr, nzone, base, n);
+  NTG_COUNT_LAUNCH();
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
 }
 
 }  // extern "C"

@@ -351,7 +351,7 @@ static void plan_free(ntg_plan* p) {
   dev_free(p->mask); dev_free(p->dinv); dev_free(p->dinvf);
   dev_free(p->red_part); dev_free(p->scal); dev_free(p->dev_err);
   dev_free(p->gs2); dev_free(p->gs4); dev_free(p->gs8); dev_free(p->gsx_idx); dev_free(p->gsx_off);
-  dev_free(p->met); dev_free(p->binv);
+  dev_free(p->met); dev_free(p->binv); dev_free(p->dscr);
   if (p->host_red) cudaFreeHost(p->host_red);
   p->host_red = nullptr;
 }
