@@ -334,6 +334,79 @@ def run_sequence(args, local):
     }
 
 
+FP64_TFLOPS = 1.20  # FP64 FMA probe on this GPU (the roof of the FP64 element-tile kernels)
+
+
+def run_terms(args, local):
+    """The FP64 terms either side of each solve of the adjoint/forward step,
+    each timed alone with CUDA events on the launching stream: the Pn/Pn
+    velocity and pressure residuals, the adjoint and linearised advection
+    (no dealiasing), the minimum-dissipation forcing, and the FP64 Ax for
+    scale.  Fields are seeded random, mu = 0.01, rho = 1, bd = 11/6,
+    dt = 1e-3; inputs are larger than L2."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = CONFIGS[args.config]
+    coef, _, _ = setup_gpu_case(pkg, cfg, dev)
+    coef.metrics()
+    n = coef.n
+    gen = torch.Generator(device=dev).manual_seed(11)
+    F = lambda: torch.randn(n, dtype=torch.float64, device=dev, generator=gen)
+    u, v, w, ue, ve, we, p, fx, fy, fz = (F() for _ in range(10))
+    r = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(3)]
+    pres = torch.zeros(n, dtype=torch.float64, device=dev)
+    ex, ey, ez = cfg["E"]
+    face = pkg.mask_face_xmax(ex, ey, ez, LX, device=dev)
+    s = torch.zeros(3, face.numel(), dtype=torch.float64, device=dev)
+    s[0] = 1.0 / (ey * ez * (LX - 1) ** 2)
+    vel, prs = pkg.pnpn_vel_res_t(), pkg.pnpn_prs_res_t()
+    adv = pkg.adv_lin_no_dealias_t(coef)
+    md = pkg.adjoint_minimum_dissipation_source_term_t(r, u, v, w, coef, obj_scale=0.5)
+    ax = pkg.ax_helm_t()
+    bd, dt = 11.0 / 6.0, 1e-3
+    terms = {
+        "vel_res": lambda: vel.compute(u, v, w, *r, p, fx, fy, fz, coef, mu=0.01, rho=1.0, bd=bd, dt=dt),
+        "prs_res": lambda: prs.compute(p, pres, u, v, w, ue, ve, we, fx, fy, fz, coef, (face, s), None, bd=bd,
+                                       dt=dt, mu=0.01, rho=1.0),
+        "adjoint_advection": lambda: adv.compute_adjoint(u, v, w, ue, ve, we, *r),
+        "linear_advection": lambda: adv.compute_linear(u, v, w, ue, ve, we, *r),
+        "min_dissipation": lambda: md.compute(),
+        "ax_helm_fp64": lambda: ax.compute(pres, p, coef),
+    }
+    # algorithmic FP64 flops per local DOF (lx = 8) of the single-kernel terms
+    flops = {"vel_res": 3 * (48 + 21 + 48 + 48 + 8 + 6), "ax_helm_fp64": 116}
+    L = pkg.lib()
+    out = {}
+    sampler = ClockSampler(local)
+    with sampler:
+        for name, fn in terms.items():
+            for _ in range(args.warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = int(L.ntg_launch_count())
+            e0.record()
+            for _ in range(args.steps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            rec = {"ms": round(ms, 4), "gdof_s": round(n / ms / 1e6, 2),
+                   "launches": (int(L.ntg_launch_count()) - l0) // args.steps}
+            if name in flops:
+                tf = flops[name] * n / (ms * 1e-3) / 1e12
+                rec["fp64_tflops"] = round(tf, 3)
+                rec["frac_of_fp64_roof"] = round(tf / FP64_TFLOPS, 3)
+            out[name] = rec
+    return {"mode": "terms", "config": {"workload": args.config, "desc": cfg["desc"], "n_local_dofs": n,
+                                         "l2": "inputs larger than L2"},
+            "dtype": "f64", "steps": args.steps, "warmup": args.warmup, "terms": out,
+            "clocks": sampler.summary()}
+
+
 def run_ours(args, ws, rank, local):
     import torch
     import __graft_entry__ as ge
@@ -645,6 +718,8 @@ def main(argv=None):
     p.add_argument("--fp64-sample", type=int, default=10, help="FP64 drop-in solves sampled in --sequence")
     p.add_argument("--fp64-warm", type=int, default=8, help="FP64 solves before the sample (fills projection)")
     p.add_argument("--proj-l", type=int, default=20, help="projection space size of --sequence (Neko's default 20)")
+    p.add_argument("--terms", action="store_true",
+                   help="time the FP64 terms either side of each solve (residuals, advection, forcing)")
     p.add_argument("--seq-modes", default="zero,projection,learned,learned_only",
                    help="initial-guess modes of --sequence (comma separated)")
     args = p.parse_args(argv)
@@ -652,6 +727,9 @@ def main(argv=None):
     ws, rank, local = dist_env()
     if args.sequence:
         print(json.dumps(run_sequence(args, local)), flush=True)
+        return 0
+    if args.terms:
+        print(json.dumps(run_terms(args, local)), flush=True)
         return 0
     if args.impl == "reference":
         res = run_reference(args, ws, rank)

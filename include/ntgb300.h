@@ -76,6 +76,7 @@ typedef struct ntg_ksp ntg_ksp;   /* Krylov solver workspace */
 typedef struct ntg_proj ntg_proj; /* residual projection space */
 typedef struct ntg_guess ntg_guess; /* learned initial-guess network */
 typedef struct ntg_schwarz ntg_schwarz; /* overlapping Schwarz preconditioner */
+typedef struct ntg_dealias ntg_dealias; /* GL over-integration space of a plan */
 
 /* ksp_monitor_t of the reference (iter, res_start, res_final;
    sources/mapping_functions/PDE_filter_mapping.f90:265-272), plus the
@@ -403,6 +404,29 @@ int ntg_linear_advection_no_dealias(ntg_plan* plan, double* fx_d, double* fy_d, 
 int ntg_adjoint_min_dissipation(ntg_plan* plan, double* fx_d, double* fy_d, double* fz_d, const double* u_d,
                                 const double* v_d, const double* w_d, double scale, const int32_t* zone_d,
                                 int64_t nzone, int base);
+
+/* Dealiased advection (sources/adjoint/adv_adjoint_dealias.f90).  create
+   replaces init_dealias (:137-224): lxd Gauss-Legendre points per direction
+   (lxd <= 0: 3 lx / 2, advection_adjoint_fctry.f90:66-90), the GLL -> GL
+   interpolation J and the metric cofactors interpolated to GL (9 x nelv
+   lxd^3 doubles).  Needs ntg_metrics_set first; compiled (lx, lxd) pairs:
+   (4,6) (5,7) (6,9) (7,10) (8,12).  The handle borrows the plan. */
+int ntg_dealias_create(ntg_dealias** d, ntg_plan* plan, int lxd);
+int ntg_dealias_destroy(ntg_dealias* d);
+int ntg_dealias_info(const ntg_dealias* d, int* lxd, int64_t* ngl);
+/* interp_t%map: to_gl != 0: out (GL, nelv lxd^3) = J in (GLL);
+   to_gl == 0: out (GLL) = J^T in (GL) */
+int ntg_dealias_map(ntg_dealias* d, double* out_d, const double* in_d, int to_gl);
+/* f_i -= J^T [ sum_j u_j opgrad_i(Ub_j) + sum_d cdtp_d(u_i Ub_d) ]_GL
+   (compute_adjoint_advection_dealias, :235-462) */
+int ntg_adjoint_advection_dealias(ntg_dealias* d, double* fx_d, double* fy_d, double* fz_d, const double* vx_d,
+                                  const double* vy_d, const double* vz_d, const double* vxb_d, const double* vyb_d,
+                                  const double* vzb_d);
+/* f_i -= J^T [ u . opgrad(Ub_i) + Ub . opgrad(u_i) ]_GL
+   (compute_linear_advection_dealias, :470-600) */
+int ntg_linear_advection_dealias(ntg_dealias* d, double* fx_d, double* fy_d, double* fz_d, const double* vx_d,
+                                 const double* vy_d, const double* vz_d, const double* vxb_d, const double* vyb_d,
+                                 const double* vzb_d);
 
 /* Pn/Pn splitting residuals (FP64), replacing prs_res%compute and
    vel_res%compute (sources/adjoint/adjoint_pnpn.f90:716-723, :747-753).

@@ -121,6 +121,12 @@ SIGNATURES = {
     "ntg_adjoint_min_dissipation": (_i, [_vp] * 7 + [_d, _vp, _i64, _i]),
     "ntg_pnpn_prs_res": (_i, [_vp] * 13 + [_d, _vp, _d, _d, _d, _vp, _vp, _i64, _vp, _vp, _i64, _i]),
     "ntg_pnpn_vel_res": (_i, [_vp] * 12 + [_d, _vp, _d, _d, _d]),
+    "ntg_dealias_create": (_i, [_vp, _vp, _i]),
+    "ntg_dealias_destroy": (_i, [_vp]),
+    "ntg_dealias_info": (_i, [_vp, _vp, _vp]),
+    "ntg_dealias_map": (_i, [_vp, _vp, _vp, _i]),
+    "ntg_adjoint_advection_dealias": (_i, [_vp] * 10),
+    "ntg_linear_advection_dealias": (_i, [_vp] * 10),
     "cuda_cadd_mask": (None, [_vp, _pd, _pi, _vp, _pi]),
     "cuda_invcol1_mask": (None, [_vp, _pi, _vp, _pi]),
     "cuda_col2_mask": (None, [_vp, _vp, _pi, _vp, _pi]),

@@ -771,6 +771,51 @@ class adv_lin_no_dealias_t:
             *[_f(c, t, "vb") for t in (vxb, vyb, vzb)]))
 
 
+class adv_lin_dealias_t:
+    """Dealiased adjoint and linearised advection
+    (sources/adjoint/adv_adjoint_dealias.f90: init_dealias :137-224,
+    compute_adjoint :235-462, compute_linear :470-600), same argument order
+    as adv_lin_no_dealias_t.  lxd None: 3 lx / 2 Gauss-Legendre points per
+    direction (advection_adjoint_fctry.f90:66-90)."""
+
+    def __init__(self, coef: coef_t, lxd=None):
+        self.coef = coef.metrics()
+        h = C.c_void_p()
+        check(lib().ntg_dealias_create(C.byref(h), coef.handle, int(lxd or 0)))
+        self._h = h
+        l, ng = C.c_int(), C.c_int64()
+        check(lib().ntg_dealias_info(h, C.byref(l), C.byref(ng)))
+        self.lxd, self.n_gl = l.value, ng.value
+
+    def map_to_gl(self, out_gl, x):
+        check(lib().ntg_dealias_map(self._h, _ptr(out_gl, n=self.n_gl, name="out"), _f(self.coef, x, "x"), 1))
+
+    def map_to_gll(self, out, x_gl):
+        check(lib().ntg_dealias_map(self._h, _f(self.coef, out, "out"), _ptr(x_gl, n=self.n_gl, name="x"), 0))
+
+    def _run(self, fn, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz):
+        c = self.coef
+        check(fn(self._h, *[_f(c, t, "f") for t in (fx, fy, fz)], *[_f(c, t, "v") for t in (vx, vy, vz)],
+                 *[_f(c, t, "vb") for t in (vxb, vyb, vzb)]))
+
+    def compute_adjoint(self, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz):
+        self._run(lib().ntg_adjoint_advection_dealias, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz)
+
+    def compute_linear(self, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz):
+        self._run(lib().ntg_linear_advection_dealias, vx, vy, vz, vxb, vyb, vzb, fx, fy, fz)
+
+    def free(self):
+        if getattr(self, "_h", None) is not None:
+            lib().ntg_dealias_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 class adjoint_minimum_dissipation_source_term_t:
     """f += obj_scale curl(curl(u)), optionally kept inside a zone
     (sources/source_terms/adjoint_minimum_dissipation_source_term.f90:175-249;

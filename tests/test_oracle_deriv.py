@@ -35,3 +35,30 @@ def test_oracle_min_dissipation_is_minus_laplacian():
     f = dr.min_dissipation_forcing(m, lambda v: orc.gs_op(m, v), [np.zeros(m.n)] * 3, u, 1.0)
     for c in f:
         assert np.abs(c + 2.0).max() < 1e-9
+
+
+def test_oracle_adjoint_is_transpose_of_linearised():
+    from oracle import dealias_ref as dl
+    m = orc.build_mesh(2, 2, 1, 6, amp=0.04, seed=3)
+    rng = np.random.default_rng(0)
+    u = [rng.standard_normal(m.n) for _ in range(3)]
+    a = [rng.standard_normal(m.n) for _ in range(3)]
+    ub = [np.sin(m.x) + m.y, np.cos(m.y) * m.z, m.x * m.z]
+    zero = [np.zeros(m.n)] * 3
+    for mod in (dr, dl):
+        L = [-t for t in mod.linear_advection(m, zero, u, ub)]
+        A = [-t for t in mod.adjoint_advection(m, zero, a, ub)]
+        lhs = sum(float(a[i] @ L[i]) for i in range(3))
+        rhs = sum(float(A[i] @ u[i]) for i in range(3))
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_oracle_gl_interpolation_exact_on_polynomials():
+    from oracle import dealias_ref as dl
+    m = orc.build_mesh(2, 1, 1, 8, amp=0.0, seed=1)
+    g = dl.GL(m)
+    p = m.x ** 3 * m.y - m.z ** 5
+    xg, yg, zg = g.to_gl(m.x), g.to_gl(m.y), g.to_gl(m.z)
+    assert np.abs(g.to_gl(p) - (xg ** 3 * yg - zg ** 5)).max() < 1e-12
+    # GL weights integrate the mass exactly: sum over GL of w3 * jac = volume
+    assert abs(g.wg.sum() - 2.0) < 1e-14
