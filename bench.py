@@ -364,6 +364,7 @@ def run_terms(args, local):
     s[0] = 1.0 / (ey * ez * (LX - 1) ** 2)
     vel, prs = pkg.pnpn_vel_res_t(), pkg.pnpn_prs_res_t()
     adv = pkg.adv_lin_no_dealias_t(coef)
+    adv_d = pkg.adv_lin_dealias_t(coef)
     md = pkg.adjoint_minimum_dissipation_source_term_t(r, u, v, w, coef, obj_scale=0.5)
     ax = pkg.ax_helm_t()
     bd, dt = 11.0 / 6.0, 1e-3
@@ -373,11 +374,22 @@ def run_terms(args, local):
                                        dt=dt, mu=0.01, rho=1.0),
         "adjoint_advection": lambda: adv.compute_adjoint(u, v, w, ue, ve, we, *r),
         "linear_advection": lambda: adv.compute_linear(u, v, w, ue, ve, we, *r),
+        "adjoint_advection_dealias": lambda: adv_d.compute_adjoint(u, v, w, ue, ve, we, *r),
+        "linear_advection_dealias": lambda: adv_d.compute_linear(u, v, w, ue, ve, we, *r),
         "min_dissipation": lambda: md.compute(),
         "ax_helm_fp64": lambda: ax.compute(pres, p, coef),
     }
-    # algorithmic FP64 flops per local DOF (lx = 8) of the single-kernel terms
-    flops = {"vel_res": 3 * (48 + 21 + 48 + 48 + 8 + 6), "ax_helm_fp64": 116}
+    # algorithmic FP64 flops per local DOF (lx = 8, lxd = 12; an FMA counts 2):
+    # vel_res: 3 x (Helmholtz 117 + mass 3) + pressure gradient 48 + 3 x 8.
+    # Dealiased, per element: 9 tensor interpolations (6 to GL, 3 back) of
+    # 29,184 FMA each; per GL point the adjoint term's 3 GL gradients (108 FMA),
+    # mixing (36 + 9) and per component a D^T of u_i V (36 FMA + 36 products);
+    # the linear term's 6 GL gradients (216 FMA) and fluxes (36); / 512 GLL points.
+    gl = 12 ** 3
+    interp = 12 * 512 + 144 * 64 + 1728 * 8
+    flops = {"vel_res": 3 * 120 + 48 + 24, "ax_helm_fp64": 116,
+             "adjoint_advection_dealias": (2 * (9 * interp + gl * (108 + 45 + 3 * 36)) + gl * (6 + 3 * 36)) / 512,
+             "linear_advection_dealias": 2 * (9 * interp + gl * (216 + 36)) / 512}
     L = pkg.lib()
     out = {}
     sampler = ClockSampler(local)

@@ -232,15 +232,17 @@ __global__ void __launch_bounds__(Shape<LX, 3>::THREADS)
     if (act) {
       for (int k = 0; k < LX; ++k) {
         const int64_t q = e * LX3 + k * LX2 + ij;
-        auto d = [&](const double* s, int dir) {
-          double r, ss, t;
-          rgrad<LX>(s, M, i, j, k, r, ss, t);
-          return met[dir * n + q] * r + met[(3 + dir) * n + q] * ss + met[(6 + dir) * n + q] * t;
+        double g[3][3];  // g[f][r|s|t]: reference derivatives of field f
+        rgrad<LX>(sx[le], M, i, j, k, g[0][0], g[0][1], g[0][2]);
+        rgrad<LX>(sy[le], M, i, j, k, g[1][0], g[1][1], g[1][2]);
+        rgrad<LX>(sz[le], M, i, j, k, g[2][0], g[2][1], g[2][2]);
+        auto d = [&](int f, int dir) {
+          return met[dir * n + q] * g[f][0] + met[(3 + dir) * n + q] * g[f][1] + met[(6 + dir) * n + q] * g[f][2];
         };
         const double w3 = M.w[i] * M.w[j] * M.w[k];
-        w0[q] = w3 * (d(sz[le], 1) - d(sy[le], 2));
-        w1[q] = w3 * (d(sx[le], 2) - d(sz[le], 0));
-        w2[q] = w3 * (d(sy[le], 0) - d(sx[le], 1));
+        w0[q] = w3 * (d(2, 1) - d(1, 2));
+        w1[q] = w3 * (d(0, 2) - d(2, 0));
+        w2[q] = w3 * (d(1, 0) - d(0, 1));
       }
     }
     __syncthreads();

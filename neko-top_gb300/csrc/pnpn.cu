@@ -122,10 +122,23 @@ __global__ void __launch_bounds__(Shape<LX, 5>::THREADS)
     const int64_t e = g * EPB + le;
     const bool act = worker && e < nelv;
     for (int k = 0; k < LX && worker; ++k) sp[le][k * LX2 + ij] = act ? p[e * LX3 + k * LX2 + ij] : 0.0;
+    __syncthreads();
+    // res_c = f_c - opgrad_c(p) first (the pressure gradient once for all
+    // three components); the thread that writes a node updates it below
+    if (act) {
+      for (int k = 0; k < LX; ++k) {
+        const int64_t q = e * LX3 + k * LX2 + ij;
+        double pr, ps, pt;
+        rgrad<LX>(sp[le], M, i, j, k, pr, ps, pt);
+        const double w3 = M.w[i] * M.w[j] * M.w[k];
+        r0[q] = f0[q] - w3 * (met[0 * n + q] * pr + met[3 * n + q] * ps + met[6 * n + q] * pt);
+        r1[q] = f1[q] - w3 * (met[1 * n + q] * pr + met[4 * n + q] * ps + met[7 * n + q] * pt);
+        r2[q] = f2[q] - w3 * (met[2 * n + q] * pr + met[5 * n + q] * ps + met[8 * n + q] * pt);
+      }
+    }
 #pragma unroll 1
     for (int cc = 0; cc < 3; ++cc) {
       const double* u = cc == 0 ? u0 : (cc == 1 ? u1 : u2);
-      const double* f = cc == 0 ? f0 : (cc == 1 ? f1 : f2);
       double* r = cc == 0 ? r0 : (cc == 1 ? r1 : r2);
       for (int k = 0; k < LX && worker; ++k) su[le][k * LX2 + ij] = act ? u[e * LX3 + k * LX2 + ij] : 0.0;
       __syncthreads();
@@ -153,12 +166,8 @@ __global__ void __launch_bounds__(Shape<LX, 5>::THREADS)
             acc = fma(M.d[l * LX + j], fs[le][k * LX2 + l * LX + i], acc);
             acc = fma(M.d[l * LX + k], ft[le][l * LX2 + j * LX + i], acc);
           }
-          double pr, ps, pt;
-          rgrad<LX>(sp[le], M, i, j, k, pr, ps, pt);
-          const double w3 = M.w[i] * M.w[j] * M.w[k];
-          const double gp = w3 * (met[cc * n + q] * pr + met[(3 + cc) * n + q] * ps + met[(6 + cc) * n + q] * pt);
           const double h2 = c.r(q) * bddt;
-          r[q] = f[q] - (acc + h2 * B[q] * su[le][k * LX2 + ij]) - gp;
+          r[q] -= acc + h2 * B[q] * su[le][k * LX2 + ij];
         }
       }
       __syncthreads();
