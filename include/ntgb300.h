@@ -77,6 +77,7 @@ typedef struct ntg_proj ntg_proj; /* residual projection space */
 typedef struct ntg_guess ntg_guess; /* learned initial-guess network */
 typedef struct ntg_schwarz ntg_schwarz; /* overlapping Schwarz preconditioner */
 typedef struct ntg_dealias ntg_dealias; /* GL over-integration space of a plan */
+typedef struct ntg_mma ntg_mma;         /* MMA optimiser state */
 
 /* ksp_monitor_t of the reference (iter, res_start, res_final;
    sources/mapping_functions/PDE_filter_mapping.f90:265-272), plus the
@@ -454,6 +455,30 @@ int ntg_pnpn_vel_res(ntg_plan* plan, double* u_res_d, double* v_res_d, double* w
                      const double* v_d, const double* w_d, const double* p_d, const double* fx_d, const double* fy_d,
                      const double* fz_d, const double* mu_d, double mu_c, const double* rho_d, double rho_c,
                      double bd, double dt);
+
+/* ---------------------------------------------------------------------- */
+/* MMA optimiser on the GPU (FP64), replacing mma_t (sources/mma/mma.f90,  */
+/* sources/mma/bcknd/cpu/mma_cpu.f90): Svanberg's method of moving         */
+/* asymptotes with the primal-dual interior-point subproblem solver.       */
+/* ---------------------------------------------------------------------- */
+/* mma_t%init (mma.f90:186-295).  n design variables (x_d, xmin_d, xmax_d:
+   device), m in [1, 4] constraints with a, c, d host arrays of m; max_iter
+   <= 0, epsimin <= 0, asy* <= 0 take the reference's defaults (100,
+   1e-9 sqrt(m + n), 0.5, 1.2, 0.7).  Kernels run on `stream`. */
+int ntg_mma_create(ntg_mma** mma, int64_t n, int m, const double* x_d, double a0, const double* a, const double* c,
+                   const double* d, const double* xmin_d, const double* xmax_d, int max_iter, double epsimin,
+                   double asyinit, double asyincr, double asydecr, void* stream);
+int ntg_mma_destroy(ntg_mma* mma);
+/* mma_t%update (mma.f90:297-324): x_d (device, n) is replaced by the new
+   design; df0dx_d device n; fval host m; dfdx_d device, the reference's
+   dfdx(m, n) layout (entry (i, j) at i + m j).  Synchronises the stream. */
+int ntg_mma_update(ntg_mma* mma, int iter, double* x_d, const double* df0dx_d, const double* fval,
+                   const double* dfdx_d);
+/* mma_t%KKT (mma.f90:355-393): max and 2-norm of the KKT residual at x */
+int ntg_mma_kkt(ntg_mma* mma, const double* x_d, const double* df0dx_d, const double* fval, const double* dfdx_d,
+                double* residumax, double* residunorm);
+/* interior-point Newton steps taken so far, last KKT max and norm */
+int ntg_mma_info(const ntg_mma* mma, long long* newton_steps, double* residumax, double* residunorm);
 
 /* ---------------------------------------------------------------------- */
 /* masked vector kernels of neko-top, same names and signatures as the     */

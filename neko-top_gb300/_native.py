@@ -121,6 +121,11 @@ SIGNATURES = {
     "ntg_adjoint_min_dissipation": (_i, [_vp] * 7 + [_d, _vp, _i64, _i]),
     "ntg_pnpn_prs_res": (_i, [_vp] * 13 + [_d, _vp, _d, _d, _d, _vp, _vp, _i64, _vp, _vp, _i64, _i]),
     "ntg_pnpn_vel_res": (_i, [_vp] * 12 + [_d, _vp, _d, _d, _d]),
+    "ntg_mma_create": (_i, [_vp, _i64, _i, _vp, _d, _pd, _pd, _pd, _vp, _vp, _i, _d, _d, _d, _d, _vp]),
+    "ntg_mma_destroy": (_i, [_vp]),
+    "ntg_mma_update": (_i, [_vp, _i, _vp, _vp, _pd, _vp]),
+    "ntg_mma_kkt": (_i, [_vp, _vp, _vp, _pd, _vp, _pd, _pd]),
+    "ntg_mma_info": (_i, [_vp, C.POINTER(C.c_longlong), _pd, _pd]),
     "ntg_dealias_create": (_i, [_vp, _vp, _i]),
     "ntg_dealias_destroy": (_i, [_vp]),
     "ntg_dealias_info": (_i, [_vp, _vp, _vp]),

@@ -886,6 +886,77 @@ class pnpn_vel_res_t:
                                      *[_f(c, t, "f") for t in (f_x, f_y, f_z)], mp, mc, rp, rc, float(bd), float(dt)))
 
 
+def _hostvec(v, m, name):
+    import numpy as np
+    a = np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (m,)))
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class mma_t:
+    """The MMA optimiser on the GPU (sources/mma/mma.f90: init :186-295,
+    update :297-324, KKT :355-393), same argument meaning: x, xmin, xmax,
+    df0dx are CUDA tensors of n; fval has m values; dfdx is (m, n) as the
+    reference stores it, i.e. a CUDA tensor whose entry (i, j) sits at
+    i + m j (a torch tensor of shape (n, m), or of m * n entries)."""
+
+    def __init__(self, x, n, m, a0, a, c, d, xmin, xmax, max_iter=None, epsimin=None, asyinit=None, asyincr=None,
+                 asydecr=None):
+        self.n, self.m = int(n), int(m)
+        self._keep = [_hostvec(v, self.m, k) for k, v in (("a", a), ("c", c), ("d", d))]
+        xmin = xmin if isinstance(xmin, torch.Tensor) else torch.full_like(x, float(xmin))
+        xmax = xmax if isinstance(xmax, torch.Tensor) else torch.full_like(x, float(xmax))
+        h = C.c_void_p()
+        check(lib().ntg_mma_create(C.byref(h), self.n, self.m, _ptr(x, n=self.n, name="x"), float(a0),
+                                   *[k[1] for k in self._keep], _ptr(xmin.contiguous(), n=self.n, name="xmin"),
+                                   _ptr(xmax.contiguous(), n=self.n, name="xmax"), int(max_iter or 0),
+                                   float(epsimin or 0.0), float(asyinit or 0.0), float(asyincr or 0.0),
+                                   float(asydecr or 0.0), _stream()))
+        self._h = h
+
+    def _dfdx(self, dfdx):
+        return _ptr(dfdx.contiguous(), n=self.n * self.m, name="dfdx")
+
+    def update(self, iter, x, df0dx, fval, dfdx):
+        fv, fp = _hostvec(fval, self.m, "fval")
+        check(lib().ntg_mma_update(self._h, int(iter), _ptr(x, n=self.n, name="x"),
+                                   _ptr(df0dx, n=self.n, name="df0dx"), fp, self._dfdx(dfdx)))
+
+    def KKT(self, x, df0dx, fval, dfdx):
+        fv, fp = _hostvec(fval, self.m, "fval")
+        mx, nr = C.c_double(), C.c_double()
+        check(lib().ntg_mma_kkt(self._h, _ptr(x, n=self.n, name="x"), _ptr(df0dx, n=self.n, name="df0dx"), fp,
+                                self._dfdx(dfdx), C.byref(mx), C.byref(nr)))
+        return mx.value, nr.value
+
+    def _info(self):
+        k, mx, nr = C.c_longlong(), C.c_double(), C.c_double()
+        check(lib().ntg_mma_info(self._h, C.byref(k), C.byref(mx), C.byref(nr)))
+        return k.value, mx.value, nr.value
+
+    @property
+    def residumax(self):
+        return self._info()[1]
+
+    @property
+    def residunorm(self):
+        return self._info()[2]
+
+    @property
+    def newton_steps(self):
+        return self._info()[0]
+
+    def free(self):
+        if getattr(self, "_h", None) is not None:
+            lib().ntg_mma_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 # masked ops: the reference's cuda_* entry points (math_ext.cu:49-108)
 def _mi(mask):
     return C.byref(C.c_int(int(mask.numel())))
