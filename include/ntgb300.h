@@ -477,8 +477,9 @@ int ntg_mma_update(ntg_mma* mma, int iter, double* x_d, const double* df0dx_d, c
 /* mma_t%KKT (mma.f90:355-393): max and 2-norm of the KKT residual at x */
 int ntg_mma_kkt(ntg_mma* mma, const double* x_d, const double* df0dx_d, const double* fval, const double* dfdx_d,
                 double* residumax, double* residunorm);
-/* interior-point Newton steps taken so far, last KKT max and norm */
-int ntg_mma_info(const ntg_mma* mma, long long* newton_steps, double* residumax, double* residunorm);
+/* counts[3] (may be NULL): interior-point Newton steps, line-search trials
+   and epsilon levels taken so far; the last KKT max and norm */
+int ntg_mma_info(const ntg_mma* mma, long long* counts, double* residumax, double* residunorm);
 
 /* ---------------------------------------------------------------------- */
 /* masked vector kernels of neko-top, same names and signatures as the     */

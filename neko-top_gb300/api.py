@@ -929,9 +929,9 @@ class mma_t:
         return mx.value, nr.value
 
     def _info(self):
-        k, mx, nr = C.c_longlong(), C.c_double(), C.c_double()
-        check(lib().ntg_mma_info(self._h, C.byref(k), C.byref(mx), C.byref(nr)))
-        return k.value, mx.value, nr.value
+        k, mx, nr = (C.c_longlong * 3)(), C.c_double(), C.c_double()
+        check(lib().ntg_mma_info(self._h, k, C.byref(mx), C.byref(nr)))
+        return tuple(k), mx.value, nr.value
 
     @property
     def residumax(self):
@@ -943,6 +943,11 @@ class mma_t:
 
     @property
     def newton_steps(self):
+        return self._info()[0][0]
+
+    @property
+    def counts(self):
+        """(Newton steps, line-search trials, epsilon levels) so far."""
         return self._info()[0]
 
     def free(self):

@@ -28,6 +28,27 @@ constexpr int LANES = 2 * MMAX + MMAX * (MMAX + 1) / 2 + 2;  // sums + 1 max
 // the reference's default-kind (single precision) literals
 constexpr double C001 = (double)0.01f, C01 = (double)0.1f, C09 = (double)0.9f, C101 = (double)1.01f;
 
+__device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
+
+// 1/a and 1/b from one division (1/(ab) times the other factor): the FP64
+// pipe, not memory, bounds these kernels, and a division costs it about ten
+// FMAs.  Each result is within a few ulp of the quotient.
+__device__ __forceinline__ void rcp2(double a, double b, double& ra, double& rb) {
+  const double r = 1.0 / (a * b);
+  ra = b * r;
+  rb = a * r;
+}
+
+// 1/a, 1/b, 1/c, 1/d from one division
+__device__ __forceinline__ void rcp4(double a, double b, double c, double d, double& ra, double& rb, double& rc,
+                                     double& rd) {
+  const double ab = a * b, cd = c * d, r = 1.0 / (ab * cd), rab = cd * r, rcd = ab * r;
+  ra = b * rab;
+  rb = a * rab;
+  rc = d * rcd;
+  rd = c * rcd;
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -66,15 +87,36 @@ __device__ __forceinline__ void reduce_out(double (&v)[NS], double mx, double* _
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  // the last block: sums in block order (one thread per lane), max
-  if (threadIdx.x <= NS) {
-    const int q = threadIdx.x;
-    double acc = q < NS ? 0.0 : -INFINITY;
-    for (int b = 0; b < (int)gridDim.x; ++b) {
-      const double pv = __ldcg(part + q * kRedSlots + b);
-      acc = q < NS ? acc + pv : fmax(acc, pv);
+  // the last block: every thread takes a fixed stride of the block partials,
+  // then the fixed block tree (the same order on every run)
+  double fin[NS];
+  double fmx = -INFINITY;
+#pragma unroll
+  for (int q = 0; q < NS; ++q) fin[q] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < NS; ++q) fin[q] += __ldcg(part + q * kRedSlots + b);
+    fmx = fmax(fmx, __ldcg(part + NS * kRedSlots + b));
+  }
+#pragma unroll
+  for (int q = 0; q < NS; ++q) fin[q] = warp_sum(fin[q]);
+  fmx = warp_max(fmx);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NS; ++q) sred[q][warp] = fin[q];
+    sred[NS][warp] = fmx;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < NS; ++q) fin[q] = warp_sum(lane < nw ? sred[q][lane] : 0.0);
+    fmx = warp_max(lane < nw ? sred[NS][lane] : -INFINITY);
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NS; ++q) out[q] = fin[q];
+      out[NS] = fmx;
     }
-    out[q] = acc;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -176,16 +218,17 @@ __global__ void __launch_bounds__(NT) k_resid(Vecs V, Dual D, int64_t n, Red R) 
       xsi = V.xsi[j];
       eta = V.eta[j];
     }
-    const double ux = V.upp[j] - x, xl = x - V.low[j];
+    double rux, rxl;
+    rcp2(V.upp[j] - x, x - V.low[j], rux, rxl);
     double pl = V.p0[j], ql = V.q0[j];
 #pragma unroll
     for (int i = 0; i < M; ++i) {
       const double p = V.P[i * n + j], q = V.Q[i * n + j];
       pl += p * D.lam[i];
       ql += q * D.lam[i];
-      acc[i] += p / ux + q / xl;
+      acc[i] += p * rux + q * rxl;
     }
-    const double rex = pl / (ux * ux) - ql / (xl * xl) - xsi + eta;
+    const double rex = pl * (rux * rux) - ql * (rxl * rxl) - xsi + eta;
     const double rexsi = xsi * (x - V.alpha[j]) - D.epsi;
     const double reeta = eta * (V.beta[j] - x) - D.epsi;
     acc[M] += rex * rex + rexsi * rexsi + reeta * reeta;
@@ -195,8 +238,11 @@ __global__ void __launch_bounds__(NT) k_resid(Vecs V, Dual D, int64_t n, Red R) 
 }
 
 // Newton assembly (mma_cpu.f90:307-405): delx, diagx per j (delx/diagx and
-// diagx kept), and the sums g_i(x), b_i = sum_j GG_ij delx_j/diagx_j,
-// A_ik = sum_j GG_ij GG_kj / diagx_j (upper triangle).
+// 1/diagx kept), and the sums g_i(x), b_i = sum_j GG_ij delx_j/diagx_j,
+// A_ik = sum_j GG_ij GG_kj / diagx_j (upper triangle).  FP64 division is
+// costly on this GPU's narrow FP64 pipe, so each kernel forms the few
+// reciprocals it needs (1/(u-x), 1/(x-l), 1/(x-alpha), 1/(beta-x),
+// 1/diagx) once and multiplies: the reference's quotients to within an ulp.
 template <int M>
 __global__ void __launch_bounds__(NT) k_newton(Vecs V, Dual D, int64_t n, Red R) {
   constexpr int NS = 2 * M + M * (M + 1) / 2;
@@ -205,28 +251,30 @@ __global__ void __launch_bounds__(NT) k_newton(Vecs V, Dual D, int64_t n, Red R)
   for (int q = 0; q < NS; ++q) acc[q] = 0.0;
   for (int64_t j = blockIdx.x * (int64_t)NT + threadIdx.x; j < n; j += (int64_t)gridDim.x * NT) {
     const double x = V.x[j], al = V.alpha[j], be = V.beta[j];
-    const double ux = V.upp[j] - x, xl = x - V.low[j], ux2 = ux * ux, xl2 = xl * xl;
+    double rux, rxl, ral, rbe;
+    rcp4(V.upp[j] - x, x - V.low[j], x - al, be - x, rux, rxl, ral, rbe);
+    const double rux2 = rux * rux, rxl2 = rxl * rxl;
     double pl = V.p0[j], ql = V.q0[j], gg[M];
 #pragma unroll
     for (int i = 0; i < M; ++i) {
       const double p = V.P[i * n + j], q = V.Q[i * n + j];
       pl += p * D.lam[i];
       ql += q * D.lam[i];
-      acc[i] += p / ux + q / xl;
-      gg[i] = p / ux2 - q / xl2;
+      acc[i] += p * rux + q * rxl;
+      gg[i] = p * rux2 - q * rxl2;
     }
-    const double delx = pl / ux2 - ql / xl2 - D.epsi / (x - al) + D.epsi / (be - x);
-    double diagx = pl / (ux2 * ux) + ql / (xl2 * xl);
-    diagx = 2.0 * diagx + V.xsi[j] / (x - al) + V.eta[j] / (be - x);
-    const double t = delx / diagx;
+    const double delx = pl * rux2 - ql * rxl2 - D.epsi * ral + D.epsi * rbe;
+    double diagx = pl * (rux2 * rux) + ql * (rxl2 * rxl);
+    diagx = 2.0 * diagx + V.xsi[j] * ral + V.eta[j] * rbe;
+    const double rdg = rcp(diagx), t = delx * rdg;
     V.tdx[j] = t;
-    V.diagx[j] = diagx;
+    V.diagx[j] = rdg;  // kept as its reciprocal
     int q = 2 * M;
 #pragma unroll
     for (int i = 0; i < M; ++i) {
       acc[M + i] += gg[i] * t;
 #pragma unroll
-      for (int k = i; k < M; ++k) acc[q++] += gg[i] * (1.0 / diagx) * gg[k];
+      for (int k = i; k < M; ++k) acc[q++] += gg[i] * rdg * gg[k];
     }
   }
   reduce_out<NS>(acc, -INFINITY, R.part, R.ticket, R.out);
@@ -240,21 +288,23 @@ __global__ void __launch_bounds__(NT) k_dir(Vecs V, Dual D, int64_t n, Red R) {
   double mx = -INFINITY;
   for (int64_t j = blockIdx.x * (int64_t)NT + threadIdx.x; j < n; j += (int64_t)gridDim.x * NT) {
     const double x = V.x[j], al = V.alpha[j], be = V.beta[j], xsi = V.xsi[j], eta = V.eta[j];
-    const double ux = V.upp[j] - x, xl = x - V.low[j], ux2 = ux * ux, xl2 = xl * xl, diagx = V.diagx[j];
+    double rux, rxl, ral, rbe, rxs, ret;
+    rcp4(V.upp[j] - x, x - V.low[j], x - al, be - x, rux, rxl, ral, rbe);
+    rcp2(xsi, eta, rxs, ret);
+    const double rux2 = rux * rux, rxl2 = rxl * rxl, rdg = V.diagx[j];
     double gl = 0.0;
 #pragma unroll
-    for (int i = 0; i < M; ++i) gl += (V.P[i * n + j] / ux2 - V.Q[i * n + j] / xl2) * D.dlam[i];
-    const double dx = -V.tdx[j] - gl / diagx;
-    const double dxsi = -xsi + (D.epsi - dx * xsi) / (x - al);
-    const double deta = -eta + (D.epsi + dx * eta) / (be - x);
+    for (int i = 0; i < M; ++i) gl += (V.P[i * n + j] * rux2 - V.Q[i * n + j] * rxl2) * D.dlam[i];
+    const double dx = -V.tdx[j] - gl * rdg;
+    const double dxsi = -xsi + (D.epsi - dx * xsi) * ral;
+    const double deta = -eta + (D.epsi + dx * eta) * rbe;
     V.dx[j] = dx;
     V.dxsi[j] = dxsi;
     V.deta[j] = deta;
     V.x0[j] = x;
     V.xsi0[j] = xsi;
     V.eta0[j] = eta;
-    mx = fmax(mx, fmax(fmax(-C101 * dxsi / xsi, -C101 * deta / eta),
-                       fmax(-C101 * dx / (x - al), C101 * dx / (be - x))));
+    mx = fmax(mx, fmax(fmax(-C101 * dxsi * rxs, -C101 * deta * ret), fmax(-C101 * dx * ral, C101 * dx * rbe)));
   }
   reduce_out<1>(none, mx, R.part, R.ticket, R.out);
 }
@@ -333,7 +383,7 @@ struct ntg_mma {
   int max_iter = 100;
   double epsimin = 0.0, asyinit = 0.5, asyincr = 1.2, asydecr = 0.7;
   double residumax = 0.0, residunorm = 0.0;
-  long long newton_steps = 0;
+  long long newton_steps = 0, trials = 0, levels = 0;
   ntg::mm::Vecs V{};
   double* part = nullptr;
   unsigned* ticket = nullptr;
@@ -407,6 +457,7 @@ int subsolve(ntg_mma* o, double* designx) {
   double z = 1.0, zeta = 1.0;
   for (int i = 0; i < m; ++i) mu[i] = std::max(1.0, 0.5 * o->c[i]);
   while (epsi > mm::C09 * o->epsimin) {
+    ++o->levels;
     o->lam = lam;
     mm::k_resid<M, false><<<g, mm::NT, 0, st>>>(o->V, dual(o, epsi), n, red(o));
     NTG_COUNT_LAUNCH();
@@ -478,6 +529,7 @@ int subsolve(ntg_mma* o, double* designx) {
       int itto = 0;
       while (newres > residunorm && itto < 50) {
         ++itto;
+        ++o->trials;
         for (int i = 0; i < m; ++i) {
           y[i] = y0[i] + steg * dy[i];
           lam[i] = lam0[i] + steg * dlam[i];
@@ -667,10 +719,14 @@ int ntg_mma_kkt(ntg_mma* o, const double* x_d, const double* df0dx_d, const doub
   });
 }
 
-int ntg_mma_info(const ntg_mma* o, long long* newton_steps, double* residumax, double* residunorm) {
+int ntg_mma_info(const ntg_mma* o, long long* counts, double* residumax, double* residunorm) {
   clear_error();
   NTG_CHECK_ARG(o, "ntg_mma_info: null handle");
-  if (newton_steps) *newton_steps = o->newton_steps;
+  if (counts) {
+    counts[0] = o->newton_steps;
+    counts[1] = o->trials;
+    counts[2] = o->levels;
+  }
   if (residumax) *residumax = o->residumax;
   if (residunorm) *residunorm = o->residunorm;
   return NTG_OK;

@@ -80,3 +80,4 @@ def test_mma_rejects_bad_sizes(pkg, dev):
     x = torch.full((4,), 0.5, dtype=torch.float64, device=dev)
     with pytest.raises(pkg.NtgError):
         pkg.mma_t(x, 4, 5, 1.0, 0.0, 1000.0, 1.0, 0.0, 1.0)
+
