@@ -413,10 +413,50 @@ def run_terms(args, local):
                 rec["fp64_tflops"] = round(tf, 3)
                 rec["frac_of_fp64_roof"] = round(tf / FP64_TFLOPS, 3)
             out[name] = rec
+    if not args.no_cpu:
+        for name, ms_cpu in terms_cpu_baseline(n).items():
+            out[name]["cpu_ms"] = round(ms_cpu, 1)
+            out[name]["cpu_over_gpu"] = round(ms_cpu / out[name]["ms"], 1)
     return {"mode": "terms", "config": {"workload": args.config, "desc": cfg["desc"], "n_local_dofs": n,
                                          "l2": "inputs larger than L2"},
             "dtype": "f64", "steps": args.steps, "warmup": args.warmup, "terms": out,
+            "cpu_baseline": {"kind": "port", "cores": 1, "unit": "ms per application",
+                             "sample": "the numpy restatements (oracle/deriv_ref.py, pnpn_ref.py, dealias_ref.py) "
+                                       "on a 4x4x4, lx = 8 box (32,768 DOFs), one timed application each after one untimed, "
+                                       "scaled per DOF to the workload"},
             "clocks": sampler.summary()}
+
+
+def terms_cpu_baseline(n):
+    """Per-application time of each term in the numpy restatements on a
+    bounded sample (4^3 elements, lx = 8), scaled to n local DOFs."""
+    import numpy as np
+    from oracle import dealias_ref, deriv_ref, oracle as orc, pnpn_ref
+    m = orc.build_mesh(4, 4, 4, LX, amp=0.05, seed=MESH_SEED)
+    rng = np.random.default_rng(0)
+    F = lambda: rng.standard_normal(m.n)
+    u, ue, f = [F() for _ in range(3)], [F() for _ in range(3)], [F() for _ in range(3)]
+    p = F()
+    gs = lambda a: orc.gs_op(m, a)
+    face = np.nonzero(np.isclose(m.x, m.x.max()))[0]
+    surf = (face, np.stack([np.full(face.size, 1e-3), np.zeros(face.size), np.zeros(face.size)]))
+    fns = {
+        "vel_res": lambda: pnpn_ref.vel_res(m, u, p, f, 0.01, 1.0, 11 / 6, 1e-3),
+        "prs_res": lambda: pnpn_ref.prs_res(m, p, u, ue, f, 0.01, 1.0, 11 / 6, 1e-3, surf, None),
+        "adjoint_advection": lambda: deriv_ref.adjoint_advection(m, f, u, ue),
+        "linear_advection": lambda: deriv_ref.linear_advection(m, f, u, ue),
+        "adjoint_advection_dealias": lambda: dealias_ref.adjoint_advection(m, f, u, ue),
+        "linear_advection_dealias": lambda: dealias_ref.linear_advection(m, f, u, ue),
+        "min_dissipation": lambda: deriv_ref.min_dissipation_forcing(m, gs, f, u, 0.5),
+        "ax_helm_fp64": lambda: orc.ax_helm(m, p),
+    }
+    out = {}
+    for name, fn in fns.items():
+        fn()
+        t0 = time.perf_counter()
+        fn()
+        out[name] = (time.perf_counter() - t0) * 1e3 * n / m.n
+    return out
 
 
 def run_mma(args, local):
