@@ -482,6 +482,30 @@ int ntg_mma_kkt(ntg_mma* mma, const double* x_d, const double* df0dx_d, const do
 int ntg_mma_info(const ntg_mma* mma, long long* counts, double* residumax, double* residunorm);
 
 /* ---------------------------------------------------------------------- */
+/* field files (Nek5000 binary "#std" format, as Neko's fld_file_t writes  */
+/* them for fld_file_output_t; sources/topology_optimization/             */
+/* topopt_design.f90:283-286).  Host code; on_device = 1: the field        */
+/* pointers are device arrays, 0: host arrays.                             */
+/* ---------------------------------------------------------------------- */
+/* Write one file: header (wdsize 4 = float32 data, 8 = float64), element
+   numbers glb_el (host, 1-based; NULL = 1..nelv), then the fields given (a
+   NULL pointer leaves a field out; x, y, z and u, v, w come as triples;
+   nscal scalar fields s[0..nscal)) and the per-element min/max block. */
+int ntg_fld_write(const char* path, int lx, int64_t nelv, const int64_t* glb_el, double time, int tstep, int wdsize,
+                  int on_device, const double* x, const double* y, const double* z, const double* u,
+                  const double* v, const double* w, const double* p, const double* t, const double* const* s,
+                  int nscal);
+/* the "<name>.nek5000" index: filetemplate <name>%01d.f%05d, first step, count */
+int ntg_fld_write_index(const char* path, const char* name, int first, int count);
+/* header of a field file; rdcode receives the field codes (e.g. "XUPTS02") */
+int ntg_fld_info(const char* path, int* lx, int64_t* nelv, int* wdsize, double* time, int* tstep, char* rdcode,
+                 int cap);
+/* read the fields the file holds into the non-NULL arrays (n = nelv lx^3
+   each, element order as stored; element numbers to glb_el if given) */
+int ntg_fld_read(const char* path, int on_device, int64_t* glb_el, double* x, double* y, double* z, double* u,
+                 double* v, double* w, double* p, double* t, double* const* s, int nscal);
+
+/* ---------------------------------------------------------------------- */
 /* masked vector kernels of neko-top, same names and signatures as the     */
 /* reference's extern "C" wrappers (math_ext.cu:49-108): device arrays by  */
 /* value, sizes and scalars by pointer, 1-based masks, real = double.      */

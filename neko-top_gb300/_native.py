@@ -126,6 +126,10 @@ SIGNATURES = {
     "ntg_mma_update": (_i, [_vp, _i, _vp, _vp, _pd, _vp]),
     "ntg_mma_kkt": (_i, [_vp, _vp, _vp, _pd, _vp, _pd, _pd]),
     "ntg_mma_info": (_i, [_vp, C.POINTER(C.c_longlong), _pd, _pd]),
+    "ntg_fld_write": (_i, [C.c_char_p, _i, _i64, _vp, _d, _i, _i, _i] + [_vp] * 9 + [_i]),
+    "ntg_fld_write_index": (_i, [C.c_char_p, C.c_char_p, _i, _i]),
+    "ntg_fld_info": (_i, [C.c_char_p, _vp, _vp, _vp, _vp, _vp, C.c_char_p, _i]),
+    "ntg_fld_read": (_i, [C.c_char_p, _i, _vp] + [_vp] * 8 + [_vp, _i]),
     "ntg_dealias_create": (_i, [_vp, _vp, _i]),
     "ntg_dealias_destroy": (_i, [_vp]),
     "ntg_dealias_info": (_i, [_vp, _vp, _vp]),

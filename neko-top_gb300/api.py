@@ -962,6 +962,98 @@ class mma_t:
             pass
 
 
+class fld_file_t:
+    """Field files in the Nek5000 binary format, as Neko's fld_file_t writes
+    them for fld_file_output_t (sources/topology_optimization/
+    topopt_design.f90:283-286): write(fields, t, tstep) and read().  Fields
+    are CUDA tensors or numpy arrays of n = nelv lx^3 doubles, keyed x, y, z
+    (coordinates), u, v, w (velocity), p, t (temperature) and s (a list of
+    scalars).  precision "sp" writes float32 data (Neko's default), "dp"
+    float64."""
+
+    KEYS = ("x", "y", "z", "u", "v", "w", "p", "t")
+
+    def __init__(self, fname, precision="sp"):
+        if precision not in ("sp", "dp"):
+            raise ValueError("precision is 'sp' or 'dp'")
+        self.fname, self.wdsize = str(fname), 4 if precision == "sp" else 8
+
+    @staticmethod
+    def _arg(a):
+        import numpy as np
+        if a is None:
+            return None, None
+        if isinstance(a, torch.Tensor):
+            if a.dtype != torch.float64 or not a.is_contiguous():
+                raise TypeError("fields must be contiguous float64")
+            return C.c_void_p(a.data_ptr()), (1 if a.is_cuda else 0)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        return C.c_void_p(a.ctypes.data), 0
+
+    def write(self, fields, lx, nelv, t=0.0, tstep=0, glb_el=None):
+        import numpy as np
+        keep, ptrs, dev = [], [], set()
+        for k in self.KEYS:
+            a = fields.get(k)
+            if a is not None and not isinstance(a, torch.Tensor):
+                a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            pa, d = self._arg(a)
+            ptrs.append(pa)
+            if d is not None:
+                dev.add(d)
+        sc = [a if isinstance(a, torch.Tensor) else np.ascontiguousarray(a, dtype=np.float64)
+              for a in fields.get("s", [])]
+        sp = [self._arg(a) for a in sc]
+        dev.update(d for _, d in sp)
+        if len(dev) > 1:
+            raise ValueError("fields must be all on the device or all on the host")
+        sarr = (C.c_void_p * max(1, len(sp)))(*[p for p, _ in sp])
+        el = None
+        if glb_el is not None:
+            el = np.ascontiguousarray(glb_el, dtype=np.int64)
+        check(lib().ntg_fld_write(self.fname.encode(), int(lx), int(nelv),
+                                  None if el is None else C.c_void_p(el.ctypes.data), float(t), int(tstep),
+                                  self.wdsize, dev.pop() if dev else 0, *ptrs, sarr if sp else None, len(sp)))
+
+    @staticmethod
+    def write_index(path, name, first, count):
+        """The "<name>.nek5000" file that visualisation tools open."""
+        check(lib().ntg_fld_write_index(str(path).encode(), str(name).encode(), int(first), int(count)))
+
+    def info(self):
+        lx, ne, wd, st = C.c_int(), C.c_int64(), C.c_int(), C.c_int()
+        tm = C.c_double()
+        code = C.create_string_buffer(64)
+        check(lib().ntg_fld_info(self.fname.encode(), C.byref(lx), C.byref(ne), C.byref(wd), C.byref(tm),
+                                 C.byref(st), code, 64))
+        return {"lx": lx.value, "nelv": ne.value, "wdsize": wd.value, "time": tm.value, "tstep": st.value,
+                "rdcode": code.value.decode()}
+
+    def read(self, device=None):
+        """Dict of the fields the file holds (numpy arrays, or CUDA tensors on
+        `device`) plus "glb_el" and the header items."""
+        import numpy as np
+        h = self.info()
+        n = h["nelv"] * h["lx"] ** 3
+        code = h["rdcode"]
+        want = {"x": "X", "y": "X", "z": "X", "u": "U", "v": "U", "w": "U", "p": "P", "t": "T"}
+        mk = (lambda: torch.empty(n, dtype=torch.float64, device=device)) if device is not None else \
+            (lambda: np.empty(n))
+        out = {k: mk() for k, c in want.items() if c in code}
+        ns = int(code[code.index("S") + 1:code.index("S") + 3]) if "S" in code else 0
+        out["s"] = [mk() for _ in range(ns)]
+        el = np.empty(h["nelv"], dtype=np.int64)
+        ptr = lambda a: None if a is None else C.c_void_p(a.data_ptr() if isinstance(a, torch.Tensor)
+                                                           else a.ctypes.data)
+        sarr = (C.c_void_p * max(1, ns))(*[ptr(a) for a in out["s"]])
+        check(lib().ntg_fld_read(self.fname.encode(), 1 if device is not None else 0, C.c_void_p(el.ctypes.data),
+                                 *[ptr(out.get(k)) for k in self.KEYS], sarr if ns else None, ns))
+        out["glb_el"] = el
+        out.update(h)
+        return out
+
+
 # masked ops: the reference's cuda_* entry points (math_ext.cu:49-108)
 def _mi(mask):
     return C.byref(C.c_int(int(mask.numel())))
