@@ -9,7 +9,7 @@ from oracle import dealias_ref as dl
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(2, 2, 2, 8, 0.05), (3, 2, 1, 6, 0.04), (2, 1, 2, 5, 0.0)]
+SHAPES = [(2, 2, 2, 8, 0.05), (3, 2, 1, 6, 0.04), (2, 1, 2, 5, 0.0), (2, 2, 1, 7, 0.03), (3, 1, 1, 4, 0.05)]
 
 
 def T(a, dev):

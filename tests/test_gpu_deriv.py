@@ -10,7 +10,8 @@ from oracle import deriv_ref as dr
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(3, 2, 2, 8, 0.05), (2, 2, 3, 5, 0.04), (2, 3, 1, 4, 0.0), (2, 1, 2, 10, 0.03)]
+SHAPES = [(3, 2, 2, 8, 0.05), (2, 2, 3, 5, 0.04), (2, 3, 1, 4, 0.0), (2, 1, 2, 10, 0.03), (3, 3, 2, 2, 0.0),
+          (5, 3, 1, 3, 0.04)]
 
 
 def T(a, dev, dtype=torch.float64):

@@ -44,7 +44,8 @@ def surfaces(m, rng):
 
 
 @pytest.mark.parametrize("shape,props", [((3, 2, 2, 8, 0.05), "const"), ((2, 2, 3, 6, 0.04), "field"),
-                                         ((2, 3, 2, 5, 0.0), "field")])
+                                         ((2, 3, 2, 5, 0.0), "field"), ((2, 1, 1, 10, 0.03), "const"),
+                                         ((3, 2, 1, 3, 0.02), "field")])
 def test_vel_res_matches_oracle(pkg, orc, dev, shape, props):
     ex, ey, ez, lx, amp = shape
     m = orc.build_mesh(ex, ey, ez, lx, amp=amp, seed=3)
@@ -63,7 +64,7 @@ def test_vel_res_matches_oracle(pkg, orc, dev, shape, props):
 
 
 @pytest.mark.parametrize("shape,props,surf", [((3, 2, 2, 8, 0.05), "const", True), ((2, 2, 3, 6, 0.04), "field", True),
-                                              ((2, 3, 2, 5, 0.0), "const", False)])
+                                              ((2, 3, 2, 5, 0.0), "const", False), ((2, 1, 2, 10, 0.03), "field", True)])
 def test_prs_res_matches_oracle(pkg, orc, dev, shape, props, surf):
     ex, ey, ez, lx, amp = shape
     m = orc.build_mesh(ex, ey, ez, lx, amp=amp, seed=5)
