@@ -19,6 +19,7 @@ path, with the same names and argument meaning:
     adv_lin_dealias_t.compute_adjoint / compute_linear           (sources/adjoint/adv_adjoint_dealias.f90)
     adjoint_minimum_dissipation_source_term_t.compute            (sources/source_terms/adjoint_minimum_dissipation_source_term.f90)
     pnpn_prs_res_t / pnpn_vel_res_t .compute                     (prs_res / vel_res, sources/adjoint/adjoint_pnpn.f90:716-753)
+    pnpn_step_t.step                                             (the pressure + velocity solve sequence, :714-801)
     mma_t.update / KKT                                           (sources/mma/mma.f90, on the GPU)
     fld_file_t.write / read                                      (Nek5000 binary field files, fld_file_output_t)
 
@@ -37,7 +38,7 @@ from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, adjoint_minimum_d
                   col2_mask, col3_mask, conv1, curl, dudxyz, fld_file_t, glsc2_mask, glsc3, gs_t, invcol1_mask, jacobi_t, opgrad,
                   krylov_solver_factory, ksp_monitor_t, learned_guess_t, mask_face_xmax, mma_t, permeability,
                   pnpn_prs_res_t,
-                  pnpn_vel_res_t, projection_t, schwarz_t,
+                  pnpn_step_t, pnpn_vel_res_t, projection_t, schwarz_t,
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
 
 from . import dist  # noqa: E402  (element-partitioned solves across ranks)
@@ -50,5 +51,5 @@ __all__ = [
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
     "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t", "dist", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
-    "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "mma_t", "fld_file_t",
+    "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "pnpn_step_t", "mma_t", "fld_file_t",
 ]

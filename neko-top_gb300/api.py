@@ -748,6 +748,94 @@ def curl(w1, w2, w3, u1, u2, u3, coef: coef_t):
                          *[_f(coef, t, f"u{i}") for i, t in enumerate((u1, u2, u3))]))
 
 
+class pnpn_step_t:
+    """The solve sequence of one Pn/Pn step in the reference's order
+    (sources/adjoint/adjoint_pnpn.f90:714-801):
+
+      pressure  prs_res -> gs -> bc -> projection pre -> pc update + solve
+                (zero initial guess) -> projection post -> p += dp
+      velocity  vel_res -> gs (3 components) -> bc -> projection pre ->
+                coupled solve -> projection post -> u += du
+
+    Two coef_t of the same mesh carry the pressure operator (h1 = 1/rho, no
+    mass term, its Dirichlet mask) and the velocity operator (h1 = mu,
+    h2 = rho bd/dt, its Dirichlet mask, shared by the three components).
+    L = 0 switches the projections off; activ_step is the reference's
+    projection_hold_steps.  With projection each solve is held to rtol times
+    the norm of its unprojected right-hand side (an absolute tolerance, as
+    the reference's solvers use), and the velocity components are solved one
+    after another."""
+
+    def __init__(self, coef_p: coef_t, coef_v: coef_t, prs_solver="cg", vel_solver="cg", max_iter=800,
+                 rtol=1e-10, L=20, activ_step=5):
+        self.cp, self.cv = coef_p.metrics(), coef_v.metrics()
+        self.ksp_p = krylov_solver_factory(coef_p, prs_solver, max_iter, rtol)
+        self.ksp_v = krylov_solver_factory(coef_v, vel_solver, max_iter, rtol)
+        self.proj_p = projection_t(coef_p, L, activ_step) if L else None
+        self.proj_v = [projection_t(coef_v, L, activ_step) for _ in range(3)] if L else None
+        self.prs, self.vel = pnpn_prs_res_t(), pnpn_vel_res_t()
+        self.gs_p, self.gs_v = gs_t(coef_p), gs_t(coef_v)
+        self.rtol = float(rtol)
+        self.mult = coef_p.geometry()["mult"] if L else None
+        z = lambda: torch.zeros(coef_p.n, dtype=torch.float64, device=coef_p.device)
+        self.p_res, self.dp = z(), z()
+        self.res = [z() for _ in range(3)]
+        self.du = [z() for _ in range(3)]
+
+    @staticmethod
+    def _inv(v):
+        return 1.0 / v if isinstance(v, torch.Tensor) else 1.0 / float(v)
+
+    def step(self, u, v, w, p, ue, ve, we, fx, fy, fz, mu=1.0, rho=1.0, bd=1.0, dt=1.0, tstep=None,
+             prs_surface=None, sym_surface=None, base=1):
+        """Advances p and (u, v, w) in place; returns the pressure monitor
+        and the three velocity monitors."""
+        cp, cv = self.cp, self.cv
+        self.prs.compute(p, self.p_res, u, v, w, ue, ve, we, fx, fy, fz, cp, prs_surface, sym_surface, bd=bd,
+                         dt=dt, mu=mu, rho=rho, base=base)
+        self.gs_p.op(self.p_res)
+        bc_list_apply_scalar(cp, self.p_res)
+        h1p = self._inv(rho)
+        if isinstance(h1p, torch.Tensor):
+            cp.set_coefs(h1=h1p.contiguous(), ifh2=False)
+        else:
+            cp.set_coefs(h1c=h1p, ifh2=False)
+        if self.proj_p is not None:
+            # the projected system keeps the tolerance of the original
+            # right-hand side (the reference's absolute tolerance)
+            self.ksp_p.set_tol(0.0, self.rtol * glsc3(cp, self.p_res, self.p_res, self.mult) ** 0.5)
+            self.proj_p.pre_solving(self.p_res, tstep)
+        self.dp.zero_()
+        mon_p = self.ksp_p.solve(self.dp, self.p_res)
+        if self.proj_p is not None:
+            self.proj_p.post_solving(self.dp, tstep)
+        p.add_(self.dp)
+        self.vel.compute(u, v, w, *self.res, p, fx, fy, fz, cv, mu=mu, rho=rho, bd=bd, dt=dt)
+        for r in self.res:
+            self.gs_v.op(r)
+            bc_list_apply_scalar(cv, r)
+        h2v = (rho * (bd / dt)) if isinstance(rho, torch.Tensor) else torch.full_like(self.dp, float(rho) * bd / dt)
+        if isinstance(mu, torch.Tensor):
+            cv.set_coefs(h1=mu.contiguous(), h2=h2v.contiguous(), ifh2=True)
+        else:
+            cv.set_coefs(h1c=float(mu), h2=h2v.contiguous(), ifh2=True)
+        for d in self.du:
+            d.zero_()
+        if self.proj_v is None:
+            mons_v = self.ksp_v.solve_coupled(*self.du, *self.res)
+        else:
+            # per component, each to the tolerance of its unprojected RHS
+            mons_v = []
+            for pr, r, d in zip(self.proj_v, self.res, self.du):
+                self.ksp_v.set_tol(0.0, self.rtol * glsc3(cv, r, r, self.mult) ** 0.5)
+                pr.pre_solving(r, tstep)
+                mons_v.append(self.ksp_v.solve(d, r))
+                pr.post_solving(d, tstep)
+        for x, d in zip((u, v, w), self.du):
+            x.add_(d)
+        return mon_p, mons_v
+
+
 class adv_lin_no_dealias_t:
     """Adjoint and linearised advection without dealiasing
     (sources/adjoint/adv_adjoint_no_dealias.f90: adjoint_advection_no_dealias
