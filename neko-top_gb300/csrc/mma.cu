@@ -28,8 +28,6 @@ constexpr int LANES = 2 * MMAX + MMAX * (MMAX + 1) / 2 + 2;  // sums + 1 max
 // the reference's default-kind (single precision) literals
 constexpr double C001 = (double)0.01f, C01 = (double)0.1f, C09 = (double)0.9f, C101 = (double)1.01f;
 
-__device__ __forceinline__ double rcp(double a) { return 1.0 / a; }
-
 // 1/a and 1/b from one division (1/(ab) times the other factor): the FP64
 // pipe, not memory, bounds these kernels, and a division costs it about ten
 // FMAs.  Each result is within a few ulp of the quotient.
@@ -266,7 +264,7 @@ __global__ void __launch_bounds__(NT) k_newton(Vecs V, Dual D, int64_t n, Red R)
     const double delx = pl * rux2 - ql * rxl2 - D.epsi * ral + D.epsi * rbe;
     double diagx = pl * (rux2 * rux) + ql * (rxl2 * rxl);
     diagx = 2.0 * diagx + V.xsi[j] * ral + V.eta[j] * rbe;
-    const double rdg = rcp(diagx), t = delx * rdg;
+    const double rdg = 1.0 / diagx, t = delx * rdg;
     V.tdx[j] = t;
     V.diagx[j] = rdg;  // kept as its reciprocal
     int q = 2 * M;
