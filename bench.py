@@ -334,7 +334,7 @@ def run_sequence(args, local):
     }
 
 
-FP64_TFLOPS = 1.20  # FP64 FMA probe on this GPU (the roof of the FP64 element-tile kernels)
+FP64_TFLOPS = 1.2556  # FP64 FMA roof measured by `bench.py --fp64-peak` (ntg_probe_fp64) on GB300
 
 
 def run_terms(args, local):
@@ -659,7 +659,7 @@ def run_ours(args, ws, rank, local):
     fp64_peak = FP64_TFLOPS * 1e3
     roof64 = {"kernel": "k_ax_helm<double,8> (FP64 Ax, residual replacements)", "bound": "fp64",
               "achieved": round(116.0 * n / t_k64 / 1e9, 1), "peak": fp64_peak, "unit": "GFLOP/s",
-              "frac": round(116.0 * n / t_k64 / 1e9 / fp64_peak, 4), "peak_source": "own FP64 FMA-chain probe"}
+              "frac": round(116.0 * n / t_k64 / 1e9 / fp64_peak, 4), "peak_source": "FP64 FMA-chain probe, bench.py --fp64-peak"}
 
     # end to end through the public API: host RHS in, host solution out
     f_h = f.cpu().pin_memory()
@@ -847,6 +847,7 @@ def main(argv=None):
     p.add_argument("--fp64-warm", type=int, default=8, help="FP64 solves before the sample (fills projection)")
     p.add_argument("--proj-l", type=int, default=20, help="projection space size of --sequence (Neko's default 20)")
     p.add_argument("--mma", action="store_true", help="time MMA design updates on the workload's DOF count")
+    p.add_argument("--fp64-peak", action="store_true", help="measure the FP64 FMA roof (the FP64 denominator)")
     p.add_argument("--terms", action="store_true",
                    help="time the FP64 terms either side of each solve (residuals, advection, forcing)")
     p.add_argument("--seq-modes", default="zero,projection,learned,learned_only",
@@ -862,6 +863,22 @@ def main(argv=None):
         return 0
     if args.mma:
         print(json.dumps(run_mma(args, local)), flush=True)
+        return 0
+    if args.fp64_peak:
+        import ctypes as C
+        import torch
+        import __graft_entry__ as ge
+        torch.cuda.set_device(local)
+        pkg = ge.load_package()
+        vals = []
+        with ClockSampler(local) as clk:
+            for _ in range(max(args.steps, 3)):
+                tf = C.c_double()
+                if pkg.lib().ntg_probe_fp64(1 << 16, C.byref(tf), None) != 0:
+                    raise RuntimeError(pkg.lib().ntg_last_error().decode())
+                vals.append(tf.value)
+        print(json.dumps({"mode": "fp64_peak", "unit": "TFLOP/s", "runs": [round(v, 4) for v in vals],
+                          "median": round(statistics.median(vals), 4), "clocks": clk.summary()}), flush=True)
         return 0
     if args.impl == "reference":
         res = run_reference(args, ws, rank)
