@@ -135,7 +135,7 @@ def test_ramp_derivatives(orc):
             assert np.allclose(d * q, fd, rtol=1e-6)
         else:
             assert np.allclose(d, fd, rtol=1e-6)
-    # BASELINE chi(rho) = chimax (1-rho)/(1+q rho) is the convex-down map at 1-rho
+    # the Brinkman coefficient chi(rho) = chimax (1-rho)/(1+q rho) is the convex-down map at 1-rho
     rho = np.linspace(0, 1, 11)
     chi = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
     assert np.allclose(chi, 1e4 * (1 - rho) / (1 + 8 * rho))
