@@ -1,8 +1,12 @@
 /*
  * ntgb300.h - C ABI of the GB300-native spectral-element Helmholtz/Poisson
  * hot path (ax_helm, gather-scatter, Jacobi-PCG, residual projection,
- * mixed-precision flexible CG, learned initial guess, RAMP/Brinkman
- * coefficient kernels and the masked vector kernels of neko-top).
+ * mixed-precision CG and GMRES, overlapping Schwarz, learned initial guess,
+ * RAMP/Brinkman coefficient kernels and the masked vector kernels of
+ * neko-top) and of the steps either side of it: the derivative operators,
+ * the Pn/Pn residuals, the adjoint and linearised advection terms (with and
+ * without dealiasing), the minimum-dissipation forcing, the MMA optimiser
+ * and Nek5000 field files.
  *
  * Conventions (the same as the reference's own C ABI in
  * sources/neko_ext/math/bcknd/device/cuda/math_ext.cu:41-108 and its
