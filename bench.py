@@ -414,50 +414,57 @@ def run_terms(args, local):
                 rec["fp64_tflops"] = round(tf, 3)
                 rec["frac_of_fp64_roof"] = round(tf / FP64_TFLOPS, 3)
             out[name] = rec
+    cpu_threads = None
     if not args.no_cpu:
-        for name, ms_cpu in terms_cpu_baseline(n).items():
+        cpu, cpu_threads = terms_cpu_baseline(n)
+        for name, ms_cpu in cpu.items():
             out[name]["cpu_ms"] = round(ms_cpu, 1)
             out[name]["cpu_over_gpu"] = round(ms_cpu / out[name]["ms"], 1)
     return {"mode": "terms", "config": {"workload": args.config, "desc": cfg["desc"], "n_local_dofs": n,
                                          "l2": "inputs larger than L2"},
             "dtype": "f64", "steps": args.steps, "warmup": args.warmup, "terms": out,
-            "cpu_baseline": {"kind": "port", "cores": 1, "unit": "ms per application",
-                             "sample": "the numpy restatements (oracle/deriv_ref.py, pnpn_ref.py, dealias_ref.py) "
-                                       "on a 4x4x4, lx = 8 box (32,768 DOFs), one timed application each after one untimed, "
+            "cpu_baseline": {"kind": "port", "cores": cpu_threads, "unit": "ms per application",
+                             "sample": "the compiled OpenMP restatement (oracle/terms_oracle.c via oracle/terms_c.py, "
+                                       "checked against the numpy restatements) on a 6x6x6, lx = 8 box "
+                                       "(110,592 DOFs), two timed applications each after one untimed, "
                                        "scaled per DOF to the workload"},
             "clocks": sampler.summary()}
 
 
 def terms_cpu_baseline(n):
-    """Per-application time of each term in the numpy restatements on a
-    bounded sample (4^3 elements, lx = 8), scaled to n local DOFs."""
+    """Per-application time of each term in the compiled OpenMP restatement
+    (oracle/terms_oracle.c, all host threads) on a bounded sample (6^3
+    elements, lx = 8), scaled to n local DOFs."""
     import numpy as np
-    from oracle import dealias_ref, deriv_ref, oracle as orc, pnpn_ref
-    m = orc.build_mesh(4, 4, 4, LX, amp=0.05, seed=MESH_SEED)
+    from oracle import dealias_ref, oracle as orc
+    from oracle.terms_c import Terms
+    m = orc.build_mesh(6, 6, 6, LX, amp=0.05, seed=MESH_SEED)
+    t = Terms(m)
+    gl = dealias_ref.GL(m)
     rng = np.random.default_rng(0)
     F = lambda: rng.standard_normal(m.n)
     u, ue, f = [F() for _ in range(3)], [F() for _ in range(3)], [F() for _ in range(3)]
     p = F()
-    gs = lambda a: orc.gs_op(m, a)
     face = np.nonzero(np.isclose(m.x, m.x.max()))[0]
     surf = (face, np.stack([np.full(face.size, 1e-3), np.zeros(face.size), np.zeros(face.size)]))
     fns = {
-        "vel_res": lambda: pnpn_ref.vel_res(m, u, p, f, 0.01, 1.0, 11 / 6, 1e-3),
-        "prs_res": lambda: pnpn_ref.prs_res(m, p, u, ue, f, 0.01, 1.0, 11 / 6, 1e-3, surf, None),
-        "adjoint_advection": lambda: deriv_ref.adjoint_advection(m, f, u, ue),
-        "linear_advection": lambda: deriv_ref.linear_advection(m, f, u, ue),
-        "adjoint_advection_dealias": lambda: dealias_ref.adjoint_advection(m, f, u, ue),
-        "linear_advection_dealias": lambda: dealias_ref.linear_advection(m, f, u, ue),
-        "min_dissipation": lambda: deriv_ref.min_dissipation_forcing(m, gs, f, u, 0.5),
+        "vel_res": lambda: t.vel_res(u, p, f, 0.01, 1.0, 11 / 6, 1e-3),
+        "prs_res": lambda: t.prs_res(p, u, ue, f, 0.01, 1.0, 11 / 6, 1e-3, surf, None),
+        "adjoint_advection": lambda: t.advection(f, u, ue, "adjoint"),
+        "linear_advection": lambda: t.advection(f, u, ue, "linear"),
+        "adjoint_advection_dealias": lambda: t.advection(f, u, ue, "adjoint", gl),
+        "linear_advection_dealias": lambda: t.advection(f, u, ue, "linear", gl),
+        "min_dissipation": lambda: t.min_dissipation(f, u, 0.5),
         "ax_helm_fp64": lambda: orc.ax_helm(m, p),
     }
     out = {}
     for name, fn in fns.items():
         fn()
         t0 = time.perf_counter()
-        fn()
-        out[name] = (time.perf_counter() - t0) * 1e3 * n / m.n
-    return out
+        for _ in range(2):
+            fn()
+        out[name] = (time.perf_counter() - t0) / 2 * 1e3 * n / m.n
+    return out, orc.num_threads()
 
 
 def run_mma(args, local):
