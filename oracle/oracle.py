@@ -31,7 +31,7 @@ _D = C.c_double
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP)."""
-    srcs = [os.path.join(_HERE, f) for f in ("sem_oracle.c", "terms_oracle.c", "Makefile")]
+    srcs = [os.path.join(_HERE, f) for f in ("sem_oracle.c", "terms_oracle.c", "mma_oracle.c", "Makefile")]
     if force or not os.path.exists(_LIB_PATH) or any(os.path.getmtime(_LIB_PATH) < os.path.getmtime(f) for f in srcs):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
