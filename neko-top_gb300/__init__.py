@@ -22,6 +22,7 @@ path, with the same names and argument meaning:
     pnpn_step_t.step                                             (the pressure + velocity solve sequence, :714-801)
     mma_t.update / KKT                                           (sources/mma/mma.f90, on the GPU)
     fld_file_t.write / read                                      (Nek5000 binary field files, fld_file_output_t)
+    load_case, solver_from_case, build_solver                    (solver wiring from the case file, adjoint_scheme.f90:693-851)
 
 Field arguments are CUDA tensors (torch) laid out like Neko's x(lx,ly,lz,nelv):
 contiguous, i fastest.  Only their device pointers cross the boundary.  There
@@ -36,7 +37,8 @@ from ._native import (GS_OP_ADD, GS_OP_MAX, GS_OP_MIN, GS_OP_MUL, KSP_CG, KSP_CG
 from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, adjoint_minimum_dissipation_source_term_t,
                   adv_lin_dealias_t, adv_lin_no_dealias_t, ar1_modes, ax_helm_t, build_box, cadd_mask, cdtp, cmult_mask, coef_t,
                   col2_mask, col3_mask, conv1, curl, dudxyz, fld_file_t, glsc2_mask, glsc3, gs_t, invcol1_mask, jacobi_t, opgrad,
-                  krylov_solver_factory, ksp_monitor_t, learned_guess_t, mask_face_xmax, mma_t, permeability,
+                  build_solver, krylov_solver_factory, ksp_monitor_t, learned_guess_t, load_case, mask_face_xmax, mma_t,
+                  permeability, solver_config_t, solver_from_case,
                   pnpn_prs_res_t,
                   pnpn_step_t, pnpn_vel_res_t, projection_t, schwarz_t,
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
@@ -51,5 +53,6 @@ __all__ = [
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
     "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t", "dist", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
-    "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "pnpn_step_t", "mma_t", "fld_file_t",
+    "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "pnpn_step_t", "mma_t", "fld_file_t", "load_case", "solver_from_case",
+    "solver_config_t", "build_solver",
 ]

@@ -748,6 +748,120 @@ def curl(w1, w2, w3, u1, u2, u3, coef: coef_t):
                          *[_f(coef, t, f"u{i}") for i, t in enumerate((u1, u2, u3))]))
 
 
+@dataclass
+class solver_config_t:
+    """Solver wiring of one field as the reference reads it from the case
+    file (sources/adjoint/adjoint_scheme.f90:693-851): Krylov type,
+    preconditioner, absolute tolerance, iteration cap, projection space."""
+    field: str
+    ksp: str
+    pc: str
+    abstol: float
+    max_iter: int
+    projection_space_size: int
+    projection_hold_steps: int
+
+
+def load_case(text):
+    """Parse a Neko case file: JSON with // comments and trailing commas
+    (outside strings)."""
+    import json
+
+    def strip(src, drop):
+        out, i, n, in_str = [], 0, len(src), False
+        while i < n:
+            ch = src[i]
+            if in_str:
+                out.append(ch)
+                if ch == "\\" and i + 1 < n:
+                    out.append(src[i + 1])
+                    i += 1
+                elif ch == '"':
+                    in_str = False
+            elif ch == '"':
+                in_str = True
+                out.append(ch)
+            else:
+                k = drop(src, i)
+                if k > i:
+                    i = k
+                    continue
+                out.append(ch)
+            i += 1
+        return "".join(out)
+
+    def comment(src, i):  # "//" to the end of the line
+        if src.startswith("//", i):
+            j = src.find("\n", i)
+            return len(src) if j < 0 else j
+        return i
+
+    def trailing_comma(src, i):  # a comma before a closing bracket
+        if src[i] == ",":
+            j = i + 1
+            while j < len(src) and src[j] in " \t\r\n":
+                j += 1
+            if j < len(src) and src[j] in "}]":
+                return i + 1
+        return i
+
+    return json.loads(strip(strip(text, comment), trailing_comma))
+
+
+def solver_from_case(params, field="pressure"):
+    """The reference's lookup for the pressure or velocity solver: the key
+    under case.adjoint falls back to case.fluid; max_iterations defaults to
+    800, projection_space_size to 20 and projection_hold_steps to 5
+    (adjoint_scheme.f90:386-403, 693-851)."""
+    if field not in ("pressure", "velocity"):
+        raise ValueError("field is 'pressure' or 'velocity'")
+    case = params.get("case", params)
+
+    def get(key, default=None, required=False):
+        for section in ("adjoint", "fluid"):
+            v = case.get(section, {}).get(f"{field}_solver", {}).get(key)
+            if v is not None:
+                return v
+        if required:
+            raise KeyError(f"case.fluid.{field}_solver.{key} is required")
+        return default
+
+    def numerics(key, default):
+        for section in ("adjoint", "fluid"):
+            v = case.get(section, {}).get(key)
+            if v is not None:
+                return v
+        return default
+
+    return solver_config_t(field, str(get("type", required=True)), str(get("preconditioner", required=True)),
+                           float(get("absolute_tolerance", required=True)), int(get("max_iterations", 800)),
+                           int(get("projection_space_size", numerics("projection_space_size", 20))),
+                           int(get("projection_hold_steps", numerics("projection_hold_steps", 5))))
+
+
+_KSP_FAST = {"cg": "cg_mixed", "gmres": "gmres_mixed"}
+
+
+def build_solver(coef: coef_t, cfg: solver_config_t, fast=True):
+    """Krylov solver and preconditioner for a case's solver entry.  fast:
+    the FP32-inner variants ("cg" -> cg_mixed, "gmres" -> gmres_mixed) at the
+    same absolute tolerance; "hsmg" maps to the two-level Schwarz, "jacobi"
+    to Jacobi.  Returns (ksp, projection or None)."""
+    if cfg.ksp not in ("cg", "gmres"):
+        raise ValueError(f"solver type {cfg.ksp!r} is not built (cg, gmres)")
+    if cfg.pc not in ("jacobi", "hsmg"):
+        raise ValueError(f"preconditioner {cfg.pc!r} is not built (jacobi, hsmg)")
+    kind = _KSP_FAST[cfg.ksp] if fast else cfg.ksp
+    ksp = krylov_solver_factory(coef, kind, cfg.max_iter, 0.0, cfg.abstol)
+    if cfg.pc == "hsmg":
+        ksp.set_schwarz(schwarz_t(coef, coarse=True))
+        if kind == "cg_mixed":
+            ksp.set_inner(1e-3, 1)  # reliable-update spacing measured for the two-level Schwarz
+    proj = projection_t(coef, cfg.projection_space_size, cfg.projection_hold_steps) \
+        if cfg.projection_space_size > 0 else None
+    return ksp, proj
+
+
 class pnpn_step_t:
     """The solve sequence of one Pn/Pn step in the reference's order
     (sources/adjoint/adjoint_pnpn.f90:714-801):
