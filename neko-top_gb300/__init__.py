@@ -4,7 +4,7 @@ Python host side over the C ABI (include/ntgb300.h) of ``lib/libntgb300.so``.
 The classes mirror the Neko/neko-top interfaces the reference drives on this
 path, with the same names and argument meaning:
 
-    coef_t / dofmap      mesh, geometric factors, mult, gs maps   (Neko coef_t, gs_t%init)
+    coef_t / dofmap      mesh, geometric factors, mult, gs maps   (Neko coef_t, gs_t%init, dofmap_t)
     gs_t.op              direct stiffness summation              (gs_t%op(u, n, GS_OP_ADD))
     ax_helm_t.compute    w = h1 K u + h2 B u                     (ax_helm)
     jacobi_t             update / solve                          (pc_t, jacobi)
@@ -44,6 +44,7 @@ from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, adjoint_minimum_d
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
 
 from . import dist  # noqa: E402  (element-partitioned solves across ranks)
+from . import dofmap  # noqa: E402  (global node ids from element-vertex connectivity)
 
 __all__ = [
     "GS_OP_ADD", "GS_OP_MUL", "GS_OP_MIN", "GS_OP_MAX", "KSP_CG", "KSP_CG_MIXED", "KSP_FCG_MIXED", "KSP_GMRES",
@@ -52,7 +53,7 @@ __all__ = [
     "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
-    "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t", "dist", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
+    "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t", "dist", "dofmap", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
     "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "pnpn_step_t", "mma_t", "fld_file_t", "load_case", "solver_from_case",
     "solver_config_t", "build_solver",
 ]

@@ -98,6 +98,20 @@ class coef_t:
         self._metrics = False
 
     @classmethod
+    def from_vertices(cls, ev, lx, x, y, z):
+        """A plan for a general hexahedral mesh: ev (E x 8 numpy, global
+        vertex ids in tensor corner order) numbers the GLL nodes
+        (dofmap.dofmap_from_vertices); x, y, z are the node coordinates
+        (CUDA tensors, Neko layout)."""
+        import numpy as np
+        from .dofmap import dofmap_from_vertices
+        ev = np.asarray(ev)
+        gid = torch.from_numpy(dofmap_from_vertices(ev, lx)).to(x.device)
+        c = cls(ev.shape[0], lx, x, y, z, gid)
+        c.x, c.y, c.z, c.gid = x, y, z, gid
+        return c
+
+    @classmethod
     def box(cls, ex, ey, ez, lx=8, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.0, seed=0, device="cuda"):
         x, y, z, gid = build_box(ex, ey, ez, lx, lo, hi, amp, seed, device)
         c = cls(ex * ey * ez, lx, x, y, z, gid)
