@@ -15,6 +15,8 @@ CUDA tensors, gloo for CPU tensors).
                   shared face sorted on both sides (the buffers line up
                   without sending index lists), one representative local
                   copy per global node to send, every local copy to update
+  GeneralInterface  the same for any element partition (shared ids found by
+                  one all-gather of the ranks' sorted unique ids)
   DistPCG         Jacobi-PCG in FP64 on the distributed operator, every dot
                   weighted by the global multiplicity
 
@@ -100,6 +102,68 @@ class Interface:
             q.wait()
         for (nb, idx, slot, rep, _), r in zip(self.faces, recvs):
             u[idx] = u[idx] + r[slot]
+        return u
+
+
+class GeneralInterface:
+    """Exchange plan for any element partition (the elements a rank owns need
+    not be contiguous or slab-shaped; meshes numbered by dofmap.py).  The
+    ranks all-gather their sorted unique global ids once; the ids a rank
+    shares with rank q are the sorted intersection, the same list on both
+    sides, so the exchange buffers line up without index lists.
+    exchange_add sums the partials of a node's owners in ascending rank
+    order on every owner, so all copies stay bit-identical whatever the
+    number of owners.  Same interface as Interface."""
+
+    def __init__(self, gid: torch.Tensor):
+        world, rank = dist.get_world_size(), dist.get_rank()
+        dev = gid.device
+        uniq, inv = torch.unique(gid, sorted=True, return_inverse=True)
+        size = torch.tensor([uniq.numel()], dtype=torch.int64, device=dev)
+        sizes = [torch.zeros_like(size) for _ in range(world)]
+        dist.all_gather(sizes, size)
+        cap = int(max(int(s.item()) for s in sizes))
+        pad = torch.full((cap,), -1, dtype=torch.int64, device=dev)
+        pad[: uniq.numel()] = uniq
+        allg = [torch.empty_like(pad) for _ in range(world)]
+        dist.all_gather(allg, pad)
+        self.rank, self.faces = rank, []
+        for q in range(world):
+            if q == rank:
+                continue
+            other = allg[q][: int(sizes[q].item())]
+            shared = uniq[torch.isin(uniq, other)]  # sorted, identical on both sides
+            if shared.numel() == 0:
+                continue
+            on = torch.isin(gid, shared)
+            idx = torch.nonzero(on).squeeze(1)
+            slot = torch.searchsorted(shared, gid[idx])
+            rep = torch.full((shared.numel(),), torch.iinfo(torch.int64).max, dtype=torch.int64, device=dev)
+            rep = rep.scatter_reduce(0, slot, idx, reduce="amin")
+            self.faces.append((q, idx, slot, rep, shared))
+
+    def exchange_add(self, u: torch.Tensor):
+        if not self.faces:
+            return u
+        recvs, reqs = [], []
+        for q, idx, slot, rep, _ in self.faces:
+            s = u[rep].contiguous()
+            r = torch.empty_like(s)
+            reqs.append(dist.isend(s, q))
+            reqs.append(dist.irecv(r, q))
+            recvs.append((s, r))
+        for rq in reqs:
+            rq.wait()
+        tot = torch.zeros_like(u)
+        own = False
+        for (q, idx, slot, rep, _), (_, r) in sorted(zip(self.faces, recvs), key=lambda t: t[0][0]):
+            if not own and q > self.rank:
+                tot += u
+                own = True
+            tot[idx] += r[slot]
+        if not own:
+            tot += u
+        u.copy_(tot)
         return u
 
 

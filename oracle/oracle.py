@@ -190,12 +190,21 @@ def mesh_slice(m: Mesh, e0: int, e1: int) -> Mesh:
     ids sliced, geometry and rank-local gather-scatter maps rebuilt): one
     rank's part of an element partition.  ex/ey/ez keep the box's x and y
     counts with ez = the slab's planes, so nelv = e1 - e0 for z-slabs."""
+    return mesh_subset(m, np.arange(e0, e1), (m.ex, m.ey, (e1 - e0) // (m.ex * m.ey)))
+
+
+def mesh_subset(m: Mesh, elems, dims=None) -> Mesh:
+    """The oracle Mesh of the elements `elems` of `m` (any subset, in the
+    given order): one rank's part of a general element partition.  `dims`
+    (ex, ey, ez) with ex ey ez = len(elems) labels it; default (len, 1, 1)."""
     lx = m.lx
     nl = lx ** 3
-    planes = (e1 - e0) // (m.ex * m.ey)
-    s = Mesh(m.ex, m.ey, planes, lx, m.lo, m.hi, m.amp, m.seed)
-    s.x, s.y, s.z = (np.ascontiguousarray(a[e0 * nl:e1 * nl]) for a in (m.x, m.y, m.z))
-    s.gid = np.ascontiguousarray(m.gid[e0 * nl:e1 * nl])
+    elems = np.asarray(elems, dtype=np.int64)
+    ex, ey, ez = dims if dims is not None else (len(elems), 1, 1)
+    s = Mesh(ex, ey, ez, lx, m.lo, m.hi, m.amp, m.seed)
+    sel = (elems[:, None] * nl + np.arange(nl)[None, :]).ravel()
+    s.x, s.y, s.z = (np.ascontiguousarray(a[sel]) for a in (m.x, m.y, m.z))
+    s.gid = np.ascontiguousarray(m.gid[sel])
     s.w, s.D = m.w, m.D
     n = s.n
     G = {k: np.zeros(n) for k in ("g11", "g12", "g13", "g22", "g23", "g33")}

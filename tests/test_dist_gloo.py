@@ -110,3 +110,68 @@ def test_distributed_pcg_matches_single_rank(orc, tmp_path, world):
     assert len(its) == 1 and abs(its.pop() - it_ref) <= 2
     assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
     assert all(float(p["r1"]) <= 1e-10 * float(p["fn"]) * (1 + 1e-9) for p in parts)
+
+
+def _worker_general(rank, world, port, outdir):
+    """A random (non-contiguous) element partition with the GeneralInterface."""
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import sys
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as orc
+    torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        D = _dist_module()
+        ex, ey, ez, lx = SHAPE
+        m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=11)
+        mask = orc.mask_face_xmax(ex, ey, ez, lx)
+        owner = np.random.default_rng(99).integers(0, world, m.nelv)
+        elems = np.nonzero(owner == rank)[0]
+        ms = orc.mesh_subset(m, elems)
+        nl = lx ** 3
+        sel = (elems[:, None] * nl + np.arange(nl)[None, :]).ravel()
+        pos = np.full(m.n, -1)
+        pos[sel] = np.arange(sel.size)
+        mloc = (pos[mask - 1][pos[mask - 1] >= 0] + 1).astype(np.int32)
+        ops = OracleOps(orc, ms, mloc)
+        iface = D.GeneralInterface(ops.gid)
+        rng = np.random.default_rng(5)
+        u = rng.standard_normal(m.n)
+        v = torch.from_numpy(u[sel].copy())
+        ops.gs(v)
+        iface.exchange_add(v)
+        pcg = D.DistPCG(ops, iface, rtol=1e-10, max_iter=5000)
+        k, a, ph = orc.fourier_params(11, 8)
+        f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+        x = torch.zeros(ms.n, dtype=torch.float64)
+        it, r0, r1, fn = pcg.solve(x, torch.from_numpy(f[sel].copy()))
+        np.savez(os.path.join(outdir, f"grank{rank}.npz"), gs=v.numpy(), mult=pcg.mult.numpy(), x=x.numpy(),
+                 it=it, sel=sel, gid=ms.gid)
+    finally:
+        torch.distributed.destroy_process_group()
+
+
+def test_general_partition_matches_single_rank(orc, tmp_path):
+    world = 3
+    mp.spawn(_worker_general, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    ex, ey, ez, lx = SHAPE
+    m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=11)
+    mask = orc.mask_face_xmax(ex, ey, ez, lx)
+    u = np.random.default_rng(5).standard_normal(m.n)
+    gs_ref = orc.gs_op(m, u)
+    k, a, ph = orc.fourier_params(11, 8)
+    f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+    x_ref, it_ref, _, _ = orc.cg(m, f, mask=mask, rtol=1e-10, max_iter=5000)
+    parts = [dict(np.load(os.path.join(tmp_path, f"grank{r}.npz"))) for r in range(world)]
+    gs, mult, x = np.zeros(m.n), np.zeros(m.n), np.zeros(m.n)
+    for p in parts:
+        gs[p["sel"]], mult[p["sel"]], x[p["sel"]] = p["gs"], p["mult"], p["x"]
+    assert np.allclose(gs, gs_ref, rtol=1e-13, atol=1e-13 * np.abs(gs_ref).max())
+    assert np.array_equal(mult, m.mult)
+    # every copy of a node, on every rank, holds the same bits
+    for g in np.unique(m.gid)[:: max(1, len(np.unique(m.gid)) // 2000)]:
+        vals = np.concatenate([p["gs"][p["gid"] == g] for p in parts])
+        assert vals.min() == vals.max()
+    its = {int(p["it"]) for p in parts}
+    assert len(its) == 1 and abs(its.pop() - it_ref) <= 2
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
