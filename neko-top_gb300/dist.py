@@ -17,6 +17,7 @@ CUDA tensors, gloo for CPU tensors).
                   copy per global node to send, every local copy to update
   GeneralInterface  the same for any element partition (shared ids found by
                   one all-gather of the ranks' sorted unique ids)
+  rcb_partition   balanced recursive coordinate bisection of the elements
   DistPCG         Jacobi-PCG in FP64 on the distributed operator, every dot
                   weighted by the global multiplicity
 
@@ -103,6 +104,31 @@ class Interface:
         for (nb, idx, slot, rep, _), r in zip(self.faces, recvs):
             u[idx] = u[idx] + r[slot]
         return u
+
+
+def rcb_partition(centroids, world):
+    """Recursive coordinate bisection of elements (centroids: E x 3 numpy)
+    into `world` parts of sizes differing by at most one: split along the
+    longest extent at the weighted median, recursing with the rank counts
+    floor(w/2) and ceil(w/2).  Returns the owner rank of each element."""
+    import numpy as np
+    c = np.asarray(centroids, dtype=np.float64)
+    owner = np.empty(c.shape[0], dtype=np.int64)
+
+    def split(ids, r0, w):
+        if w == 1:
+            owner[ids] = r0
+            return
+        wl = w // 2
+        pts = c[ids]
+        d = int(np.argmax(pts.max(0) - pts.min(0))) if len(ids) else 0
+        order = ids[np.argsort(pts[:, d], kind="stable")]
+        cut = (len(ids) * wl) // w
+        split(order[:cut], r0, wl)
+        split(order[cut:], r0 + wl, w - wl)
+
+    split(np.arange(c.shape[0]), 0, int(world))
+    return owner
 
 
 class GeneralInterface:

@@ -175,3 +175,16 @@ def test_general_partition_matches_single_rank(orc, tmp_path):
     its = {int(p["it"]) for p in parts}
     assert len(its) == 1 and abs(its.pop() - it_ref) <= 2
     assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+
+
+def test_rcb_partition_is_balanced_and_compact(orc):
+    D = _dist_module()
+    m = orc.build_mesh(6, 5, 4, 3, amp=0.05, seed=1)
+    cen = np.stack([a.reshape(m.nelv, -1).mean(1) for a in (m.x, m.y, m.z)], 1)
+    for world in (1, 2, 3, 5, 8):
+        owner = D.rcb_partition(cen, world)
+        counts = np.bincount(owner, minlength=world)
+        assert counts.sum() == m.nelv and counts.max() - counts.min() <= 1
+    # two parts of a 6x5x4 box: a cut across x (the longest extent)
+    owner = D.rcb_partition(cen, 2)
+    assert set(np.unique(owner[cen[:, 0] < 0.45])) == {0} and set(np.unique(owner[cen[:, 0] > 0.55])) == {1}
