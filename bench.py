@@ -335,7 +335,7 @@ def run_sequence(args, local):
     }
 
 
-FP64_TFLOPS = 1.2556  # FP64 FMA roof measured by `bench.py --fp64-peak` (ntg_probe_fp64) on GB300
+FP64_TFLOPS = 1.2556  # FP64 FMA roof measured by `bench.py --fp64-peak` (the probe library libntgb300_probe.so) on GB300
 
 
 def run_terms(args, local):
@@ -888,12 +888,16 @@ def main(argv=None):
         import __graft_entry__ as ge
         torch.cuda.set_device(local)
         pkg = ge.load_package()
+        probe = C.CDLL(os.path.join(ROOT, "neko-top_gb300", "lib", "libntgb300_probe.so"))
+        probe.ntgprobe_fp64.restype = C.c_int
+        probe.ntgprobe_fp64.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_void_p]
         vals = []
         with ClockSampler(local) as clk:
             for _ in range(max(args.steps, 3)):
                 tf = C.c_double()
-                if pkg.lib().ntg_probe_fp64(1 << 16, C.byref(tf), None) != 0:
-                    raise RuntimeError(pkg.lib().ntg_last_error().decode())
+                st = probe.ntgprobe_fp64(1 << 16, C.byref(tf), None)
+                if st != 0:
+                    raise RuntimeError(f"FP64 probe failed ({st})")
                 vals.append(tf.value)
         print(json.dumps({"mode": "fp64_peak", "unit": "TFLOP/s", "runs": [round(v, 4) for v in vals],
                           "median": round(statistics.median(vals), 4), "clocks": clk.summary()}), flush=True)

@@ -114,10 +114,6 @@ unsigned long long ntg_launch_count(void);
 int ntg_timer_enable(int on);
 int ntg_timer_read(int id, double* total_ms, long long* count);
 int ntg_timer_reset(void);
-/* FP64 FMA throughput of this GPU in TFLOP/s (8 independent FMA chains per
-   thread, 8 x 256-thread blocks per SM, `iters` FMAs per chain, CUDA-event
-   timed): the roof the FP64-bound kernels are reported against */
-int ntg_probe_fp64(int iters, double* tflops, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* mesh / coef_t / gs_t plan                                               */

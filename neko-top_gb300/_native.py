@@ -123,7 +123,6 @@ SIGNATURES = {
     "ntg_pnpn_vel_res": (_i, [_vp] * 12 + [_d, _vp, _d, _d, _d]),
     "ntg_mma_create": (_i, [_vp, _i64, _i, _vp, _d, _pd, _pd, _pd, _vp, _vp, _i, _d, _d, _d, _d, _vp]),
     "ntg_mma_destroy": (_i, [_vp]),
-    "ntg_probe_fp64": (_i, [_i, _pd, _vp]),
     "ntg_mma_update": (_i, [_vp, _i, _vp, _vp, _pd, _vp]),
     "ntg_mma_kkt": (_i, [_vp, _vp, _vp, _pd, _vp, _pd, _pd]),
     "ntg_mma_info": (_i, [_vp, C.POINTER(C.c_longlong), _pd, _pd]),

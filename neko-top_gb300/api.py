@@ -840,17 +840,12 @@ def solver_from_case(params, field="pressure"):
             raise KeyError(f"case.fluid.{field}_solver.{key} is required")
         return default
 
-    def numerics(key, default):
-        for section in ("adjoint", "fluid"):
-            v = case.get(section, {}).get(key)
-            if v is not None:
-                return v
-        return default
-
+    # the projection keys are read only under <field>_solver, as the
+    # reference does (adjoint_scheme.f90:384-403); a key placed directly
+    # under case.adjoint or case.fluid is ignored
     return solver_config_t(field, str(get("type", required=True)), str(get("preconditioner", required=True)),
                            float(get("absolute_tolerance", required=True)), int(get("max_iterations", 800)),
-                           int(get("projection_space_size", numerics("projection_space_size", 20))),
-                           int(get("projection_hold_steps", numerics("projection_hold_steps", 5))))
+                           int(get("projection_space_size", 20)), int(get("projection_hold_steps", 5)))
 
 
 _KSP_FAST = {"cg": "cg_mixed", "gmres": "gmres_mixed"}

@@ -2,7 +2,10 @@
 // ax_helm, the derivative and dealiasing kernels, the MMA) are reported
 // against.  Eight independent FMA chains per thread, grid = 8 blocks of 256
 // threads per SM, timed with CUDA events on the given stream.
-#include "common.cuh"
+//
+// A measurement tool, not part of the drop-in: it is built into its own
+// library (lib/libntgb300_probe.so) that only bench.py --fp64-peak loads.
+#include <cuda_runtime.h>
 
 namespace {
 
@@ -22,13 +25,18 @@ __global__ void __launch_bounds__(256) k_fp64_fma(double* __restrict__ out, int 
 
 }  // namespace
 
-extern "C" int ntg_probe_fp64(int iters, double* tflops, void* stream) {
-  ntg::clear_error();
-  NTG_CHECK_ARG(iters > 0 && iters <= (1 << 24) && tflops, "ntg_probe_fp64: bad argument");
+// Returns 0 and the FMA rate in TFLOP/s (an FMA counts 2), or a CUDA error
+// code.
+extern "C" __attribute__((visibility("default"))) int ntgprobe_fp64(int iters, double* tflops, void* stream) {
+  if (iters <= 0 || iters > (1 << 24) || !tflops) return -1;
   cudaStream_t s = (cudaStream_t)stream;
-  const int blocks = ntg::num_sms() * 8, threads = 256;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) return -2;
+  const int blocks = sms * 8, threads = 256;
   double* out = nullptr;
-  NTG_TRY(ntg::dev_alloc(&out, (size_t)blocks * threads));
+  cudaError_t err = cudaMalloc(&out, sizeof(double) * blocks * threads);
+  if (err != cudaSuccess) return (int)err;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -36,18 +44,13 @@ extern "C" int ntg_probe_fp64(int iters, double* tflops, void* stream) {
   cudaEventRecord(e0, s);
   k_fp64_fma<<<blocks, threads, 0, s>>>(out, iters, 0.999999, 1e-7);
   cudaEventRecord(e1, s);
-  NTG_COUNT_LAUNCH();
-  NTG_COUNT_LAUNCH();
-  const cudaError_t err = cudaEventSynchronize(e1);
+  err = cudaEventSynchronize(e1);
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  ntg::dev_free(out);
-  if (err != cudaSuccess) {
-    ntg::set_error("ntg_probe_fp64: %s", cudaGetErrorString(err));
-    return NTG_ERR_CUDA;
-  }
+  cudaFree(out);
+  if (err != cudaSuccess) return (int)err;
   *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
-  return NTG_OK;
+  return 0;
 }

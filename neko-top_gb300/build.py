@@ -19,6 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libntgb300.so")
+PROBE_SRC = os.path.join(HERE, "bench_probe", "fp64_probe.cu")
+PROBE_LIB = os.path.join(LIB_DIR, "libntgb300_probe.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -72,6 +74,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if jobs or force or _stale(LIB, objs):
         link = [nvcc] + ARCH + ["-shared", "-o", LIB] + objs
         run(link)
+    # the FP64 roof probe: a measurement tool for bench.py, outside the ABI
+    if force or _stale(PROBE_LIB, [PROBE_SRC]):
+        run([nvcc] + ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PROBE_SRC, "-o", PROBE_LIB])
     return LIB
 
 

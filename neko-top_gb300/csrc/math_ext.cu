@@ -8,6 +8,8 @@
 // multiple of the SM count, 64-bit indices, no atomics.
 #include <cmath>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "reduce.cuh"
 
@@ -128,18 +130,44 @@ __global__ void k_sens_md(double* __restrict__ s, const double* __restrict__ u, 
   }
 }
 
-// One scratch block for the standalone masked dot (device partials +
-// scalars), allocated on first use per process.
-static double* g_part = nullptr;
-static Scalars* g_scal = nullptr;
-static double* g_host = nullptr;
+// Scratch of the standalone masked dot (device partials + scalars + a
+// pinned result slot), allocated on the first call made with each device
+// current and kept per device ordinal until the process exits; a mutex
+// serialises the first calls of concurrent host threads.
+struct GlscScratch {
+  double* part = nullptr;
+  Scalars* scal = nullptr;
+  double* host = nullptr;
+};
+static std::mutex g_glsc_mu;
+static GlscScratch g_glsc[64];
 
-static int ensure_glsc_scratch() {
-  if (g_part) return NTG_OK;
-  NTG_TRY(dev_alloc(&g_part, (size_t)kRedSlots * kRedLanes));
-  NTG_TRY(dev_alloc(&g_scal, 1));
-  NTG_CUDA_TRY(cudaMemset(g_scal, 0, sizeof(Scalars)));
-  NTG_CUDA_TRY(cudaMallocHost(&g_host, sizeof(double)));
+static int glsc_scratch(GlscScratch** out) {
+  int dev = 0;
+  NTG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("cuda_glsc2_mask: device ordinal %d out of range", dev);
+    return NTG_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(g_glsc_mu);
+  GlscScratch& g = g_glsc[dev];
+  if (!g.host) {
+    GlscScratch t;
+    int st = NTG_OK;
+    do {
+      if ((st = dev_alloc(&t.part, (size_t)kRedSlots * kRedLanes))) break;
+      if ((st = dev_alloc(&t.scal, 1))) break;
+      if (cudaMemset(t.scal, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; set_error("cuda_glsc2_mask: memset"); break; }
+      if (cudaMallocHost(&t.host, sizeof(double)) != cudaSuccess) { st = NTG_ERR_ALLOC; set_error("cuda_glsc2_mask: pinned slot"); t.host = nullptr; break; }
+    } while (0);
+    if (st) {
+      dev_free(t.part);
+      dev_free(t.scal);
+      return st;
+    }
+    g = t;
+  }
+  *out = &g;
   return NTG_OK;
 }
 
@@ -206,16 +234,17 @@ double cuda_glsc2_mask(void* a, void* b, int* size, int* mask, int* mask_size) {
   clear_error();
   (void)size;
   if (*mask_size <= 0) return 0.0;
-  if (ensure_glsc_scratch() != NTG_OK) return NAN;
+  GlscScratch* g = nullptr;
+  if (glsc_scratch(&g) != NTG_OK) return NAN;
   { k_glsc2_mask<<<grid1(*mask_size), 256, 0, g_glb_queue>>>((const double*)a, (const double*)b, mask, *mask_size,
-                                                           g_part, g_scal); NTG_COUNT_LAUNCH(); }
+                                                           g->part, g->scal); NTG_COUNT_LAUNCH(); }
   report_launch("cuda_glsc2_mask");
-  cudaMemcpyAsync(g_host, &g_scal->red[0], sizeof(double), cudaMemcpyDeviceToHost, g_glb_queue);
+  cudaMemcpyAsync(g->host, &g->scal->red[0], sizeof(double), cudaMemcpyDeviceToHost, g_glb_queue);
   if (cudaStreamSynchronize(g_glb_queue) != cudaSuccess) {
     set_error("cuda_glsc2_mask: %s", cudaGetErrorString(cudaGetLastError()));
     return NAN;
   }
-  return *g_host;
+  return *g->host;
 }
 
 int ntg_ramp_forward(double* xout_d, const double* xin_d, int64_t n, double fmin, double fmax, double q,

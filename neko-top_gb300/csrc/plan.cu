@@ -81,19 +81,31 @@ static void timer_resolve() {
   g_tm.pending.clear();
 }
 
+// SM count of the current device, looked up once per device ordinal.
 int num_sms() {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+  if (dev >= 64) {
+    int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    return sms;
+  }
+  int sms = cache[dev].load(std::memory_order_relaxed);
+  if (sms <= 0) {
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 152;
+    cache[dev].store(sms, std::memory_order_relaxed);
   }
   return sms;
 }
 
+// Grid for a grid-stride loop over `work` items: 16 blocks per SM at most,
+// and never more than kRedSlots blocks, since the reducing kernels write one
+// partial per block into kRedSlots slots per lane.
 int grid_for(int64_t work, int threads) {
   int64_t g = (work + threads - 1) / threads;
   int64_t cap = (int64_t)num_sms() * 16;
+  if (cap > kRedSlots) cap = kRedSlots;
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   return (int)g;

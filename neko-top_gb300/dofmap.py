@@ -91,13 +91,22 @@ def _keys_face(ev, lx, d, side):
 
 def dofmap_from_vertices(ev, lx):
     """int64 global node ids (Neko layout, i fastest) from the element-vertex
-    connectivity ev (E x 8, tensor corner order)."""
+    connectivity ev (E x 8, tensor corner order; vertex ids in [0, 2^31)).
+
+    Host memory: the key table holds 6 int64 per local node and np.unique
+    sorts a copy of it, so the peak is about 100 bytes per local node (5 GB
+    for 2^21 elements of lx = 8, 13 GB for the 64^3-element lx = 8 box).
+    Number such meshes in parts, or generate box ids directly
+    (coef_t.box), when that is too much."""
     ev = np.ascontiguousarray(ev, dtype=np.int64)
     E = ev.shape[0]
     if ev.ndim != 2 or ev.shape[1] != 8:
         raise ValueError("ev must be E x 8")
     if lx < 2:
         raise ValueError("lx must be >= 2")
+    if E and (int(ev.min()) < 0 or int(ev.max()) >= 2 ** 31):
+        # face keys pack two sorted corner ids into one int64
+        raise ValueError("vertex ids must lie in [0, 2^31)")
     N, l3 = lx - 1, lx ** 3
     records = []  # (local index array, key columns)
     vmax = int(ev.max()) + 1

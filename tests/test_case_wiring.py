@@ -26,6 +26,7 @@ CASE = """
         },
         "adjoint": {
             "pressure_solver": {"absolute_tolerance": 1e-7, "max_iterations": 300},
+            "velocity_solver": {"projection_hold_steps": 3},
             "projection_hold_steps": 2,
         },
     },
@@ -43,9 +44,12 @@ def test_adjoint_keys_fall_back_to_fluid(pkg):
     p = pkg.load_case(CASE)
     prs = pkg.solver_from_case(p, "pressure")
     assert (prs.ksp, prs.pc, prs.abstol, prs.max_iter) == ("gmres", "hsmg", 1e-7, 300)
-    assert prs.projection_space_size == 20 and prs.projection_hold_steps == 2
+    # a projection key directly under case.adjoint is not a solver key: the
+    # reference reads them only under <field>_solver, so the default 5 holds
+    assert prs.projection_space_size == 20 and prs.projection_hold_steps == 5
     vel = pkg.solver_from_case(p, "velocity")
     assert (vel.ksp, vel.pc, vel.abstol, vel.max_iter, vel.projection_space_size) == ("cg", "jacobi", 1e-6, 800, 0)
+    assert vel.projection_hold_steps == 3
 
 
 def test_missing_required_key(pkg):

@@ -84,3 +84,7 @@ def test_reoriented_elements(orc, dofmap, seed):
 def test_bad_input(dofmap):
     with pytest.raises(ValueError):
         dofmap.dofmap_from_vertices(np.zeros((2, 7), dtype=np.int64), 4)
+    ev = np.arange(16, dtype=np.int64).reshape(2, 8)
+    ev[1, 7] = 2 ** 31  # face keys pack two ids into one int64
+    with pytest.raises(ValueError):
+        dofmap.dofmap_from_vertices(ev, 4)

@@ -46,3 +46,11 @@ def test_noalloc_rejects_oversized_masks(pkg, dev):
     st = L.ntg_glsc2_mask_noalloc(None, None, None, 16_777_217, C.c_void_p(out.data_ptr()), None)
     assert st == 1
     assert b"exceeds the maximum" in L.ntg_last_error()
+
+
+def test_noalloc_empty_mask_writes_zero(pkg, dev):
+    L = pkg.lib()
+    out = torch.full((1,), 7.0, dtype=torch.float64, device=dev)
+    assert _run(L, out, out, torch.zeros(1, dtype=torch.int32, device=dev)[:0], out) == 0, L.ntg_last_error()
+    torch.cuda.synchronize()
+    assert float(out.item()) == 0.0
