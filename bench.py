@@ -1,22 +1,26 @@
 #!/usr/bin/env python
-"""Benchmark: time to a 1e-10 relative residual for the SEM pressure-Poisson
-solve on one GB300, learned-free mixed precision (FP32 inner Jacobi-PCG in an
-FP64 flexible CG) against the plain FP64 Jacobi-PCG drop-in, plus the Ax
+"""Benchmark: time to a 1e-10 relative residual of the SEM Brinkman
+pressure-Poisson sequence on one GB300 with the learned initial guess and
+the FP32-inner / FP64-refined CG, against the plain FP64 drop-in
+(Jacobi-PCG with Neko's residual projection) on the same GPU, plus the Ax
 GDOF/s of both precisions.
 
-Workload (default, --config c2): 32^3 hex elements, N = 7 (16.8M local
+Workload (default, --config c5seq): 64^3 hex elements, N = 7 (134M local
 DOFs), box deformed by a seeded sinusoid of amplitude 0.05 h per axis,
-pressure-Poisson (h1 = 1, h2 = 0) with a Dirichlet face at x = 1, RHS the weak
-form of 16 seeded Fourier modes with amplitudes ~ |k|^-2.  Inputs are
-synthetic (seeded generators in the library) and larger than L2.
-
-One step = one full solve from a zero initial guess, RHS resident in HBM.
-`e2e` repeats the step through the public API with the RHS copied from pinned
-host memory and the solution copied back inside the timed region.
+Brinkman pressure-Poisson h1 = 1, h2 = chi(rho) (RAMP q = 8, chimax = 1e4,
+rho = 12 Gaussian blobs moved by a seeded 1% perturbation every 20 solves),
+Dirichlet face x = 1, a 200-solve sequence of right-hand sides from 32
+Fourier modes with AR(1) amplitudes (rho = 0.98).  The network trains
+online on solves 1-100; one step = one solve of the evaluation half (101 on)
+with its RHS resident in HBM; `e2e` times further solves through the public
+API with the RHS copied from pinned host memory and the solution copied
+back.  Inputs are synthetic (seeded generators in the library) and larger
+than L2.  --config c1/c2/c3/c5 times single solves from a zero guess.
 
 --impl reference times the reference algorithm's CPU implementation (the C
 oracle: FP64 Jacobi-PCG, matrix-free sum factorisation, OpenMP) on the host
-cores, each step a bounded sample of CG iterations scaled to a full solve.
+cores; each step is a bounded sample of CG iterations, and the value scales
+it by the iterations of a full solve (the line says by how many).
 """
 from __future__ import annotations
 
@@ -226,17 +230,388 @@ def run_kernels_only(args, pkg, coef, f, dev):
 
 
 SEQUENCES = {
-    "c5": dict(E=(64, 64, 64), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.05, nsolves=100, ntrain=50,
+    "c5": dict(E=(64, 64, 64), lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), amp=0.05, nsolves=200, ntrain=100,
                desc="64^3 deformed hex (0.05h sinusoid), N=7 (134M local DOFs); Brinkman Poisson h1=1, h2=chi(rho) "
                     "(RAMP q=8, chimax=1e4, rho = 12 Gaussian blobs, moved by a seeded 1% perturbation every 20 "
-                    "solves); RHS = 32 Fourier modes with AR(1) amplitudes (rho=0.98); Dirichlet x=1; 100 solves to "
-                    "1e-10, online training on 1-50, evaluation on 51-100"),
+                    "solves); RHS = 32 Fourier modes with AR(1) amplitudes (rho=0.98); Dirichlet x=1; 200 solves to "
+                    "1e-10, online training on 1-100, evaluation on 101-200"),
     "c4": dict(E=(64, 16, 16), lo=(0.0, 0.0, 0.0), hi=(8.0, 2.0, 2.0), amp=0.05, nsolves=400, ntrain=200,
                desc="channel 64x16x16 hex on [0,8]x[0,2]x[0,2] (0.05h sinusoid), N=7 (8.4M local DOFs); Brinkman "
                     "Poisson h1=1, h2=chi(rho) (RAMP q=8, chimax=1e4, rho = 12 Gaussian blobs, moved by a seeded 1% "
                     "perturbation every 20 solves); RHS = 32 Fourier modes with AR(1) amplitudes (rho=0.98); Dirichlet "
                     "x=8; 400 solves to 1e-10, online training on 1-200, evaluation on 201-400"),
 }
+DESIGN_EVERY = 20  # the design field moves every 20 solves
+
+
+class SequenceCase:
+    """The seeded Brinkman pressure-Poisson sequence on the device: mesh,
+    Dirichlet face, AR(1) right-hand sides and the design field of each
+    solve (a 1% perturbation every 20 solves)."""
+
+    def __init__(self, pkg, name, dev):
+        import torch
+        self.pkg, self.cfg, self.dev = pkg, SEQUENCES[name], dev
+        ex, ey, ez = self.cfg["E"]
+        self.coef = pkg.coef_t.box(ex, ey, ez, LX, lo=self.cfg["lo"], hi=self.cfg["hi"], amp=self.cfg["amp"],
+                                   seed=MESH_SEED, device=dev)
+        self.coef.set_mask(pkg.mask_face_xmax(ex, ey, ez, LX, device=dev), base=1)
+        self.nsol, self.ntrain = self.cfg["nsolves"], self.cfg["ntrain"]
+        self.k, self.ph, self.amps = pkg.ar1_modes(RHS_SEED, 32, self.nsol, rho=0.98)
+        self.ramp = pkg.RAMP_mapping_t(0.0, 1e4, 8.0, False)
+        self.rho0 = self.coef.field_blobs(RHO_SEED, 12, 0.1)
+        self.torch = torch
+
+    def chi(self, t):
+        """h2 = chi(rho) of the design that solve t sees."""
+        rho = self.rho0.clone()
+        for q in range(1, t // DESIGN_EVERY + 1):
+            d = self.coef.field_fourier(8, 1000 + q)
+            rho.add_(0.01 * d / d.abs().max()).clamp_(0.0, 1.0)
+        chi = self.torch.empty_like(rho)
+        self.ramp.apply_forward(chi, 1.0 - rho)
+        return chi
+
+    def set_design(self, t, chi=None):
+        self.coef.set_coefs(h1c=1.0, h2=self.chi(t) if chi is None else chi, ifh2=True)
+
+    def rhs(self, t):
+        return self.coef.rhs_assemble(self.coef.field_modes(self.k, self.amps[t], self.ph))
+
+
+def run_headline_sequence(args, ws, rank, local):
+    """The headline: the Brinkman pressure-Poisson sequence (C5: 64^3
+    deformed hex, N = 7, 134M local DOFs, 200 solves) solved to 1e-10 with
+    the learned initial guess inside Neko's residual projection and the
+    FP32-inner / FP64-refined CG with the two-level Schwarz preconditioner.
+    The network trains online on solves 1-100; solves from 101 on are the
+    evaluation half.  W of them are warm-up, the next K are the timed steps
+    (one step = one solve, RHS and design already in HBM), the K after that
+    are timed end to end through the public API (RHS copied from pinned host
+    memory, solution copied back), the rest of the evaluation half runs
+    untimed for its iteration statistics.  Beside it, on the same timed
+    solves: projection alone, the zero guess, and the plain FP64 drop-in
+    (Jacobi-PCG with Neko's projection) on a sample of them."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    L = pkg.lib()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    t_setup = time.time()
+    case = SequenceCase(pkg, args.config_seq, dev)
+    coef, nsol, ntrain = case.coef, case.nsol, case.ntrain
+    n = coef.n
+    W, K = args.warmup, args.steps
+    t0 = ntrain + W
+    if t0 + 2 * K > nsol:
+        raise SystemExit(f"--warmup {W} --steps {K}: the evaluation half holds {nsol - ntrain} solves "
+                         f"(W + 2K at most)")
+    pc = "schwarz2" if args.pc in ("auto", "schwarz2") else args.pc
+    delta = args.delta if args.delta is not None else (1e-3 if pc == "schwarz2" else 0.1)
+    mode = args.guess
+
+    def new_seq(guess, method="cg_mixed", pc_=pc, delta_=delta):
+        return pkg.SolveSequence(coef, method, guess, rtol=RTOL, L=args.proj_l, train_steps=args.train_steps,
+                                 seed=3, lr=5e-4, pc=pc_, delta=delta_)
+
+    last_change = lambda t: t - t % DESIGN_EVERY
+    case.set_design(0)
+    seq = new_seq(mode)
+    torch.cuda.synchronize()
+    t_setup = time.time() - t_setup
+
+    keep = {}  # solutions of the current design window before t0 (seed the FP64 projection) and the timed ones
+    its_train, its_eval, used_eval = [], [], []
+    t_train = time.time()
+
+    def solve(t, f):
+        if t > 0 and t % DESIGN_EVERY == 0:
+            case.set_design(t)
+            seq.coefficients_changed()
+        seq.training = t < ntrain
+        x, mon, used, fn = seq.solve(f)
+        assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), (t, mon)
+        return x, mon, used
+
+    # training half and warm-up
+    for t in range(t0):
+        x, mon, used = solve(t, case.rhs(t))
+        (its_train if t < ntrain else its_eval).append(mon.iter)
+        if t >= ntrain:
+            used_eval.append(used)
+        if t >= last_change(t0):
+            keep[t] = x.clone()
+    torch.cuda.synchronize()
+    t_train = time.time() - t_train
+
+    # the K timed solves: RHS and design fields prepared in HBM beforehand
+    fs = [case.rhs(t) for t in range(t0, t0 + K)]
+    chis = {t: case.chi(t) for t in range(t0, t0 + K) if t % DESIGN_EVERY == 0}
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    mons = []
+    l0 = int(L.ntg_launch_count())
+    torch.cuda.nvtx.range_push("timed_solves")
+    with ClockSampler(local) as clk:
+        e0, e1 = ev(), ev()
+        e0.record()
+        for q, t in enumerate(range(t0, t0 + K)):
+            if t % DESIGN_EVERY == 0:
+                case.set_design(t, chis[t])
+                seq.coefficients_changed()
+            seq.training = False
+            x, mon, used, fn = seq.solve(fs[q])
+            mons.append((mon, fn, used))
+            if q < args.fp64_sample:
+                keep[t] = x.clone()
+        e1.record()
+        torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    launches = int(L.ntg_launch_count()) - l0
+    barrier(ws)
+    t_timed = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws)
+    for mon, fn, used in mons:
+        assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), mon
+        its_eval.append(mon.iter)
+        used_eval.append(used)
+    del fs
+
+    # end to end through the public API: per step, the RHS is copied from
+    # pinned host memory and the solution back, inside the timed region
+    f_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    x_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    f_d = torch.empty(n, dtype=torch.float64, device=dev)
+    t_e2e = 0.0
+    for t in range(t0 + K, t0 + 2 * K):
+        f_h.copy_(case.rhs(t))  # prepared untimed
+        chi_t = case.chi(t) if t % DESIGN_EVERY == 0 else None
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record()
+        f_d.copy_(f_h, non_blocking=True)
+        if chi_t is not None:
+            case.set_design(t, chi_t)
+            seq.coefficients_changed()
+        seq.training = False
+        x, mon, used, fn = seq.solve(f_d)
+        x_h.copy_(x, non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        t_e2e += a.elapsed_time(b) / 1e3
+        assert mon.status == pkg.NTG_OK, mon
+        its_eval.append(mon.iter)
+        used_eval.append(used)
+    t_e2e = max_over_ranks(t_e2e, ws)
+
+    # the rest of the evaluation half, untimed (iteration statistics)
+    if not args.short_eval:
+        for t in range(t0 + 2 * K, nsol):
+            x, mon, used = solve(t, case.rhs(t))
+            its_eval.append(mon.iter)
+            used_eval.append(used)
+
+    # live per-kernel device times inside one more solve of the sequence
+    L.ntg_timer_reset()
+    L.ntg_timer_enable(1)
+    tprof = min(nsol - 1, t0 + 2 * K)
+    seq.training = False
+    _, mon_prof, _, _ = seq.solve(case.rhs(tprof))
+    torch.cuda.synchronize()
+    L.ntg_timer_enable(0)
+    ktimes = read_timers(L)
+    seq = None
+    torch.cuda.empty_cache()
+
+    # comparison modes on the same timed solves (same design window)
+    def window_run(guess, method="cg_mixed", pc_=pc, delta_=delta, seed_from=None, nt=K):
+        case.set_design(last_change(t0))
+        s2 = new_seq(guess, method, pc_, delta_)
+        start = last_change(t0)
+        if guess in ("zero",) or method == "cg":
+            start = t0
+        if seed_from is not None:
+            for t in range(last_change(t0), t0):
+                s2.record(case.rhs(t), seed_from[t])
+        for t in range(start, t0):
+            s2.solve(case.rhs(t))
+        its, secs, xs = [], [], []
+        for q, t in enumerate(range(t0, t0 + nt)):
+            if t % DESIGN_EVERY == 0:
+                case.set_design(t)
+                s2.coefficients_changed()
+            f = case.rhs(t)
+            torch.cuda.synchronize()
+            a, b = ev(), ev()
+            a.record()
+            x, mon, used, fn = s2.solve(f)
+            b.record()
+            torch.cuda.synchronize()
+            assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), (guess, t, mon)
+            its.append(mon.iter)
+            secs.append(a.elapsed_time(b) / 1e3)
+            if method == "cg":
+                xs.append(x.clone())
+        del s2
+        torch.cuda.empty_cache()
+        return its, secs, xs
+
+    extra = {}
+    t_ours = t_timed / K
+    if not args.no_compare:
+        for g in ("projection", "zero"):
+            if g == mode:
+                continue
+            its, secs, _ = window_run(g)
+            extra[g] = {"iters_mean": round(statistics.mean(its), 2), "s_per_solve": round(statistics.mean(secs), 5)}
+    # the plain FP64 drop-in (Jacobi-PCG + Neko's projection, L = 20) on the
+    # first solves of the timed window, its basis seeded with this design
+    # window's earlier solutions
+    fp64 = None
+    if args.fp64_sample > 0:
+        its, secs, xs = window_run("projection", "cg", "jacobi", None, seed_from=keep, nt=args.fp64_sample)
+        errs = [float(torch.linalg.norm(keep[t0 + q] - xs[q]) / torch.linalg.norm(xs[q])) for q in range(len(xs))]
+        t64 = statistics.mean(secs)
+        ours_same = statistics.mean(float(m[0].iter) for m in mons[:len(xs)])
+        fp64 = {"method": "FP64 Jacobi-PCG + residual projection (L=%d), the plain drop-in" % args.proj_l,
+                "s_per_solve": round(t64, 4), "iters_mean": round(statistics.mean(its), 1), "solves": len(xs),
+                "error_vs_fp64_solution": max(errs), "ours_iters_same_solves": ours_same}
+    del keep
+    torch.cuda.empty_cache()
+
+    # Ax alone at this size: both precisions, cold L2 per launch (a 256 MB
+    # write between launches), against the in-solve FP32 launches
+    ax = ax_rates(pkg, coef, dev)
+    pk, pk_kind = peaks()
+    ncoef = 1  # h2 = chi * B precombined
+    ax32 = ktimes.get("ax_fp32")
+    bpd = (2 + 6 + ncoef) * 4
+    t_in = ax32["avg_us"] * 1e-6 if ax32 else ax["fp32_s"]
+    roof = {"kernel": "k_ax_helm_f32_tma (FP32 Ax inside the timed solves)", "bound": "hbm",
+            "achieved": round(bpd * n / t_in / 1e9, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(bpd * n / t_in / 1e9 / pk["hbm_gbs"], 4), "peak_source": pk_kind,
+            "bytes_per_dof": bpd, "standalone_cold": {
+                "us": round(ax["fp32_s"] * 1e6, 1), "achieved": round(bpd * n / ax["fp32_s"] / 1e9, 1),
+                "frac": round(bpd * n / ax["fp32_s"] / 1e9 / pk["hbm_gbs"], 4)},
+            "traffic": args.traffic if args.traffic is not None else measured_traffic("k_ax_helm_f32_tma", n, ncoef)}
+    fdm = ktimes.get("schwarz_fdm")
+    roof_fdm = None
+    if fdm:
+        # algorithmic bytes per element: the extended box's values of r are
+        # read once per element in the ideal (each local DOF once, 4 B) and
+        # the extended result written (LE^3 x 4 B, LE = lx + 2), plus the
+        # element's six scalars
+        E = coef.nelv
+        b_fdm = 4 * n + 4 * E * (LX + 2) ** 3 + 6 * 4 * E
+        roof_fdm = {"kernel": "k_fdm<8> (Schwarz local solves, the largest share of a solve)", "bound": "hbm",
+                    "achieved": round(b_fdm / (fdm["avg_us"] * 1e-6) / 1e9, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                    "frac": round(b_fdm / (fdm["avg_us"] * 1e-6) / 1e9 / pk["hbm_gbs"], 4), "peak_source": pk_kind,
+                    "bytes_per_launch": b_fdm, "avg_us": fdm["avg_us"],
+                    "traffic": measured_traffic("k_fdm", n, 0)}
+    ax64 = ktimes.get("ax_fp64")
+    t_k64 = ax64["avg_us"] * 1e-6 if ax64 else ax["fp64_s"]
+    roof64 = {"kernel": "k_ax_helm<double,8> (FP64 Ax: residual replacements, projection)", "bound": "fp64",
+              "achieved": round(116.0 * n / t_k64 / 1e9, 1), "peak": FP64_TFLOPS * 1e3, "unit": "GFLOP/s",
+              "frac": round(116.0 * n / t_k64 / 1e9 / (FP64_TFLOPS * 1e3), 4),
+              "peak_source": "FP64 FMA-chain probe, bench.py --fp64-peak"}
+
+    ev_its = its_eval
+    out = {
+        "metric": METRIC,
+        "value": round(ws * K / t_timed, 4),
+        "unit": "solves/s",
+        "n_gpus": ws,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": round(t_timed / K * 1e3, 3),
+        "s_per_solve": round(t_timed / K, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 inner / f64 outer (bf16 network)",
+        "data": "synthetic (seeded generators; no dataset)",
+        "config": {"workload": f"{args.config_seq} sequence: {case.cfg['desc']}", "n_local_dofs": n,
+                   "n_unique_dofs": coef.nu,
+                   "method": f"guess '{mode}' (learned network inside Neko's residual projection, L={args.proj_l}) + "
+                             f"cg_mixed (FP32 PCG, {pc} preconditioner, FP64 reliable updates at delta={delta:g})",
+                   "step": f"one solve of the evaluation half to 1e-10 (solves {t0 + 1}-{t0 + K} of {nsol}; "
+                           f"{ntrain} training solves and {W} warm-up solves before)",
+                   "l2": "inputs larger than L2 (FP32 G 3.2 GB, FP64 G 6.4 GB at 64^3)",
+                   "parallelism": "replicas only" if ws > 1 else "1 GPU"},
+        "iterations": {"timed_mean": round(statistics.mean(m[0].iter for m in mons), 2),
+                       "eval_mean": round(statistics.mean(ev_its), 2), "eval_solves": len(ev_its),
+                       "train_mean": round(statistics.mean(its_train), 2),
+                       "fp64_ax_per_solve": round(statistics.mean(m[0].fp64_ax for m in mons), 2),
+                       "guess_used": {u: used_eval.count(u) for u in sorted(set(used_eval))}},
+        "compare_same_solves": extra,
+        "fp64_dropin": fp64,
+        "speedup_vs_fp64_dropin": round(fp64["s_per_solve"] / t_ours, 2) if fp64 else None,
+        "ax_gdof_s": {"fp64": round(n / ax["fp64_s"] / 1e9, 3), "fp32": round(n / ax["fp32_s"] / 1e9, 3),
+                      "fp32_in_solve": round(n / t_in / 1e9, 3)},
+        "roofline": roof,
+        "roofline_fdm": roof_fdm,
+        "roofline_fp64_ax": roof64,
+        "kernels_in_one_solve": ktimes,
+        "e2e": {"value": round(ws * K / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(n * 8),
+                "d2h_bytes_per_step": int(n * 8),
+                "note": "each step timed alone (CUDA events): H2D copy of its RHS from pinned memory, the solve "
+                        "through SolveSequence.solve, D2H copy of x; the RHS is prepared untimed between steps"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "setup_s": round(t_setup, 3),
+        "train_s": round(t_train, 2),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_sample_seq(args.config_seq, args.cpu_iters, fp64["iters_mean"] if fp64 else None)
+    return out
+
+
+def read_timers(L):
+    import ctypes as C
+    names = {0: "ax_fp64", 1: "ax_fp32", 2: "gs_fp64", 3: "gs_fp32", 4: "cg_update_fp64", 5: "cg_update_fp32",
+             6: "cg_dir_fp64", 7: "cg_dir_fp32", 8: "precond_fp32", 9: "schwarz_fdm", 10: "schwarz_coarse",
+             11: "schwarz_pull"}
+    out = {}
+    for i, nm in names.items():
+        ms, cnt = C.c_double(), C.c_longlong()
+        L.ntg_timer_read(i, C.byref(ms), C.byref(cnt))
+        if cnt.value:
+            out[nm] = {"total_ms": round(ms.value, 4), "launches": cnt.value,
+                       "avg_us": round(ms.value / cnt.value * 1e3, 2)}
+    # shares of the solve: the preconditioner's parts are inside precond_fp32
+    tot = sum(v["total_ms"] for k, v in out.items() if not k.startswith("schwarz_")) or 1.0
+    for v in out.values():
+        v["share"] = round(v["total_ms"] / tot, 4)
+    return out
+
+
+def ax_rates(pkg, coef, dev, reps=10):
+    """Seconds per Ax launch, FP64 and FP32, each launch timed alone with
+    CUDA events after a 256 MB write that evicts L2."""
+    import torch
+    n = coef.n
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=dev)
+    ax = pkg.ax_helm_t()
+    res = {}
+    for dt, key in ((torch.float64, "fp64_s"), (torch.float32, "fp32_s")):
+        u = torch.randn(n, dtype=dt, device=dev)
+        w = torch.empty_like(u)
+        for _ in range(3):
+            ax.compute(w, u, coef)
+        tt = []
+        for _ in range(reps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            ax.compute(w, u, coef)
+            b.record()
+            torch.cuda.synchronize()
+            tt.append(a.elapsed_time(b) / 1e3)
+        res[key] = statistics.median(tt)
+        del u, w
+    return res
 
 
 def run_sequence(args, local):
@@ -791,6 +1166,106 @@ def cpu_sample(cfg, iters, solve_iters):
                       f"scaled by the {solve_iters} iterations of the FP64 solve to 1e-10"}
 
 
+def setup_cpu_sequence(name, t):
+    """The oracle's copy of solve t of a sequence: mesh, mask, h2 = chi of
+    that solve's design, and its right-hand side."""
+    import numpy as np
+    from oracle import oracle as orc
+    orc.build()
+    cfg = SEQUENCES[name]
+    ex, ey, ez = cfg["E"]
+    m = orc.build_mesh(ex, ey, ez, LX, lo=cfg["lo"], hi=cfg["hi"], amp=cfg["amp"], seed=MESH_SEED)
+    mask = orc.mask_face_xmax(ex, ey, ez, LX)
+    rho = orc.field_blobs(m, RHO_SEED, 12, 0.1)
+    for q in range(1, t // DESIGN_EVERY + 1):
+        d = orc.field_fourier(m, *orc.fourier_params(1000 + q, 8))
+        rho = np.clip(rho + 0.01 * d / np.abs(d).max(), 0.0, 1.0)
+    h2 = orc.ramp_forward(1.0 - rho, 0.0, 1e4, 8.0, 0)
+    import __graft_entry__ as ge  # the AR(1) parameters (host code, no GPU)
+    k, ph, amps = ge.load_package().ar1_modes(RHS_SEED, 32, cfg["nsolves"], rho=0.98)
+    f = orc.assemble_rhs(m, orc.field_fourier(m, k.reshape(-1, 3), amps[t], ph), mask)
+    dinv = orc.jacobi(m, h1c=1.0, h2=h2, mask=mask)
+    return orc, m, mask, h2, f, dinv
+
+
+def sequence_fp64_iterations(name):
+    """Iterations per solve of the plain FP64 drop-in (Jacobi-PCG + residual
+    projection) on the timed solves of the sequence, as recorded from the
+    drop-in's run on the GPU (the same algorithm as the oracle's CG; the
+    parity tests hold the two iteration counts within 2)."""
+    try:
+        return float(json.load(open(os.path.join(ROOT, "oracle", "iterations.json")))[name + "seq"]["iters"])
+    except Exception:
+        return None
+
+
+def cpu_sample_seq(name, iters, solve_iters):
+    t = SEQUENCES[name]["ntrain"]
+    orc, m, mask, h2, f, dinv = setup_cpu_sequence(name, t)
+    t_it = orc.cg_time_per_iter(m, f, iters, h1c=1.0, h2=h2, mask=mask, dinv=dinv)
+    if solve_iters is None:
+        solve_iters = sequence_fp64_iterations(name)
+    s_solve = t_it * solve_iters if solve_iters else None
+    return {"value": round(1.0 / s_solve, 6) if s_solve else None, "unit": "solves/s", "cores": orc.num_threads(),
+            "kind": "port", "s_per_iter": round(t_it, 4), "s_per_solve": round(s_solve, 2) if s_solve else None,
+            "sample": f"{iters} FP64 Jacobi-PCG iterations of solve {t + 1} of the sequence (the oracle, "
+                      f"{orc.num_threads()} host threads), times the {solve_iters} iterations per solve of the FP64 "
+                      f"drop-in on the timed solves"}
+
+
+def run_reference_sequence(args, ws, rank):
+    """The reference algorithm on the host cores for the sequence workload:
+    FP64 Jacobi-PCG (the oracle, all host threads).  Each step times
+    --cpu-iters CG iterations of the first evaluation solve; ms_per_step is
+    that measured time.  `value` (solves/s) scales the time per iteration by
+    the iterations per solve of the FP64 drop-in (iterations_scaling says
+    which).  A full CPU solve of C1 (8^3 elements) is timed outright
+    beside it."""
+    if rank != 0:
+        return None
+    import numpy as np
+    name = args.config_seq
+    t = SEQUENCES[name]["ntrain"]
+    t_set = time.time()
+    orc, m, mask, h2, f, dinv = setup_cpu_sequence(name, t)
+    t_set = time.time() - t_set
+    for _ in range(max(args.warmup, 1)):
+        orc.cg_time_per_iter(m, f, 1, h1c=1.0, h2=h2, mask=mask, dinv=dinv)
+    samples = [orc.cg_time_per_iter(m, f, args.cpu_iters, h1c=1.0, h2=h2, mask=mask, dinv=dinv)
+               for _ in range(args.steps)]
+    t_it = statistics.median(samples)
+    iters = sequence_fp64_iterations(name)
+    s_solve = t_it * iters if iters else None
+    val = round(1.0 / s_solve, 7) if s_solve else None
+    cores = orc.num_threads()
+    del m, f, dinv, h2
+    # one CPU solve timed outright: C1 (8^3 affine, N=7, Brinkman RAMP, Jacobi-PCG to 1e-10)
+    orc1, m1, mask1, h1c1, h21, f1, dinv1 = setup_cpu_case(CONFIGS["c1"])
+    t1 = time.time()
+    _, it1, r01, r11 = orc1.cg(m1, f1, h1c=h1c1, h2=h21, mask=mask1, dinv=dinv1, rtol=RTOL, max_iter=20000)
+    t1 = time.time() - t1
+    sample = (f"each step: {args.cpu_iters} FP64 Jacobi-PCG iterations of solve {t + 1} of the {name} sequence on "
+              f"{cores} host threads (the oracle); value = 1 / (median time per iteration x {iters} iterations per "
+              f"solve of the FP64 drop-in)")
+    return {
+        "metric": METRIC, "impl": "reference", "value": val, "unit": "solves/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_it * args.cpu_iters * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generators; no dataset)",
+        "config": {"workload": f"{name}seq sequence: {SEQUENCES[name]['desc']}",
+                   "n_local_dofs": int(np.prod(SEQUENCES[name]["E"])) * LX ** 3,
+                   "method": "FP64 Jacobi-PCG, matrix-free sum factorisation (C oracle, OpenMP)"},
+        "iterations_scaling": {"timed_per_step": args.cpu_iters, "iterations_per_solve": iters,
+                               "source": "FP64 drop-in (Jacobi-PCG + projection) on the timed solves, oracle/iterations.json",
+                               "s_per_iter": round(t_it, 4), "s_per_solve": round(s_solve, 2) if s_solve else None},
+        "c1_full_solve": {"s": round(t1, 3), "iterations": it1, "res_start": r01, "res_final": r11,
+                          "solves_per_s": round(1.0 / t1, 3), "cores": cores},
+        "setup_s": round(t_set, 2),
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
@@ -841,7 +1316,9 @@ def main(argv=None):
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=sorted(CONFIGS), default="c2")
+    p.add_argument("--config", choices=sorted(CONFIGS) + [k + "seq" for k in SEQUENCES], default="c5seq",
+                   help="c5seq (default, the headline): the 64^3 Brinkman sequence with the learned guess; "
+                        "c1/c2/c3/c5: single solves from a zero guess")
     p.add_argument("--method", choices=["cg_mixed", "fcg_mixed"], default="cg_mixed")
     p.add_argument("--delta", type=float, default=None,
                    help="reliable-update threshold of cg_mixed (default: 2.2e-4 with schwarz2, 0.1 otherwise; "
@@ -853,7 +1330,8 @@ def main(argv=None):
     p.add_argument("--inner-rtol", type=float, default=1e-4)
     p.add_argument("--inner-max", type=int, default=2000)
     p.add_argument("--fp64-steps", type=int, default=2)
-    p.add_argument("--cpu-iters", type=int, default=20)
+    p.add_argument("--cpu-iters", type=int, default=None,
+                   help="CG iterations per CPU sample (default: 2 for sequences, 20 for single solves)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--kernels-only", action="store_true",
                    help="set up the workload and launch each hot kernel a few times (profiler captures)")
@@ -861,7 +1339,8 @@ def main(argv=None):
                    help="dram bytes per FP32 Ax launch from an ncu capture (reported as roofline.traffic)")
     p.add_argument("--sequence", choices=sorted(SEQUENCES), default=None,
                    help="instead of the headline line: a solve sequence with each initial-guess mode")
-    p.add_argument("--fp64-sample", type=int, default=10, help="FP64 drop-in solves sampled in --sequence")
+    p.add_argument("--fp64-sample", type=int, default=None,
+                   help="FP64 drop-in solves sampled (default: 2 in the headline sequence, 10 in --sequence)")
     p.add_argument("--fp64-warm", type=int, default=8, help="FP64 solves before the sample (fills projection)")
     p.add_argument("--proj-l", type=int, default=20, help="projection space size of --sequence (Neko's default 20)")
     p.add_argument("--mma", action="store_true", help="time MMA design updates on the workload's DOF count")
@@ -870,8 +1349,22 @@ def main(argv=None):
                    help="time the FP64 terms either side of each solve (residuals, advection, forcing)")
     p.add_argument("--seq-modes", default="zero,projection,learned,learned_only",
                    help="initial-guess modes of --sequence (comma separated)")
+    p.add_argument("--guess", default="learned", choices=["zero", "projection", "learned", "learned_only"],
+                   help="initial-guess mode of the headline sequence")
+    p.add_argument("--train-steps", type=int, default=30, help="Adam steps per training solve")
+    p.add_argument("--short-eval", action="store_true",
+                   help="headline sequence: skip the untimed rest of the evaluation half")
+    p.add_argument("--no-compare", action="store_true",
+                   help="headline sequence: skip the projection-only and zero-guess runs of the timed solves")
     args = p.parse_args(argv)
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else max(args.warmup, 1)
+    args.config_seq = args.config[:-3] if args.config.endswith("seq") else None
+    if args.config_seq and (args.terms or args.mma or args.kernels_only or args.sequence or args.fp64_peak):
+        args.config, args.config_seq = "c2", None  # the analysis modes run on a single-solve mesh
+    if args.fp64_sample is None:
+        args.fp64_sample = 2 if args.config_seq else 10
+    if args.cpu_iters is None:
+        args.cpu_iters = 2 if args.config_seq else 20
     ws, rank, local = dist_env()
     if args.sequence:
         print(json.dumps(run_sequence(args, local)), flush=True)
@@ -903,7 +1396,7 @@ def main(argv=None):
                           "median": round(statistics.median(vals), 4), "clocks": clk.summary()}), flush=True)
         return 0
     if args.impl == "reference":
-        res = run_reference(args, ws, rank)
+        res = run_reference_sequence(args, ws, rank) if args.config_seq else run_reference(args, ws, rank)
         if res is not None:
             print(json.dumps(res), flush=True)
         return 0
@@ -912,7 +1405,7 @@ def main(argv=None):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    res = run_ours(args, ws, rank, local)
+    res = run_headline_sequence(args, ws, rank, local) if args.config_seq else run_ours(args, ws, rank, local)
     if rank == 0:
         print(json.dumps(res), flush=True)
     if ws > 1:

@@ -108,12 +108,19 @@ int ntg_supported_lx(int* lx, int cap);
 /* kernels the library has launched in this process (all entry points) */
 unsigned long long ntg_launch_count(void);
 /* per-kernel device timers (CUDA events around each launch, on the
-   launching stream; the stand-in for Neko's profiler regions).  Ids: 0 FP64
-   Ax, 1 FP32 Ax, 2 FP64 gs, 3 FP32 gs, 4/5 CG update FP64/FP32, 6/7 CG
-   direction FP64/FP32.  Off by default. */
+   launching stream).  Ids: 0 FP64 Ax, 1 FP32 Ax, 2 FP64 gs, 3 FP32 gs, 4/5
+   CG update FP64/FP32, 6/7 CG direction FP64/FP32, 8 the whole FP32
+   preconditioner application, 9 Schwarz FDM local solves, 10 Schwarz
+   coarse solve, 11 Schwarz prolongation (pull).  Off by default. */
 int ntg_timer_enable(int on);
 int ntg_timer_read(int id, double* total_ms, long long* count);
 int ntg_timer_reset(void);
+/* Neko's profiler_start_region(name, colour) / profiler_end_region as NVTX
+   ranges (the reference's regions: sources/adjoint/adjoint_pnpn.f90:715,
+   733,746,783; sources/mapping_functions/PDE_filter_mapping.f90:254,341).
+   colour <= 0: no colour.  Regions nest; end closes the innermost. */
+int ntg_profiler_start_region(const char* name, int colour);
+int ntg_profiler_end_region(void);
 
 /* ---------------------------------------------------------------------- */
 /* mesh / coef_t / gs_t plan                                               */
@@ -292,6 +299,15 @@ int ntg_proj_pre_solving_with(ntg_proj* proj, double* b_d, const double* g_d, in
    one FP64 operator application updates the basis */
 int ntg_proj_post_solving(ntg_proj* proj, double* x_d);
 int ntg_proj_size(const ntg_proj* proj);
+/* post_solving for a solution x_d of the full right-hand side found
+   elsewhere (another solver, a restart): the basis takes x - xbar as
+   post_solving(x - xbar) would; x_d is not modified.  Follows
+   ntg_proj_pre_solving (not pre_solving_with). */
+int ntg_proj_post_solving_full(ntg_proj* proj, const double* x_d);
+/* checkpoint access: dir = 0 stores the basis size in *m and copies the m
+   basis vectors and their A-images to xs_d / axs_d (device, m*n doubles
+   each; either may be null); dir = 1 loads *m (<= L) of them back. */
+int ntg_proj_state(ntg_proj* proj, int* m, double* xs_d, double* axs_d, int dir);
 
 /* ---------------------------------------------------------------------- */
 /* learned initial guess (new; the reference has no learned part).  A      */
@@ -317,6 +333,13 @@ int ntg_guess_predict(ntg_guess* guess, const double* b_d, double* x_d, int* rea
    x into the history.  *loss = the last training loss (-1 if none). */
 int ntg_guess_observe(ntg_guess* guess, const double* b_d, const double* x_d, int train_steps, double* loss);
 int ntg_guess_reset_history(ntg_guess* guess);
+/* checkpoint of the network state: a device FP32 buffer of
+   ntg_guess_state_len floats (weights, Adam moments, solution history),
+   ints[4] = {Adam step, history head, history count, 0} and hrms[8] (the
+   history's RMS scales); dir = 0 stores, dir = 1 loads.  A restored network
+   continues bit for bit. */
+int64_t ntg_guess_state_len(const ntg_guess* g);
+int ntg_guess_state(ntg_guess* g, float* buf_d, long long* ints, double* hrms, int dir);
 /* online-training loss: 1 (default) = relative element-energy error
    (e, A_e e)/(x, A_e x) plus relative L2 error (CG pays for energy-norm
    error, so a guess trained in L2 alone carries nodal noise); 0 = MSE */

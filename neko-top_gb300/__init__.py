@@ -38,7 +38,8 @@ from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, adjoint_minimum_d
                   adv_lin_dealias_t, adv_lin_no_dealias_t, ar1_modes, ax_helm_t, build_box, cadd_mask, cdtp, cmult_mask, coef_t,
                   col2_mask, col3_mask, conv1, curl, dudxyz, fld_file_t, glsc2_mask, glsc3, gs_t, invcol1_mask, jacobi_t, opgrad,
                   build_solver, krylov_solver_factory, ksp_monitor_t, learned_guess_t, load_case, mask_face_xmax, mma_t,
-                  permeability, solver_config_t, solver_from_case,
+                  permeability, profiler_end_region, profiler_region, profiler_start_region, solver_config_t,
+                  solver_from_case,
                   pnpn_prs_res_t,
                   pnpn_step_t, pnpn_vel_res_t, projection_t, schwarz_t,
                   sens_min_dissipation, simple_brinkman_source_term_t, sub3_mask)
@@ -53,7 +54,7 @@ __all__ = [
     "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
-    "learned_guess_t", "SolveSequence", "ar1_modes", "schwarz_t", "dist", "dofmap", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
+    "learned_guess_t", "SolveSequence", "profiler_start_region", "profiler_end_region", "profiler_region", "ar1_modes", "schwarz_t", "dist", "dofmap", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
     "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "pnpn_step_t", "mma_t", "fld_file_t", "load_case", "solver_from_case",
     "solver_config_t", "build_solver",
 ]

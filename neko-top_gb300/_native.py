@@ -90,6 +90,10 @@ SIGNATURES = {
     "ntg_proj_post_solving": (_i, [_vp, _vp]),
     "ntg_proj_pre_solving_with": (_i, [_vp, _vp, _vp, _pi]),
     "ntg_proj_size": (_i, [_vp]),
+    "ntg_proj_post_solving_full": (_i, [_vp, _vp]),
+    "ntg_proj_state": (_i, [_vp, _pi, _vp, _vp, _i]),
+    "ntg_profiler_start_region": (_i, [C.c_char_p, _i]),
+    "ntg_profiler_end_region": (_i, []),
     "ntg_glsc3": (_i, [_vp, _vp, _vp, _vp, _i64, _pd]),
     "ntg_guess_create": (_i, [_vp, _i, _i, C.c_uint64, C.POINTER(_vp)]),
     "ntg_guess_destroy": (_i, [_vp]),
@@ -97,6 +101,8 @@ SIGNATURES = {
     "ntg_guess_predict": (_i, [_vp, _vp, _vp, _pi]),
     "ntg_guess_observe": (_i, [_vp, _vp, _vp, _i, _pd]),
     "ntg_guess_reset_history": (_i, [_vp]),
+    "ntg_guess_state_len": (_i64, [_vp]),
+    "ntg_guess_state": (_i, [_vp, _vp, C.POINTER(C.c_longlong), _pd, _i]),
     "ntg_guess_set_loss": (_i, [_vp, _i]),
     "ntg_guess_set_head": (_i, [_vp, _i]),
     "ntg_guess_num_params": (_i64, [_vp]),

@@ -406,6 +406,30 @@ def krylov_solver_factory(coef: coef_t, type_: str = "cg", max_iter: int = 800, 
     return _ksp(coef, t, max_iter, rtol, abstol)
 
 
+def profiler_start_region(name: str, colour: int = 0):
+    """Neko's profiler_start_region: an NVTX range named as the reference's
+    regions are (e.g. 'Pressure solve')."""
+    check(lib().ntg_profiler_start_region(name.encode(), int(colour)))
+
+
+def profiler_end_region():
+    check(lib().ntg_profiler_end_region())
+
+
+class profiler_region:
+    """with profiler_region('Pressure solve', 3): ... (start/end pair)."""
+
+    def __init__(self, name: str, colour: int = 0):
+        self.name, self.colour = name, colour
+
+    def __enter__(self):
+        profiler_start_region(self.name, self.colour)
+        return self
+
+    def __exit__(self, *a):
+        profiler_end_region()
+
+
 class projection_t:
     """Residual projection: init(n, L, activ_step), pre_solving(b, tstep),
     post_solving(x, tstep) (sources/adjoint/adjoint_pnpn.f90:365-374,729-741;
@@ -446,6 +470,35 @@ class projection_t:
         if not self._active:  # pre_solving was skipped for this solve
             return
         check(lib().ntg_proj_post_solving(self._h, _ptr(x, n=self.coef.n, name="x")))
+
+    def record(self, b, x):
+        """Enter a solution x of the (assembled, masked) right-hand side b
+        that was found elsewhere, as pre_solving(b) + solve +
+        post_solving would have; b and x are not modified."""
+        check(lib().ntg_proj_pre_solving(self._h, _ptr(b.clone(), n=self.coef.n, name="b")))
+        check(lib().ntg_proj_post_solving_full(self._h, _ptr(x, n=self.coef.n, name="x")))
+
+    def state(self):
+        """(m, xs [m, n], axs [m, n]): a copy of the basis and its A-images."""
+        m = C.c_int()
+        check(lib().ntg_proj_state(self._h, C.byref(m), None, None, 0))
+        n = self.coef.n
+        xs = torch.empty((m.value, n), dtype=torch.float64, device=self.coef.device)
+        axs = torch.empty_like(xs)
+        if m.value:
+            check(lib().ntg_proj_state(self._h, C.byref(m), C.c_void_p(xs.data_ptr()), C.c_void_p(axs.data_ptr()),
+                                       0))
+        return m.value, xs, axs
+
+    def load_state(self, m, xs, axs):
+        mm = C.c_int(int(m))
+        if m:
+            xs = xs.to(device=self.coef.device, dtype=torch.float64).contiguous()
+            axs = axs.to(device=self.coef.device, dtype=torch.float64).contiguous()
+            check(lib().ntg_proj_state(self._h, C.byref(mm), C.c_void_p(xs.data_ptr()), C.c_void_p(axs.data_ptr()),
+                                       1))
+        else:
+            check(lib().ntg_proj_state(self._h, C.byref(mm), None, None, 1))
 
     @property
     def size(self):
@@ -498,6 +551,23 @@ class learned_guess_t:
 
     def reset_history(self):
         check(lib().ntg_guess_reset_history(self._h))
+
+    def state(self):
+        """Checkpoint: {'buf': FP32 device tensor, 'ints': [4], 'hrms': [8]}."""
+        n = int(lib().ntg_guess_state_len(self._h))
+        buf = torch.empty(n, dtype=torch.float32, device=self.coef.device)
+        ints = (C.c_longlong * 4)()
+        hrms = (C.c_double * 8)()
+        check(lib().ntg_guess_state(self._h, C.c_void_p(buf.data_ptr()), ints, hrms, 0))
+        return {"buf": buf, "ints": list(ints), "hrms": list(hrms)}
+
+    def load_state(self, st):
+        buf = st["buf"].to(device=self.coef.device, dtype=torch.float32).contiguous()
+        if buf.numel() != int(lib().ntg_guess_state_len(self._h)):
+            raise ValueError("network checkpoint of another shape")
+        ints = (C.c_longlong * 4)(*[int(v) for v in st["ints"]])
+        hrms = (C.c_double * 8)(*[float(v) for v in st["hrms"]])
+        check(lib().ntg_guess_state(self._h, C.c_void_p(buf.data_ptr()), ints, hrms, 1))
 
     @property
     def num_params(self):
@@ -579,14 +649,24 @@ class SolveSequence:
                       worse than zero is replaced by zero)
 
     Every solve converges to the same tolerance, relative to the original
-    right-hand side, whatever the guess."""
+    right-hand side, whatever the guess.  Each solve runs inside the
+    profiler region `region` (the reference's 'Pressure solve',
+    adjoint_pnpn.f90:733), and with `log` (a path or a writable file) each
+    solve appends one JSON line: solve index, iterations, FP64 operator
+    applications, start / final residual, right-hand-side norm, status,
+    guess used and its wall time; the caller may add fields per solve
+    (e.g. the error against an FP64 solution) through solve(f, extra=...).
+    state_dict / load_state_dict checkpoint everything the next solve
+    depends on (projection basis, network weights, Adam moments and step,
+    solution history, counters), so a sequence resumes bit for bit."""
 
     def __init__(self, coef: coef_t, method="cg_mixed", guess="zero", rtol=1e-10, max_iter=50000, L=20,
-                 history=4, hidden=64, seed=0, lr=1e-3, train_steps=20, pc="jacobi", delta=None):
+                 history=4, hidden=64, seed=0, lr=1e-3, train_steps=20, pc="jacobi", delta=None, log=None,
+                 region="Pressure solve", region_colour=3):
         if guess not in ("zero", "projection", "learned", "learned_only"):
             raise ValueError(f"unknown guess mode {guess!r}")
         if pc not in ("jacobi", "schwarz", "schwarz2"):
-            raise ValueError(f"unknown preconditioner {pc!r}")
+            raise ValueError(f"preconditioner {pc!r} is not built (jacobi, schwarz, schwarz2)")
         self.coef, self.guess, self.rtol = coef, guess, rtol
         self.ksp = krylov_solver_factory(coef, method, max_iter, rtol)
         self.sw = None
@@ -603,36 +683,70 @@ class SolveSequence:
             self.ksp.set_guess_guard(True)
         self.train_steps = train_steps
         self.training = True
+        self.nsolved = 0
+        self.region, self.region_colour = region, region_colour
+        self._log_own = isinstance(log, str)
+        self._log = open(log, "a") if isinstance(log, str) else log
         self.x = torch.zeros(coef.n, dtype=torch.float64, device=coef.device)
         self.g = torch.zeros(coef.n, dtype=torch.float64, device=coef.device) if self.net is not None else None
 
-    def solve(self, f):
+    def solve(self, f, extra=None):
         """Returns (x, monitor, guess used, ||f||)."""
+        import time
+        t0 = time.perf_counter() if self._log is not None else 0.0
         x = self.x
         x.zero_()
         used = "zero"
         fn = glsc3(self.coef, f, f, self._mult()) ** 0.5
-        if self.proj is not None:
-            # the reduced system keeps the tolerance of the original RHS
-            b = f.clone()
-            used = "projection"
-            if self.net is not None and self.net.predict(f, self.g):
-                if self.proj.pre_solving_with(b, self.g):
-                    used = "projection+learned"
+        profiler_start_region(self.region, self.region_colour)
+        try:
+            if self.proj is not None:
+                # the reduced system keeps the tolerance of the original RHS
+                b = f.clone()
+                used = "projection"
+                if self.net is not None and self.net.predict(f, self.g):
+                    if self.proj.pre_solving_with(b, self.g):
+                        used = "projection+learned"
+                else:
+                    self.proj.pre_solving(b)
+                self.ksp.set_tol(0.0, self.rtol * fn)
+                mon = self.ksp.solve(x, b)
+                self.proj.post_solving(x)
             else:
-                self.proj.pre_solving(b)
-            self.ksp.set_tol(0.0, self.rtol * fn)
-            mon = self.ksp.solve(x, b)
-            self.proj.post_solving(x)
-        else:
-            if self.net is not None and self.net.predict(f, x):
-                used = "learned"
-            mon = self.ksp.solve(x, f)
-            if mon.guess_rejected:
-                used = "zero (learned rejected)"
-        if self.net is not None:
-            self.net.observe(f, x, self.train_steps if self.training else 0)
+                if self.net is not None and self.net.predict(f, x):
+                    used = "learned"
+                mon = self.ksp.solve(x, f)
+                if mon.guess_rejected:
+                    used = "zero (learned rejected)"
+            if self.net is not None:
+                self.net.observe(f, x, self.train_steps if self.training else 0)
+        finally:
+            profiler_end_region()
+        if self._log is not None:
+            import json
+            torch.cuda.synchronize(self.coef.device)
+            rec = {"solve": self.nsolved, "iter": mon.iter, "inner_iter": mon.inner_iter, "fp64_ax": mon.fp64_ax,
+                   "res_start": mon.res_start, "res_final": mon.res_final, "rhs_norm": fn,
+                   "rel_res": mon.res_final / fn if fn > 0 else 0.0, "status": mon.status, "guess": used,
+                   "training": bool(self.training and self.net is not None),
+                   "time_s": round(time.perf_counter() - t0, 6)}
+            if extra:
+                rec.update(extra)
+            self._log.write(json.dumps(rec) + "\n")
+            self._log.flush()
+        self.nsolved += 1
         return x, mon, used, fn
+
+    def record(self, f, x):
+        """Take a converged solution x of f found elsewhere (another solver,
+        a restart) into the guess state, as if this sequence had solved it:
+        the projection basis and the network's history are updated; nothing
+        is solved."""
+        if self.proj is not None:
+            self.proj.record(f, x)
+        if self.net is not None:
+            self.net.observe(f, x, 0)
+        self.nsolved += 1
 
     def coefficients_changed(self):
         """Refresh what depends on h1/h2 (Jacobi diagonal, Schwarz means)
@@ -642,6 +756,37 @@ class SolveSequence:
             self.sw.update()
         if self.proj is not None:
             self.proj.reset()
+
+    def state_dict(self):
+        """Everything the next solve depends on, as host tensors."""
+        st = {"nsolved": self.nsolved, "training": self.training, "guess": self.guess}
+        if self.proj is not None:
+            m, xs, axs = self.proj.state()
+            st["proj"] = {"m": m, "xs": xs.cpu(), "axs": axs.cpu()}
+        if self.net is not None:
+            st["net"] = {k: (v.cpu() if isinstance(v, torch.Tensor) else v) for k, v in self.net.state().items()}
+        return st
+
+    def load_state_dict(self, st):
+        if st["guess"] != self.guess:
+            raise ValueError(f"checkpoint of guess mode {st['guess']!r}, sequence is {self.guess!r}")
+        self.nsolved, self.training = int(st["nsolved"]), bool(st["training"])
+        if self.proj is not None:
+            p = st["proj"]
+            self.proj.load_state(p["m"], p["xs"], p["axs"])
+        if self.net is not None:
+            self.net.load_state(st["net"])
+
+    def save(self, path):
+        torch.save(self.state_dict(), path)
+
+    def load(self, path):
+        self.load_state_dict(torch.load(path, map_location="cpu", weights_only=False))
+
+    def close(self):
+        if self._log is not None and self._log_own:
+            self._log.close()
+        self._log = None
 
     def _mult(self):
         if not hasattr(self, "_mult_t"):
@@ -679,16 +824,25 @@ class PDE_filter_t:
     (r^2 K + B) X_out = B X_in, all-Neumann, initial guess X_in; r = 0.01,
     abstol 1e-10, 200 iterations by default."""
 
-    def __init__(self, coef: coef_t, r=0.01, abstol=1e-10, max_iter=200):
+    def __init__(self, coef: coef_t, r=0.01, abstol=1e-10, max_iter=200, log=None):
         self.coef, self.r = coef, r
         self.ksp = krylov_solver_factory(coef, "cg", max_iter, 0.0, abstol)
         self.ksp_results = None
+        self.log = log  # None, or a callable taking each solve's log line
 
     def _apply(self, X_out, X_in):
         mon = ntg_monitor()
-        check(lib().ntg_filter_apply(self.coef.handle, self.ksp.handle, _ptr(X_out, n=self.coef.n),
-                                     _ptr(X_in, n=self.coef.n), float(self.r), C.byref(mon)))
+        # the solve inside the reference's 'filter solve' region
+        # (PDE_filter_mapping.f90:254-259)
+        with profiler_region("filter solve"):
+            check(lib().ntg_filter_apply(self.coef.handle, self.ksp.handle, _ptr(X_out, n=self.coef.n),
+                                         _ptr(X_in, n=self.coef.n), float(self.r), C.byref(mon)))
         self.ksp_results = ksp_monitor_t.from_c(mon)
+        if self.log is not None:
+            # the reference's 'Filter' message (PDE_filter_mapping.f90:264-272)
+            m = self.ksp_results
+            self.log("Filter\nIterations:   Start residual:     Final residual:\n"
+                     f"{m.iter:11d}   {m.res_start:15.7E}     {m.res_final:15.7E}")
         return self.ksp_results
 
     def apply_forward(self, X_out, X_in):
@@ -914,10 +1068,14 @@ class pnpn_step_t:
         """Advances p and (u, v, w) in place; returns the pressure monitor
         and the three velocity monitors."""
         cp, cv = self.cp, self.cv
+        # profiler regions and colours as the reference names them
+        # (adjoint_pnpn.f90:715,733,746,783)
+        profiler_start_region("Pressure residual", 18)
         self.prs.compute(p, self.p_res, u, v, w, ue, ve, we, fx, fy, fz, cp, prs_surface, sym_surface, bd=bd,
                          dt=dt, mu=mu, rho=rho, base=base)
         self.gs_p.op(self.p_res)
         bc_list_apply_scalar(cp, self.p_res)
+        profiler_end_region()
         h1p = self._inv(rho)
         if isinstance(h1p, torch.Tensor):
             cp.set_coefs(h1=h1p.contiguous(), ifh2=False)
@@ -929,14 +1087,17 @@ class pnpn_step_t:
             self.ksp_p.set_tol(0.0, self.rtol * glsc3(cp, self.p_res, self.p_res, self.mult) ** 0.5)
             self.proj_p.pre_solving(self.p_res, tstep)
         self.dp.zero_()
-        mon_p = self.ksp_p.solve(self.dp, self.p_res)
+        with profiler_region("Pressure solve", 3):
+            mon_p = self.ksp_p.solve(self.dp, self.p_res)
         if self.proj_p is not None:
             self.proj_p.post_solving(self.dp, tstep)
         p.add_(self.dp)
+        profiler_start_region("Velocity residual", 19)
         self.vel.compute(u, v, w, *self.res, p, fx, fy, fz, cv, mu=mu, rho=rho, bd=bd, dt=dt)
         for r in self.res:
             self.gs_v.op(r)
             bc_list_apply_scalar(cv, r)
+        profiler_end_region()
         h2v = (rho * (bd / dt)) if isinstance(rho, torch.Tensor) else torch.full_like(self.dp, float(rho) * bd / dt)
         if isinstance(mu, torch.Tensor):
             cv.set_coefs(h1=mu.contiguous(), h2=h2v.contiguous(), ifh2=True)
@@ -945,14 +1106,16 @@ class pnpn_step_t:
         for d in self.du:
             d.zero_()
         if self.proj_v is None:
-            mons_v = self.ksp_v.solve_coupled(*self.du, *self.res)
+            with profiler_region("Velocity solve", 4):
+                mons_v = self.ksp_v.solve_coupled(*self.du, *self.res)
         else:
             # per component, each to the tolerance of its unprojected RHS
             mons_v = []
             for pr, r, d in zip(self.proj_v, self.res, self.du):
                 self.ksp_v.set_tol(0.0, self.rtol * glsc3(cv, r, r, self.mult) ** 0.5)
                 pr.pre_solving(r, tstep)
-                mons_v.append(self.ksp_v.solve(d, r))
+                with profiler_region("Velocity solve", 4):
+                    mons_v.append(self.ksp_v.solve(d, r))
                 pr.post_solving(d, tstep)
         for x, d in zip((u, v, w), self.du):
             x.add_(d)

@@ -162,7 +162,7 @@ void count_launch();
 // off by default; enabled with ntg_timer_enable.
 enum TimerId {
   TM_AX64 = 0, TM_AX32 = 1, TM_GS64 = 2, TM_GS32 = 3, TM_UPD64 = 4, TM_UPD32 = 5, TM_DIR64 = 6,
-  TM_DIR32 = 7, TM_PC32 = 8, TM_COUNT = 16
+  TM_DIR32 = 7, TM_PC32 = 8, TM_FDM = 9, TM_CRS = 10, TM_PULL = 11, TM_COUNT = 16
 };
 // z = M r with the Schwarz preconditioner (schwarz.cu); no-op once sc->done
 // z = M r (FP32).  With mult non-null also (r, z)_mult into sc (FinRz{rz_mode}).

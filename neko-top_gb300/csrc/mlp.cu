@@ -840,6 +840,47 @@ int ntg_guess_set_loss(ntg_guess* g, int energy) {
   return NTG_OK;
 }
 
+// Checkpoint of the whole network state: one FP32 device buffer of
+// ntg_guess_state_len floats [P | Adam m1 | Adam m2 | history ring, slot by
+// slot], the integers {Adam step, ring head, ring count, 0} and the ring's
+// RMS scales (8 doubles).  dir = 0 stores, dir = 1 loads (the BF16 weight
+// copy is rebuilt from P, so a restored network computes bit for bit as
+// the saved one).
+int64_t ntg_guess_state_len(const ntg_guess* g) { return g ? 3 * g->np + (int64_t)g->nhist * g->n : 0; }
+
+int ntg_guess_state(ntg_guess* g, float* buf_d, long long* ints, double* hrms, int dir) {
+  clear_error();
+  NTG_CHECK_ARG(g && buf_d && ints && hrms && (dir == 0 || dir == 1), "ntg_guess_state: bad argument");
+  cudaStream_t s = g->plan->stream;
+  const int64_t np = g->np, n = g->n;
+  float* parts[3] = {g->P, g->m1, g->m2};
+  const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+  if (dir == 0) {
+    for (int q = 0; q < 3; ++q) NTG_CUDA_TRY(cudaMemcpyAsync(buf_d + q * np, parts[q], sizeof(float) * np, k, s));
+    for (int h = 0; h < g->nhist; ++h)
+      NTG_CUDA_TRY(cudaMemcpyAsync(buf_d + 3 * np + h * n, g->hist[h], sizeof(float) * n, k, s));
+    ints[0] = g->t;
+    ints[1] = g->head;
+    ints[2] = g->hcount;
+    ints[3] = 0;
+    for (int h = 0; h < 8; ++h) hrms[h] = g->hrms[h];
+  } else {
+    NTG_CHECK_ARG(ints[0] >= 0 && ints[1] >= 0 && ints[1] < g->nhist && ints[2] >= 0 && ints[2] <= g->nhist,
+                  "ntg_guess_state: counters out of range");
+    for (int q = 0; q < 3; ++q) NTG_CUDA_TRY(cudaMemcpyAsync(parts[q], buf_d + q * np, sizeof(float) * np, k, s));
+    for (int h = 0; h < g->nhist; ++h)
+      NTG_CUDA_TRY(cudaMemcpyAsync(g->hist[h], buf_d + 3 * np + h * n, sizeof(float) * n, k, s));
+    { k_f2bf<<<grid_for(np, 256), 256, 0, s>>>(g->P, g->Pb, np); NTG_COUNT_LAUNCH(); }
+    NTG_CUDA_TRY(cudaGetLastError());
+    g->t = ints[0];
+    g->head = (int)ints[1];
+    g->hcount = (int)ints[2];
+    for (int h = 0; h < 8; ++h) g->hrms[h] = hrms[h];
+  }
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  return NTG_OK;
+}
+
 int ntg_guess_reset_history(ntg_guess* g) {
   clear_error();
   NTG_CHECK_ARG(g, "ntg_guess_reset_history: null argument");

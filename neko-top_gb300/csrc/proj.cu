@@ -122,6 +122,12 @@ __global__ void k_sum3(double* __restrict__ o, const double* __restrict__ a, con
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     o[i] = a[i] + b[i];
 }
+// o = a - b
+__global__ void k_sub3(double* __restrict__ o, const double* __restrict__ a, const double* __restrict__ b,
+                       int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    o[i] = a[i] - b[i];
+}
 // o = a * B
 __global__ void k_mulB(double* __restrict__ o, const double* __restrict__ a, const double* __restrict__ B, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -329,6 +335,55 @@ int ntg_proj_post_solving(ntg_proj* q, double* x_d) {
   // x = xbar + dx
   { k_sum3<<<G, 256, 0, s>>>(x_d, q->xbar, x_d, n); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+// post_solving for a solution found elsewhere: x_d is the full solution of
+// the right-hand side given to the preceding pre_solving (not the reduced
+// one), e.g. the same solve made by another solver or read from a restart.
+// The basis takes dx = x - xbar exactly as post_solving(dx) would; x_d is
+// left unchanged.  Not after pre_solving_with (its extra direction is
+// for one solve only).
+int ntg_proj_post_solving_full(ntg_proj* q, const double* x_d) {
+  clear_error();
+  NTG_CHECK_ARG(q && x_d, "ntg_proj_post_solving_full: null argument");
+  NTG_CHECK_ARG(q->have_pre, "ntg_proj_post_solving_full: pre_solving was not called");
+  NTG_CHECK_ARG(!q->have_extra, "ntg_proj_post_solving_full: not after pre_solving_with");
+  ntg_plan* p = q->plan;
+  cudaStream_t s = p->stream;
+  const int64_t n = p->n;
+  const int G = grid_for(n, 256);
+  // dx = x - xbar into the (unused) extra-direction buffer
+  { k_sub3<<<G, 256, 0, s>>>(q->gv, x_d, q->xbar, n); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return ntg_proj_post_solving(q, q->gv);
+}
+
+// The basis for checkpoints: m (vectors held), and with dir = 0 copies the
+// m basis vectors and their A-images out to xs_d / axs_d (m*n doubles
+// each), with dir = 1 loads m of them (m <= L) back in.
+int ntg_proj_state(ntg_proj* q, int* m, double* xs_d, double* axs_d, int dir) {
+  clear_error();
+  NTG_CHECK_ARG(q && m && (dir == 0 || dir == 1), "ntg_proj_state: bad argument");
+  ntg_plan* p = q->plan;
+  cudaStream_t s = p->stream;
+  const size_t bytes = sizeof(double) * (size_t)p->n;
+  if (dir == 0) {
+    *m = q->m;
+    if (xs_d && q->m) NTG_CUDA_TRY(cudaMemcpyAsync(xs_d, q->xs, bytes * q->m, cudaMemcpyDeviceToDevice, s));
+    if (axs_d && q->m) NTG_CUDA_TRY(cudaMemcpyAsync(axs_d, q->axs, bytes * q->m, cudaMemcpyDeviceToDevice, s));
+  } else {
+    NTG_CHECK_ARG(*m >= 0 && *m <= q->L, "ntg_proj_state: m must be in [0, L]");
+    NTG_CHECK_ARG(*m == 0 || (xs_d && axs_d), "ntg_proj_state: null basis");
+    if (*m) {
+      NTG_CUDA_TRY(cudaMemcpyAsync(q->xs, xs_d, bytes * *m, cudaMemcpyDeviceToDevice, s));
+      NTG_CUDA_TRY(cudaMemcpyAsync(q->axs, axs_d, bytes * *m, cudaMemcpyDeviceToDevice, s));
+    }
+    q->m = *m;
+    q->have_pre = 0;
+    q->have_extra = 0;
+  }
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
   return NTG_OK;
 }
 

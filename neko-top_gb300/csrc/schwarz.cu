@@ -996,19 +996,43 @@ int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s,
   ntg_plan* p = w->plan;
   switch (p->lx) {
     case 4:
+      timer_start(TM_FDM, s);
       NTG_TRY(sw::fdm_launch<4>(w, r, s, sc));
-      if (w->coarse_ready) NTG_TRY(sw::coarse_launch(w, s, sc));
+      timer_stop(TM_FDM, s);
+      if (w->coarse_ready) {
+        timer_start(TM_CRS, s);
+        NTG_TRY(sw::coarse_launch(w, s, sc));
+        timer_stop(TM_CRS, s);
+      }
+      timer_start(TM_PULL, s);
       NTG_TRY(sw::pull_launch<4>(w, z, r, s, sc, mult, part, rz_mode));
+      timer_stop(TM_PULL, s);
       break;
     case 6:
+      timer_start(TM_FDM, s);
       NTG_TRY(sw::fdm_launch<6>(w, r, s, sc));
-      if (w->coarse_ready) NTG_TRY(sw::coarse_launch(w, s, sc));
+      timer_stop(TM_FDM, s);
+      if (w->coarse_ready) {
+        timer_start(TM_CRS, s);
+        NTG_TRY(sw::coarse_launch(w, s, sc));
+        timer_stop(TM_CRS, s);
+      }
+      timer_start(TM_PULL, s);
       NTG_TRY(sw::pull_launch<6>(w, z, r, s, sc, mult, part, rz_mode));
+      timer_stop(TM_PULL, s);
       break;
     case 8:
+      timer_start(TM_FDM, s);
       NTG_TRY(sw::fdm_launch<8>(w, r, s, sc));
-      if (w->coarse_ready) NTG_TRY(sw::coarse_launch(w, s, sc));
+      timer_stop(TM_FDM, s);
+      if (w->coarse_ready) {
+        timer_start(TM_CRS, s);
+        NTG_TRY(sw::coarse_launch(w, s, sc));
+        timer_stop(TM_CRS, s);
+      }
+      timer_start(TM_PULL, s);
       NTG_TRY(sw::pull_launch<8>(w, z, r, s, sc, mult, part, rz_mode));
+      timer_stop(TM_PULL, s);
       break;
     default:
       set_error("schwarz: lx=%d not compiled (4, 6, 8)", p->lx);
