@@ -212,7 +212,9 @@ def time_solves(ksp, x, f, k, ev):
 
 def run_kernels_only(args, pkg, coef, f, dev):
     """A few launches of each hot kernel on the workload (for profiler
-    captures): FP64 Ax, FP32 Ax, gs, and 24 iterations of the mixed solver."""
+    captures): FP64 Ax, FP32 Ax, gs, 24 iterations of the mixed solver (with
+    the two-level Schwarz when --pc schwarz2), and one forward pass of the
+    learned guess's network over all elements (tensor-core GEMMs)."""
     import torch
     n = coef.n
     ax = pkg.ax_helm_t()
@@ -223,8 +225,15 @@ def run_kernels_only(args, pkg, coef, f, dev):
             ax.compute(w, u, coef)
         pkg.gs_t(coef).op(w)
     ksp = pkg.krylov_solver_factory(coef, "cg_mixed", 24, RTOL)
+    if args.pc in ("schwarz", "schwarz2"):
+        ksp.set_schwarz(pkg.schwarz_t(coef, coarse=args.pc == "schwarz2"))
     x = torch.zeros(n, dtype=torch.float64, device=dev)
     mon = ksp.solve(x, f)
+    torch.cuda.synchronize()
+    net = pkg.learned_guess_t(coef, history=4, hidden=64, seed=1)
+    E = coef.nelv
+    Xb = torch.randint(-16000, 16000, (E, net.F), dtype=torch.int16, device=dev)
+    net.forward_raw(Xb, E)
     torch.cuda.synchronize()
     return {"kernels_only": True, "n_local_dofs": n, "iters": mon.iter, "status": mon.status}
 
@@ -421,7 +430,7 @@ def run_headline_sequence(args, ws, rank, local):
     _, mon_prof, _, _ = seq.solve(case.rhs(tprof))
     torch.cuda.synchronize()
     L.ntg_timer_enable(0)
-    ktimes = read_timers(L)
+    ktimes = read_timers(L, mon_prof.iter)
     seq = None
     torch.cuda.empty_cache()
 
@@ -568,18 +577,26 @@ def run_headline_sequence(args, ws, rank, local):
     return out
 
 
-def read_timers(L):
+def read_timers(L, iters=None):
+    """Per-kernel device times of the solve(s) timed with the library's
+    timers.  The host polls the device stop flag every 16 iterations, so up
+    to 15 launches of each per-iteration FP32 kernel run after convergence
+    and return at once; with `iters` (the iterations done) their average is
+    taken over the iterations that did work."""
     import ctypes as C
     names = {0: "ax_fp64", 1: "ax_fp32", 2: "gs_fp64", 3: "gs_fp32", 4: "cg_update_fp64", 5: "cg_update_fp32",
              6: "cg_dir_fp64", 7: "cg_dir_fp32", 8: "precond_fp32", 9: "schwarz_fdm", 10: "schwarz_coarse",
              11: "schwarz_pull"}
+    per_iter = {"ax_fp32", "gs_fp32", "cg_update_fp32", "cg_dir_fp32", "precond_fp32", "schwarz_fdm",
+                "schwarz_coarse", "schwarz_pull"}
     out = {}
     for i, nm in names.items():
         ms, cnt = C.c_double(), C.c_longlong()
         L.ntg_timer_read(i, C.byref(ms), C.byref(cnt))
         if cnt.value:
-            out[nm] = {"total_ms": round(ms.value, 4), "launches": cnt.value,
-                       "avg_us": round(ms.value / cnt.value * 1e3, 2)}
+            eff = min(cnt.value, iters) if (iters and nm in per_iter) else cnt.value
+            out[nm] = {"total_ms": round(ms.value, 4), "launches": cnt.value, "launches_working": eff,
+                       "avg_us": round(ms.value / eff * 1e3, 2)}
     # shares of the solve: the preconditioner's parts are inside precond_fp32
     tot = sum(v["total_ms"] for k, v in out.items() if not k.startswith("schwarz_")) or 1.0
     for v in out.values():
@@ -1013,22 +1030,10 @@ def run_ours(args, ws, rank, local):
     L.ntg_timer_reset()
     L.ntg_timer_enable(1)
     x.zero_()
-    ksp_mx.solve(x, f)
+    mon_prof = ksp_mx.solve(x, f)
     torch.cuda.synchronize()
     L.ntg_timer_enable(0)
-    import ctypes as C
-    names = {0: "ax_fp64", 1: "ax_fp32", 2: "gs_fp64", 3: "gs_fp32", 4: "cg_update_fp64", 5: "cg_update_fp32",
-             6: "cg_dir_fp64", 7: "cg_dir_fp32", 8: "schwarz_fp32"}
-    ktimes = {}
-    for i, nm in names.items():
-        ms, cnt = C.c_double(), C.c_longlong()
-        L.ntg_timer_read(i, C.byref(ms), C.byref(cnt))
-        if cnt.value:
-            ktimes[nm] = {"total_ms": round(ms.value, 4), "launches": cnt.value,
-                          "avg_us": round(ms.value / cnt.value * 1e3, 2)}
-    tot = sum(v["total_ms"] for v in ktimes.values()) or 1.0
-    for v in ktimes.values():
-        v["share"] = round(v["total_ms"] / tot, 4)
+    ktimes = read_timers(L, mon_prof.iter)
 
     # roofline of the dominant kernel (FP32 Ax, HBM bound):
     # algorithmic bytes per local DOF = (u in + w out + 6 G + ncoef) * 4 B

@@ -246,6 +246,11 @@ int ntg_schwarz_set_coarse(ntg_schwarz* sw, int enable);
 /* penalisation): z += w D^-1 r with D the assembled diagonal and w the     */
 /* node's mass fraction (h2 B) / D in [0, 1].                               */
 int ntg_schwarz_set_mass_term(ntg_schwarz* sw, int enable);
+/* lx = 8: the FDM local solves' in-plane transforms on the tcgen05 tensor  */
+/* cores (1: one shared 100 x 100 plane operator in BF16, data split into  */
+/* two BF16 terms, FP32 accumulation; the third direction in FP32) or on   */
+/* the FP32 cores (0, the default).  Both are symmetric preconditioners.   */
+int ntg_schwarz_set_fdm_path(ntg_schwarz* sw, int tensor_cores);
 int ntg_schwarz_destroy(ntg_schwarz* sw);
 /* z = M r (FP32; assembled and masked) */
 int ntg_schwarz_apply(ntg_schwarz* sw, float* z_d, const float* r_d);
@@ -311,13 +316,15 @@ int ntg_proj_state(ntg_proj* proj, int* m, double* xs_d, double* axs_d, int dir)
 
 /* ---------------------------------------------------------------------- */
 /* learned initial guess (new; the reference has no learned part).  A      */
-/* per-element MLP, (history + 1) * lx^3 -> hidden -> hidden -> history:   */
-/* its outputs weight the stored solutions on that element (weights       */
-/* delta_f0 + y_f, so an untrained net returns the newest solution), which */
-/* keeps the guess as smooth as the solutions; BF16 weights, tensor-core   */
-/* GEMMs with FP32 accumulation, trained online with Adam on the solver's  */
-/* own solutions (relative energy + L2 loss).  Inserted where the reference*/
-/* sets the initial guess: projection pre_solving                          */
+/* per-element MLP, (history + 1) * lx^3 -> 64 -> 64 -> lx^3 (lx = 8):     */
+/* inputs the last `history` solutions and the right-hand side on the      */
+/* element's nodes, output a nodal correction of the newest solution (the  */
+/* output layer starts at zero, so an untrained net returns the newest     */
+/* solution), averaged over shared nodes and masked.  BF16 weights,        */
+/* tcgen05 tensor-core GEMMs with FP32 accumulation in tensor memory,      */
+/* trained online with Adam on the solver's own solutions (relative energy */
+/* + L2 loss of the assembled guess).  Inserted where the reference sets   */
+/* the initial guess: projection pre_solving                               */
 /* (sources/adjoint/adjoint_pnpn.f90:729) and the filter's guess copy      */
 /* (sources/mapping_functions/PDE_filter_mapping.f90:246,332).             */
 /* ---------------------------------------------------------------------- */
@@ -344,11 +351,6 @@ int ntg_guess_state(ntg_guess* g, float* buf_d, long long* ints, double* hrms, i
    (e, A_e e)/(x, A_e x) plus relative L2 error (CG pays for energy-norm
    error, so a guess trained in L2 alone carries nodal noise); 0 = MSE */
 int ntg_guess_set_loss(ntg_guess* guess, int energy);
-/* output head: 1 (default) = the per-element outputs are mean-pooled into
-   one set of weights of the stored solutions (the guess stays in their
-   span, as smooth as they are); 0 = each element weights the solutions on
-   its own nodes (element-to-element jumps; measured to cost CG iterations) */
-int ntg_guess_set_head(ntg_guess* guess, int pooled);
 /* parameters as one flat FP32 array [W1 | b1 | W2 | b2 | W3 | b3] (W row
    major, [in x out]); set != 0 writes them */
 int64_t ntg_guess_num_params(const ntg_guess* guess);
@@ -358,6 +360,15 @@ int ntg_guess_forward_raw(ntg_guess* guess, const uint16_t* X_d, int64_t E, floa
 int ntg_guess_grad_raw(ntg_guess* guess, const uint16_t* X_d, const float* T_d, int64_t E, float* grad_d,
                        double* loss);
 int ntg_guess_train_raw(ntg_guess* guess, const uint16_t* X_d, const float* T_d, int64_t E, double* loss);
+
+/* BF16 GEMM on the tcgen05 tensor cores (the learned guess's GEMM):
+   C = A B^T with A [M x K] (row stride lda) and B [N x K] (row stride
+   ldb), BF16, K contiguous, every row 16-byte aligned (lda, ldb multiples
+   of 8); C FP32 [M x ldc].  Accumulation in FP32 (tensor memory).  err_d:
+   device int set to 1 if a bounded wait of the kernel ran out (null: a
+   library-owned flag).  Asynchronous on `stream`. */
+int ntg_gemm_bf16(const uint16_t* A_d, int64_t lda, const uint16_t* B_d, int64_t ldb, float* C_d, int64_t ldc,
+                  int64_t M, int64_t N, int64_t K, int* err_d, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* dot products (FP64 accumulation, deterministic order)                   */

@@ -66,6 +66,7 @@ SIGNATURES = {
     "ntg_schwarz_update": (_i, [_vp]),
     "ntg_schwarz_set_coarse": (_i, [_vp, _i]),
     "ntg_schwarz_set_mass_term": (_i, [_vp, _i]),
+    "ntg_schwarz_set_fdm_path": (_i, [_vp, _i]),
     "ntg_schwarz_destroy": (_i, [_vp]),
     "ntg_schwarz_apply": (_i, [_vp, _vp, _vp]),
     "ntg_rhs_assemble": (_i, [_vp, _vp, _vp]),
@@ -104,12 +105,12 @@ SIGNATURES = {
     "ntg_guess_state_len": (_i64, [_vp]),
     "ntg_guess_state": (_i, [_vp, _vp, C.POINTER(C.c_longlong), _pd, _i]),
     "ntg_guess_set_loss": (_i, [_vp, _i]),
-    "ntg_guess_set_head": (_i, [_vp, _i]),
     "ntg_guess_num_params": (_i64, [_vp]),
     "ntg_guess_params": (_i, [_vp, _vp, _i]),
     "ntg_guess_forward_raw": (_i, [_vp, _vp, _i64, _vp]),
     "ntg_guess_grad_raw": (_i, [_vp, _vp, _vp, _i64, _vp, _pd]),
     "ntg_guess_train_raw": (_i, [_vp, _vp, _vp, _i64, _pd]),
+    "ntg_gemm_bf16": (_i, [_vp, _i64, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp, _vp]),
     "ntg_ramp_forward": (_i, [_vp, _vp, _i64, _d, _d, _d, _i, _vp]),
     "ntg_ramp_backward": (_i, [_vp, _vp, _vp, _i64, _d, _d, _d, _i, _vp]),
     "ntg_brinkman_compute": (_i, [_vp] * 7 + [_i64, _vp, _i64, _i, _vp]),

@@ -370,6 +370,11 @@ class schwarz_t:
         coarse level's Dirichlet faces after coef_t.set_mask)."""
         check(lib().ntg_schwarz_update(self._h))
 
+    def set_fdm_path(self, tensor_cores: bool = True):
+        """lx = 8: FDM in-plane transforms on the tensor cores or on the FP32
+        cores (the default)."""
+        check(lib().ntg_schwarz_set_fdm_path(self._h, int(bool(tensor_cores))))
+
     def set_mass_term(self, enable: bool = True):
         """Add w D^-1 r (D the assembled diagonal, w the node's mass fraction):
         for mass terms varying inside elements (Brinkman penalisation)."""
@@ -524,8 +529,9 @@ class projection_t:
 
 
 class learned_guess_t:
-    """Per-element MLP initial guess, trained online on the solver's own
-    solutions (BF16 tensor-core GEMMs, FP32 accumulate, Adam)."""
+    """Per-element MLP initial guess, (history + 1) * 512 -> 64 -> 64 -> 512
+    nodal correction of the newest solution, trained online on the solver's
+    own solutions (tcgen05 BF16 tensor-core GEMMs, FP32 accumulate, Adam)."""
 
     def __init__(self, coef: coef_t, history=4, hidden=64, seed=0, lr=1e-3):
         self.coef = coef
@@ -534,7 +540,7 @@ class learned_guess_t:
         self._h = h
         self.history, self.hidden = history, hidden
         self.F = (history + 1) * coef.lx ** 3
-        self.O = history  # per-element weights of the stored solutions
+        self.O = coef.lx ** 3  # nodal output head
         check(lib().ntg_guess_set_lr(h, float(lr)))
 
     def predict(self, b, x):
@@ -582,7 +588,7 @@ class learned_guess_t:
     def set_params(self, p):
         check(lib().ntg_guess_params(self._h, _ptr(p, torch.float32, self.num_params, "params"), 1))
 
-    # raw network access (X: int16 tensor of BF16 bit patterns, [E, F])
+    # raw network access (X: int16 tensor of BF16 bit patterns, [E, F]; Y [E, 512])
     def forward_raw(self, Xbits, E):
         Y = torch.empty(E * self.O, dtype=torch.float32, device=self.coef.device)
         check(lib().ntg_guess_forward_raw(self._h, C.c_void_p(Xbits.data_ptr()), int(E), _ptr(Y, torch.float32)))

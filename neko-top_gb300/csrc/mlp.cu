@@ -1,32 +1,39 @@
 // Learned initial guess: a per-element MLP trained online on the solver's own
-// solutions, with hand-written BF16 tensor-core GEMMs (FP32 accumulate) for
-// the forward pass, the backward pass and an Adam update.
+// solutions.  Forward, backward and Adam are hand-written; every GEMM runs
+// on the tensor cores (tcgen05, BF16 operands, FP32 accumulation in TMEM;
+// tc_gemm.cu).
 //
 // Insertion points in the reference: the initial guess of the pressure /
 // filter solves -- projection pre_solving at sources/adjoint/adjoint_pnpn.f90:729
 // and the filter's guess copy at sources/mapping_functions/PDE_filter_mapping.f90:246,332.
 // The reference has no learned part; this is new.
 //
-// Network (per element, rows = elements):
-//   X [E x 5*512]  = last 4 solutions / s and the right-hand side / s_b on the
-//                    element's 512 nodes (BF16)
+// Network (per element, rows = elements, lx^3 = 512 nodes):
+//   X  [E x 5*512] = the last 4 solutions / s_x and the right-hand side / s_b
+//                    on the element's nodes (BF16; s = RMS values)
 //   H1 = relu(X W1 + b1)   [E x 64]
 //   H2 = relu(H1 W2 + b2)  [E x 64]
-//   Y  = H2 W3 + b3        [E x 4]   per-element weights: the guess on element
-//                                    e is sum_f (delta_f0 + Y[e][f]) x_{k-1-f},
-//                                    made continuous by the mult-weighted gs.
-// A nodal output head (one BF16-computed value per node) was measured to
-// leave node-scale noise that costs Jacobi-PCG more iterations at a 1e-10
-// tolerance than the guess saves; weighting the stored solutions keeps the
-// guess as smooth as the solutions.
-// Loss (online training): relative element-energy error (e, A_e e)/(x, A_e x)
-// plus relative L2 error of the combined guess; the raw test entry points
-// use the MSE of Y.
+//   Y  = H2 W3 + b3        [E x 512]  a nodal correction: the element's guess
+//                                     is x_{k-1} + s_x Y (W3 starts at zero,
+//                                     so the untrained net returns the newest
+//                                     solution), made continuous by the
+//                                     mult-weighted gather-scatter and masked.
+// Loss (online training): relative energy error (D, A D)/(x, A x) plus
+// relative L2 error of the assembled guess D = g - x; the gradient flows
+// back through the averaging (mult * gs).  The raw test entry points use
+// the MSE of Y.
 //
-// GEMMs: one tiled kernel, C = op(A) op(B) with arbitrary strides (so the
-// transposes of the backward pass need no copies), 64x64x32 tiles, 4 warps of
-// mma.sync m16n8k16 BF16 -> FP32, optional split-K whose partials are summed in
-// a fixed order (deterministic), epilogue bias / ReLU / BF16 copy.
+// GEMM layout: every operand is K-major (C = A B^T with A [M x K], B
+// [N x K]).  The forward pass keeps BF16 copies of the weights transposed
+// (W1T [64 x 2560], W2T, W3T [512 x 64]); the backward pass uses W2 and W3
+// as stored; the weight gradients are X^T dZ1, H1^T dZ2, H2^T dY with the
+// element index as K, so the forward epilogues also write H1 and H2
+// transposed (element index contiguous) and X, dZ and dY get transposed
+// copies.  Transposed buffers have a leading dimension rounded up to 8
+// elements (16-byte rows for the TMA engine).  Weight gradients split the
+// element range over CTAs and add the partials in a fixed order, so a
+// training step is deterministic.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -35,145 +42,14 @@
 
 #include "common.cuh"
 #include "reduce.cuh"
+#include "tc.cuh"
 
 namespace ntg {
 
 namespace mlp {
 
-constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
-constexpr int GT = 128;  // 4 warps
-
-struct GemmArgs {
-  const __nv_bfloat16* A;
-  int64_t lda_m, lda_k;
-  const __nv_bfloat16* B;
-  int64_t ldb_k, ldb_n;
-  float* C;             // fp32 output (row-major, ldc), or split-K partials
-  int64_t ldc;
-  int64_t split_stride; // elements between split-K partial matrices
-  __nv_bfloat16* Cb;    // optional bf16 copy (row-major, ldc)
-  const float* bias;    // optional, per column
-  int relu;
-  int64_t M, N, K, kchunk;
-};
-
-__device__ __forceinline__ unsigned su32(const void* p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
-
-__device__ __forceinline__ void ldm_x4(unsigned (&r)[4], const void* p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(su32(p)));
-}
-__device__ __forceinline__ void ldm_x2(unsigned (&r)[2], const void* p) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(su32(p)));
-}
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__global__ void __launch_bounds__(GT) k_gemm_bf16(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 sA[BM][BK + PAD];
-  __shared__ __align__(16) __nv_bfloat16 sB[BN][BK + PAD];  // n-major, k contiguous
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int wm = warp >> 1, wn = warp & 1;
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-  const int64_t kbeg = (int64_t)blockIdx.z * g.kchunk;
-  int64_t kend = kbeg + g.kchunk;
-  if (kend > g.K) kend = g.K;
-  float acc[2][4][4];
-#pragma unroll
-  for (int a = 0; a < 2; ++a)
-#pragma unroll
-    for (int b = 0; b < 4; ++b)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int64_t k0 = kbeg; k0 < kend; k0 += BK) {
-    // load tiles: BM*BK = 2048 elements each, 16 per thread
-#pragma unroll 4
-    for (int q = 0; q < (BM * BK) / GT; ++q) {
-      const int e = q * GT + tid;
-      // A: walk m fastest when A is column-major (lda_m == 1), else k fastest
-      int mm, kk;
-      if (g.lda_m == 1) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
-      const int64_t gm = m0 + mm, gk = k0 + kk;
-      sA[mm][kk] = (gm < g.M && gk < kend) ? g.A[gm * g.lda_m + gk * g.lda_k] : zero;
-      int nn, kb;
-      if (g.ldb_n == 1) { nn = e % BN; kb = e / BN; } else { kb = e % BK; nn = e / BK; }
-      const int64_t gn = n0 + nn, gkb = k0 + kb;
-      sB[nn][kb] = (gn < g.N && gkb < kend) ? g.B[gkb * g.ldb_k + gn * g.ldb_n] : zero;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < BK; ks += 16) {
-      unsigned af[2][4], bf[4][2];
-#pragma unroll
-      for (int mi = 0; mi < 2; ++mi) ldm_x4(af[mi], &sA[wm * 32 + mi * 16 + (lane & 15)][ks + (lane >> 4) * 8]);
-#pragma unroll
-      for (int ni = 0; ni < 4; ++ni) ldm_x2(bf[ni], &sB[wn * 32 + ni * 8 + (lane & 7)][ks + ((lane >> 3) & 1) * 8]);
-#pragma unroll
-      for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], af[mi], bf[ni]);
-    }
-    __syncthreads();
-  }
-  // epilogue
-  float* C = g.C + (int64_t)blockIdx.z * g.split_stride;
-  const int gr = lane >> 2, gc = (lane & 3) * 2;
-#pragma unroll
-  for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-    for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int64_t row = m0 + wm * 32 + mi * 16 + gr + h * 8;
-        if (row >= g.M) continue;
-#pragma unroll
-        for (int cc = 0; cc < 2; ++cc) {
-          const int64_t col = n0 + wn * 32 + ni * 8 + gc + cc;
-          if (col >= g.N) continue;
-          float v = acc[mi][ni][h * 2 + cc];
-          if (g.bias) v += g.bias[col];
-          if (g.relu) v = v > 0.f ? v : 0.f;
-          if (C) C[row * g.ldc + col] = v;
-          if (g.Cb) g.Cb[row * g.ldc + col] = __float2bfloat16(v);
-        }
-      }
-}
-
-// sum of S split-K partials (fixed order) -> out
-__global__ void k_sum_splits(const float* __restrict__ part, int S, int64_t len, float* __restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int z = 0; z < S; ++z) s += part[(int64_t)z * len + i];
-    out[i] = s;
-  }
-}
-
-// column sums of a row-major [M x N] fp32 matrix, deterministic: block per
-// column chunk, fixed row partition, fixed tree
-__global__ void k_colsum(const float* __restrict__ a, int64_t M, int N, float* __restrict__ out) {
-  __shared__ float red[8][32];
-  const int col = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int rw = threadIdx.x >> 5;  // 8 row lanes
-  float s = 0.f;
-  if (col < N)
-    for (int64_t r = rw; r < M; r += 8) s += a[r * N + col];
-  red[rw][threadIdx.x & 31] = s;
-  __syncthreads();
-  if (rw == 0 && col < N) {
-    float t = 0.f;
-    for (int q = 0; q < 8; ++q) t += red[q][threadIdx.x & 31];
-    out[col] = t;
-  }
-}
-
-// X[m][f*512 + node] = bf16(field_f[m*512 + node] * scale_f), f < nf
+// X[m][f*lx3 + node] = bf16(field_f[m*lx3 + node] * scale_f), f < nhist; the
+// right-hand side last
 struct PrepArgs {
   const float* hist[8];
   const double* b;
@@ -194,47 +70,112 @@ __global__ void k_prep_x(PrepArgs pa, int64_t E, int lx3, __nv_bfloat16* __restr
   }
 }
 
-// dY = (Y - T) * g ; bf16 copy; per-thread squared error sums -> loss
+// T [cols x ldt] = S^T for S [rows x cols] (BF16), 32 x 32 tiles through
+// shared memory (coalesced on both sides)
+__global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ S, int64_t rows, int64_t cols,
+                                 __nv_bfloat16* __restrict__ T, int64_t ldt) {
+  __shared__ __nv_bfloat16 tile[32][34];
+  const int64_t ntc = (cols + 31) / 32, ntr = (rows + 31) / 32;
+  for (int64_t t = blockIdx.x; t < ntc * ntr; t += gridDim.x) {
+    const int64_t r0 = (t / ntc) * 32, c0 = (t % ntc) * 32;
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+      const int64_t r = r0 + q, c = c0 + threadIdx.x;
+      tile[q][threadIdx.x] = (r < rows && c < cols) ? S[r * cols + c] : __float2bfloat16(0.f);
+    }
+    __syncthreads();
+    for (int q = threadIdx.y; q < 32; q += blockDim.y) {
+      const int64_t c = c0 + q, r = r0 + threadIdx.x;
+      if (c < cols && r < rows) T[c * ldt + r] = tile[threadIdx.x][q];
+    }
+    __syncthreads();
+  }
+}
+
+// Activation gradient of a row-major [M x N] block: dZ = dH * (Hact > 0)
+// (no mask when Hact is null).  Writes any of: FP32 dZ, BF16 dZb (both
+// row-major), BF16 dZT (transposed, leading dimension ldt).  A block takes
+// 32 rows; the transposed write goes through shared memory.
+template <int N>
+__global__ void __launch_bounds__(256) k_act_back(const float* __restrict__ dH, const __nv_bfloat16* __restrict__ Hact,
+                                                  int64_t M, float* __restrict__ dZ, __nv_bfloat16* __restrict__ dZb,
+                                                  __nv_bfloat16* __restrict__ dZT, int64_t ldt) {
+  __shared__ __nv_bfloat16 tile[32][N + 2];
+  for (int64_t r0 = (int64_t)blockIdx.x * 32; r0 < M; r0 += (int64_t)gridDim.x * 32) {
+    for (int q = threadIdx.x; q < 32 * N; q += blockDim.x) {
+      const int rr = q / N, c = q - rr * N;
+      const int64_t r = r0 + rr;
+      float v = 0.f;
+      if (r < M) {
+        v = dH[r * N + c];
+        if (Hact && !(__bfloat162float(Hact[r * N + c]) > 0.f)) v = 0.f;
+        if (dZ) dZ[r * N + c] = v;
+        if (dZb) dZb[r * N + c] = __float2bfloat16(v);
+      }
+      tile[rr][c] = __float2bfloat16(v);
+    }
+    __syncthreads();
+    if (dZT) {
+      for (int q = threadIdx.x; q < 32 * N; q += blockDim.x) {
+        const int c = q / 32, rr = q - c * 32;
+        const int64_t r = r0 + rr;
+        if (r < M) dZT[c * ldt + r] = tile[rr][c];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// column sums of a row-major [M x N] FP32 matrix, deterministic: a block per
+// 32 columns, fixed row partition, fixed tree
+__global__ void k_colsum(const float* __restrict__ a, int64_t M, int N, float* __restrict__ out) {
+  __shared__ float red[8][32];
+  const int col = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int rw = threadIdx.x >> 5;
+  float s = 0.f;
+  if (col < N)
+    for (int64_t r = rw; r < M; r += 8) s += a[r * N + col];
+  red[rw][threadIdx.x & 31] = s;
+  __syncthreads();
+  if (rw == 0 && col < N) {
+    float t = 0.f;
+    for (int q = 0; q < 8; ++q) t += red[q][threadIdx.x & 31];
+    out[col] = t;
+  }
+}
+
+// dY = (Y - T) * g (MSE gradient), loss partials
 struct FinLoss {
   __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[1] = acc[0]; }
 };
 __global__ void k_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, int64_t len, float g,
-                            __nv_bfloat16* __restrict__ dYb, float* __restrict__ dY, double* __restrict__ part,
-                            Scalars* sc) {
+                            float* __restrict__ dY, double* __restrict__ part, Scalars* sc) {
   float s = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
     const float d = Y[i] - T[i];
     s += d * d;
-    const float gd = d * g;
-    dY[i] = gd;
-    dYb[i] = __float2bfloat16(gd);
+    dY[i] = d * g;
   }
   double v[1] = {(double)s};
   grid_reduce<1>(v, part, sc, FinLoss());
 }
 
-// The output head: per element e, nh weights Y[e][f]; the guess on the
-// element is sum_f (delta_f0 + Y[e][f]) * h_f (h_0 the newest solution).
-struct HistPtrs {
-  const float* h[8];
-  int nh;
-};
-// D = combined guess (times mult when given, minus T when given)
-__global__ void k_head_diff(const float* __restrict__ Y, HistPtrs hp, int lx3, int64_t n, const float* __restrict__ T,
-                            const float* __restrict__ mult, float* __restrict__ D) {
-  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = l / lx3;
-    float g = 0.f;
-    for (int f = 0; f < hp.nh; ++f) g += ((f == 0 ? 1.f : 0.f) + Y[e * hp.nh + f]) * hp.h[f][l];
-    if (mult) g *= mult[l];
-    D[l] = T ? g - T[l] : g;
-  }
+// D = (x_{k-1} + s Y) * mult, the element-local guess before averaging
+__global__ void k_head(const float* __restrict__ Y, const float* __restrict__ hnew, float s,
+                       const float* __restrict__ mult, int64_t n, float* __restrict__ D) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x)
+    D[l] = (hnew[l] + s * Y[l]) * mult[l];
+}
+// the same in FP64 for the guess itself
+__global__ void k_head64(const float* __restrict__ Y, const float* __restrict__ hnew, double s,
+                         const double* __restrict__ mult, int64_t n, double* __restrict__ out) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x)
+    out[l] = ((double)hnew[l] + s * (double)Y[l]) * mult[l];
 }
 __global__ void k_sub_inplace(float* __restrict__ D, const float* __restrict__ T, int64_t n) {
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x)
     D[l] -= T[l];
 }
-// AD <- ge A D + gl D, loss = sum 0.5 (ge D.AD + gl D.D) (mult-free local sums)
+// AD <- ge A D + gl D, loss = sum 0.5 (ge D.AD + gl D.D) (local sums)
 __global__ void k_energy_grad_field(const float* __restrict__ D, float* __restrict__ AD, int64_t n, float ge, float gl,
                                     double* __restrict__ part, Scalars* sc) {
   float s = 0.f;
@@ -246,108 +187,12 @@ __global__ void k_energy_grad_field(const float* __restrict__ D, float* __restri
   double v[1] = {(double)s};
   grid_reduce<1>(v, part, sc, FinLoss());
 }
-// out = guess * mult (doubles, for the averaging gs)
-__global__ void k_head_combine(const float* __restrict__ Y, HistPtrs hp, int lx3, int64_t n,
-                               const double* __restrict__ mult, double* __restrict__ out) {
-  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = l / lx3;
-    double g = 0.0;
-    for (int f = 0; f < hp.nh; ++f) g += ((f == 0 ? 1.0 : 0.0) + (double)Y[e * hp.nh + f]) * (double)hp.h[f][l];
-    out[l] = g * mult[l];
-  }
-}
-// dY[e][f] = sum over the element's nodes of mult * gG * h_f, gG the
-// (gathered, masked) gradient w.r.t. the assembled guess.  One block per
-// element (grid-stride over elements), fixed-order sums.
-__global__ void __launch_bounds__(128) k_head_grad(const float* __restrict__ gG, const float* __restrict__ mult,
-                                                   HistPtrs hp, int lx3, int64_t E, __nv_bfloat16* __restrict__ dYb,
-                                                   float* __restrict__ dY) {
-  __shared__ float red[8][128];
-  for (int64_t e = blockIdx.x; e < E; e += gridDim.x) {
-    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int q = threadIdx.x; q < lx3; q += blockDim.x) {
-      const int64_t l = e * lx3 + q;
-      const float gd = gG[l] * mult[l];
-      for (int f = 0; f < hp.nh; ++f) acc[f] += gd * hp.h[f][l];
-    }
-    for (int f = 0; f < hp.nh; ++f) red[f][threadIdx.x] = acc[f];
-    __syncthreads();
-    for (int w = 64; w > 0; w >>= 1) {
-      if (threadIdx.x < w)
-        for (int f = 0; f < hp.nh; ++f) red[f][threadIdx.x] += red[f][threadIdx.x + w];
-      __syncthreads();
-    }
-    if (threadIdx.x < hp.nh) {
-      const float v = red[threadIdx.x][0];
-      dY[e * hp.nh + threadIdx.x] = v;
-      dYb[e * hp.nh + threadIdx.x] = __float2bfloat16(v);
-    }
-    __syncthreads();
-  }
-}
-// Mean pooling of the per-element outputs: w[f] = delta_f0 + (1/E) sum_e Y[e][f]
-// (one block, fixed-order per-thread sums and tree).
-__global__ void __launch_bounds__(256) k_pool_weights(const float* __restrict__ Y, int64_t E, int nh,
-                                                      float* __restrict__ w) {
-  __shared__ float red[8][256];
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int64_t e = threadIdx.x; e < E; e += blockDim.x)
-    for (int f = 0; f < nh; ++f) acc[f] += Y[e * nh + f];
-  for (int f = 0; f < nh; ++f) red[f][threadIdx.x] = acc[f];
-  __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int f = 0; f < nh; ++f) red[f][threadIdx.x] += red[f][threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x < nh) w[threadIdx.x] = (threadIdx.x == 0 ? 1.f : 0.f) + red[threadIdx.x][0] / (float)E;
-}
-// out = sum_f w[f] h_f  (continuous: a combination of continuous solutions);
-// D variant: minus T
-__global__ void k_global_combine(const float* __restrict__ w, HistPtrs hp, int64_t n, const float* __restrict__ T,
-                                 float* __restrict__ D, double* __restrict__ out) {
-  float wf[8];
-  for (int f = 0; f < hp.nh; ++f) wf[f] = w[f];
-  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
-    if (out) {
-      double g = 0.0;
-      for (int f = 0; f < hp.nh; ++f) g += (double)wf[f] * (double)hp.h[f][l];
-      out[l] = g;
-    } else {
-      float g = 0.f;
-      for (int f = 0; f < hp.nh; ++f) g += wf[f] * hp.h[f][l];
-      D[l] = g - T[l];
-    }
-  }
-}
-// gw[f] = sum_l gG[l] h_f[l] (FP32 per thread, FP64 across blocks)
-struct FinWeights {
-  double* out;
-  int nh;
-  __device__ void operator()(const double* acc, Scalars*) const {
-    for (int f = 0; f < nh; ++f) out[f] = acc[f];
-  }
-};
-__global__ void k_global_grad(const float* __restrict__ gG, HistPtrs hp, int64_t n, double* __restrict__ part,
-                              Scalars* sc, double* __restrict__ gw) {
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
-    const float gg = gG[l];
-    for (int f = 0; f < hp.nh; ++f) acc[f] += gg * hp.h[f][l];
-  }
-  double v[8];
-#pragma unroll
-  for (int f = 0; f < 8; ++f) v[f] = (double)acc[f];
-  grid_reduce<8>(v, part, sc, FinWeights{gw, hp.nh});
-}
-// every element receives dY[e][f] = gw[f] / E (the adjoint of mean pooling)
-__global__ void k_broadcast_dy(const double* __restrict__ gw, int64_t E, int nh, __nv_bfloat16* __restrict__ dYb,
-                               float* __restrict__ dY) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < E * nh; i += (int64_t)gridDim.x * blockDim.x) {
-    const float v = (float)(gw[i % nh] / (double)E);
-    dY[i] = v;
-    dYb[i] = __float2bfloat16(v);
-  }
+// dY = s * mult * gG (the gradient w.r.t. the nodal output; nodal layout =
+// row-major [E x lx3])
+__global__ void k_head_grad(const float* __restrict__ gG, const float* __restrict__ mult, float s, int64_t n,
+                            float* __restrict__ dY) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x)
+    dY[l] = s * mult[l] * gG[l];
 }
 
 // (a, b) in FP32 per thread, FP64 across blocks -> red[3]
@@ -363,46 +208,43 @@ __global__ void k_dot_f(const float* __restrict__ a, const float* __restrict__ b
   grid_reduce<1>(v, part, sc, FinSlot3());
 }
 
-// dZ = dH * (H > 0), bf16 copy
-__global__ void k_relu_back(const float* __restrict__ dH, const __nv_bfloat16* __restrict__ H, int64_t len,
-                            float* __restrict__ dZ, __nv_bfloat16* __restrict__ dZb) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
-    const float v = __bfloat162float(H[i]) > 0.f ? dH[i] : 0.f;
-    dZ[i] = v;
-    dZb[i] = __float2bfloat16(v);
-  }
-}
-
-// Adam (bias-corrected), FP32 master weights, BF16 copy for the GEMMs
-__global__ void k_adam(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ gr,
-                       float* __restrict__ m1, float* __restrict__ m2, int64_t len, float lr, float b1, float b2,
-                       float c1, float c2, float eps) {
+// Adam (bias-corrected) on FP32 master weights
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ gr, float* __restrict__ m1,
+                       float* __restrict__ m2, int64_t len, float lr, float b1, float b2, float c1, float c2,
+                       float eps) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
     const float gg = gr[i];
     const float a = b1 * m1[i] + (1.f - b1) * gg;
     const float b = b2 * m2[i] + (1.f - b2) * gg * gg;
     m1[i] = a;
     m2[i] = b;
-    const float v = w[i] - lr * (a * c1) / (sqrtf(b * c2) + eps);
-    w[i] = v;
-    if (wb) wb[i] = __float2bfloat16(v);
+    w[i] = w[i] - lr * (a * c1) / (sqrtf(b * c2) + eps);
   }
 }
 
-__global__ void k_f2bf(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = __float2bfloat16(a[i]);
+// BF16 weight copies for the GEMMs: W (as stored, [rows x cols]) and/or its
+// transpose WT [cols x rows]
+__global__ void k_wcopy(const float* __restrict__ W, int64_t rows, int64_t cols, __nv_bfloat16* __restrict__ Wb,
+                        __nv_bfloat16* __restrict__ WT) {
+  const int64_t len = rows * cols;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+    const __nv_bfloat16 v = __float2bfloat16(W[i]);
+    if (Wb) Wb[i] = v;
+    if (WT) {
+      const int64_t r = i / cols, c = i - r * cols;
+      WT[c * rows + r] = v;
+    }
+  }
 }
 
-// target T = (x - x_prev) / s (float; x_prev may be null); history push h = x
-__global__ void k_target(const double* __restrict__ x, const float* __restrict__ xprev, double inv_s, int64_t n,
-                         float* __restrict__ T, float* __restrict__ h) {
+// T = x (float); history push h = x
+__global__ void k_target(const double* __restrict__ x, int64_t n, float* __restrict__ T, float* __restrict__ h) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (T) T[i] = (float)((x[i] - (xprev ? (double)xprev[i] : 0.0)) * inv_s);
+    if (T) T[i] = (float)x[i];
     if (h) h[i] = (float)x[i];
   }
 }
-// sum of squares of a float / double array (RMS scales), deterministic
+// sum of squares, deterministic -> red[2]
 struct FinSlot2 {
   __device__ void operator()(const double* acc, Scalars* sc) const { sc->red[2] = acc[0]; }
 };
@@ -424,26 +266,25 @@ __global__ void k_sumsq(const T* __restrict__ a, int64_t n, double* __restrict__
 struct ntg_guess {
   ntg_plan* plan = nullptr;
   int nhist = 4, H = 64, F = 0, O = 0, lx3 = 0;
-  int64_t E = 0, n = 0;
-  // parameters: flat FP32 [W1 F*H | b1 H | W2 H*H | b2 H | W3 H*O | b3 O]
+  int64_t E = 0, n = 0, ldt = 0;
+  // parameters: flat FP32 [W1 F*H | b1 H | W2 H*H | b2 H | W3 H*O | b3 O], W row-major [in x out]
   int64_t oW1 = 0, ob1 = 0, oW2 = 0, ob2 = 0, oW3 = 0, ob3 = 0, np = 0;
   float *P = nullptr, *G = nullptr, *m1 = nullptr, *m2 = nullptr;
-  __nv_bfloat16* Pb = nullptr;
-  // activations
-  __nv_bfloat16 *X = nullptr, *H1b = nullptr, *H2b = nullptr, *dYb = nullptr, *dZb = nullptr;
+  // BF16 weight copies: forward (transposed) and backward (as stored)
+  __nv_bfloat16 *W1T = nullptr, *W2T = nullptr, *W3T = nullptr, *W2b = nullptr, *W3b = nullptr;
+  // activations (row-major [E x .]) and transposed copies ([. x ldt])
+  __nv_bfloat16 *X = nullptr, *XT = nullptr, *H1b = nullptr, *H2b = nullptr, *H1T = nullptr, *H2T = nullptr;
+  __nv_bfloat16 *dYb = nullptr, *dYT = nullptr, *dZb = nullptr, *dZT = nullptr;
   float *Y = nullptr, *T = nullptr, *dY = nullptr, *dH = nullptr, *dZ = nullptr, *split = nullptr;
+  int64_t split_len = 0;
   float *D = nullptr, *AD = nullptr;  // energy loss: error and its element-local A image
   double tat = 1.0, tt = 1.0;         // (T, A T) and (T, T) of the current target
   int loss_mode = 1;                  // 1: relative energy + L2 (online training); 0: MSE
-  int pool = 1;                       // 1: mean-pooled weights (one combination); 0: per element
-  float* wpool = nullptr;             // pooled weights [8]
-  double* gw = nullptr;               // their gradient [8]
-  int splits = 16;
+  float hscale = 1.f;                 // s_x of the current input (output scale)
   // history ring of solutions (FP32), newest at hist[(head - 1) mod nhist]
   float* hist[8] = {};
   double hrms[8] = {};
   int hcount = 0, head = 0;
-  double* xloc = nullptr;
   ntg::Scalars* sc = nullptr;
   ntg::Scalars* hs = nullptr;  // pinned
   long long t = 0;
@@ -453,122 +294,113 @@ struct ntg_guess {
 using namespace ntg;
 using namespace ntg::mlp;
 
-// the stored solutions, newest first
-static HistPtrs hist_ptrs(const ntg_guess* g) {
-  HistPtrs hp;
-  hp.nh = g->nhist;
-  for (int f = 0; f < g->nhist; ++f) hp.h[f] = g->hist[(g->head - 1 - f + 2 * g->nhist) % g->nhist];
-  for (int f = g->nhist; f < 8; ++f) hp.h[f] = nullptr;
-  return hp;
-}
+static const float* newest(const ntg_guess* g) { return g->hist[(g->head - 1 + g->nhist) % g->nhist]; }
 
 static void guess_free(ntg_guess* g) {
-  dev_free(g->P); dev_free(g->G); dev_free(g->m1); dev_free(g->m2); dev_free(g->Pb);
-  dev_free(g->X); dev_free(g->H1b); dev_free(g->H2b); dev_free(g->dYb); dev_free(g->dZb);
+  dev_free(g->P); dev_free(g->G); dev_free(g->m1); dev_free(g->m2);
+  dev_free(g->W1T); dev_free(g->W2T); dev_free(g->W3T); dev_free(g->W2b); dev_free(g->W3b);
+  dev_free(g->X); dev_free(g->XT); dev_free(g->H1b); dev_free(g->H2b); dev_free(g->H1T); dev_free(g->H2T);
+  dev_free(g->dYb); dev_free(g->dYT); dev_free(g->dZb); dev_free(g->dZT);
   dev_free(g->Y); dev_free(g->T); dev_free(g->dY); dev_free(g->dH); dev_free(g->dZ); dev_free(g->split);
-  dev_free(g->D); dev_free(g->AD); dev_free(g->wpool); dev_free(g->gw);
+  dev_free(g->D); dev_free(g->AD);
   for (int i = 0; i < 8; ++i) dev_free(g->hist[i]);
-  dev_free(g->xloc); dev_free(g->sc);
+  dev_free(g->sc);
   if (g->hs) cudaFreeHost(g->hs);
   g->hs = nullptr;
 }
 
-static int gemm(ntg_guess* g, const __nv_bfloat16* A, int64_t lda_m, int64_t lda_k, const __nv_bfloat16* B,
-                int64_t ldb_k, int64_t ldb_n, float* C, __nv_bfloat16* Cb, const float* bias, int relu, int64_t M,
-                int64_t N, int64_t K, int splits, float* out_after_split) {
+// refresh the BF16 weight copies from the FP32 master weights
+static int refresh_weights(ntg_guess* g) {
   cudaStream_t s = g->plan->stream;
-  GemmArgs a;
-  a.A = A; a.lda_m = lda_m; a.lda_k = lda_k;
-  a.B = B; a.ldb_k = ldb_k; a.ldb_n = ldb_n;
-  a.ldc = N;
-  a.Cb = Cb; a.bias = bias; a.relu = relu;
-  a.M = M; a.N = N; a.K = K;
-  if (splits > 1) {
-    int64_t kc = (K + splits - 1) / splits;
-    kc = (kc + BK - 1) / BK * BK;
-    splits = (int)((K + kc - 1) / kc);
-    a.kchunk = kc;
-    a.C = g->split;
-    a.split_stride = M * N;
-    a.Cb = nullptr; a.bias = nullptr; a.relu = 0;
-  } else {
-    a.kchunk = (K + BK - 1) / BK * BK;
-    a.C = C;
-    a.split_stride = 0;
-    splits = 1;
-  }
-  dim3 grid((unsigned)((N + BN - 1) / BN), (unsigned)((M + BM - 1) / BM), (unsigned)splits);
-  { k_gemm_bf16<<<grid, GT, 0, s>>>(a); NTG_COUNT_LAUNCH(); }
-  if (a.C == g->split) {
-    { k_sum_splits<<<grid_for(M * N, 256), 256, 0, s>>>(g->split, splits, M * N, out_after_split); NTG_COUNT_LAUNCH(); }
-  }
+  const int64_t F = g->F, H = g->H, O = g->O;
+  { k_wcopy<<<grid_for(F * H, 256), 256, 0, s>>>(g->P + g->oW1, F, H, nullptr, g->W1T); NTG_COUNT_LAUNCH(); }
+  { k_wcopy<<<grid_for(H * H, 256), 256, 0, s>>>(g->P + g->oW2, H, H, g->W2b, g->W2T); NTG_COUNT_LAUNCH(); }
+  { k_wcopy<<<grid_for(H * O, 256), 256, 0, s>>>(g->P + g->oW3, H, O, g->W3b, g->W3T); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
 
-// forward on E rows of X -> Y (fp32), keeping H1b/H2b for the backward pass
+// splits of the element range (K) for a weight gradient of M x N outputs:
+// about two CTAs per SM, the partials within the split buffer
+static int wsplits(const ntg_guess* g, int64_t M, int64_t N) {
+  const int64_t bn = N <= 64 ? 64 : (N <= 128 ? 128 : 256);
+  const int64_t tiles = ((M + 127) / 128) * ((N + bn - 1) / bn);
+  int64_t sp = (2 * (int64_t)num_sms() + tiles - 1) / tiles;
+  sp = std::min<int64_t>(sp, g->split_len / (M * N));
+  return (int)std::max<int64_t>(sp, 1);
+}
+
+// forward on E rows of X -> Y (FP32); keeps H1/H2 (and their transposes)
 static int guess_forward(ntg_guess* g, const __nv_bfloat16* X, int64_t E) {
-  const int H = g->H;
-  NTG_TRY(gemm(g, X, g->F, 1, g->Pb + g->oW1, H, 1, nullptr, g->H1b, g->P + g->ob1, 1, E, H, g->F, 1, nullptr));
-  NTG_TRY(gemm(g, g->H1b, H, 1, g->Pb + g->oW2, H, 1, nullptr, g->H2b, g->P + g->ob2, 1, E, H, H, 1, nullptr));
-  NTG_TRY(gemm(g, g->H2b, H, 1, g->Pb + g->oW3, g->O, 1, g->Y, nullptr, g->P + g->ob3, 0, E, g->O, H, 1, nullptr));
+  cudaStream_t s = g->plan->stream;
+  int* err = g->plan->dev_err;
+  const int64_t F = g->F, H = g->H, O = g->O, ldt = g->ldt;
+  NTG_TRY(tc_gemm_bf16(X, F, g->W1T, F, E, H, F, nullptr, 0, g->H1b, H, g->H1T, ldt, g->P + g->ob1, 1, 1, nullptr,
+                       0, err, s));
+  NTG_TRY(tc_gemm_bf16(g->H1b, H, g->W2T, H, E, H, H, nullptr, 0, g->H2b, H, g->H2T, ldt, g->P + g->ob2, 1, 1,
+                       nullptr, 0, err, s));
+  NTG_TRY(tc_gemm_bf16(g->H2b, H, g->W3T, H, E, O, H, g->Y, O, nullptr, 0, nullptr, 0, g->P + g->ob3, 0, 1, nullptr,
+                       0, err, s));
   return NTG_OK;
 }
 
-// loss and gradients into G for targets T (after guess_forward on X).
-// energy != 0 (rows = all elements of the plan): relative element-energy +
-// relative L2 loss, with (T, A T) and (T, T) in g->tat / g->tt.
-static int guess_backward(ntg_guess* g, const __nv_bfloat16* X, const float* T, int64_t E, int energy) {
+// Gradients into G, given dY (FP32, [E x O]) after guess_forward on X; XT
+// (the transpose of X) must be current.
+static int guess_backward(ntg_guess* g, int64_t E) {
   cudaStream_t s = g->plan->stream;
-  const int H = g->H, O = g->O;
-  const int64_t len = E * O;
-  if (energy) {
-    // the guess is the per-element combination C of the stored solutions
-    // (weights delta_f0 + Y[e][f]) averaged over shared nodes and masked:
-    // G = mask(gs(mult C)).  Loss on the assembled error D = G - x, so jumps
-    // between neighbouring elements' weights are paid for; its gradient
-    // flows back through the averaging (adjoint: mult * gs).
-    ntg_plan* p = g->plan;
-    HistPtrs hp = hist_ptrs(g);
-    if (g->pool) {
-      // mean-pooled head: one set of weights, guess = sum_f w_f h_f
-      { k_pool_weights<<<1, 256, 0, s>>>(g->Y, E, g->nhist, g->wpool); NTG_COUNT_LAUNCH(); }
-      { k_global_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->wpool, hp, g->n, T, g->D, nullptr); NTG_COUNT_LAUNCH(); }
-    } else {
-      { k_head_diff<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hp, g->lx3, g->n, nullptr, p->multf, g->D); NTG_COUNT_LAUNCH(); }
-      NTG_TRY(gs_launch_f32(p, g->D, NTG_GS_ADD, s));
-      NTG_TRY(mask_launch_f32(p, g->D, s));
-      { k_sub_inplace<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, T, g->n); NTG_COUNT_LAUNCH(); }
-    }
-    NTG_TRY(ax_launch_f32(p, g->AD, g->D, nullptr, 0, s));
-    const float ge = (float)(2.0 / g->tat), gl = (float)(2.0 / g->tt);
-    // AD <- ge A D + gl D (gradient w.r.t. the assembled guess), loss
-    { k_energy_grad_field<<<grid_for(g->n, 256), 256, 0, s>>>(g->D, g->AD, g->n, ge, gl, p->red_part, g->sc); NTG_COUNT_LAUNCH(); }
-    if (g->pool) {
-      { k_global_grad<<<grid_for(g->n, 256), 256, 0, s>>>(g->AD, hp, g->n, p->red_part, g->sc, g->gw); NTG_COUNT_LAUNCH(); }
-      { k_broadcast_dy<<<grid_for(E * g->nhist, 256), 256, 0, s>>>(g->gw, E, g->nhist, g->dYb, g->dY); NTG_COUNT_LAUNCH(); }
-    } else {
-      NTG_TRY(gs_launch_f32(p, g->AD, NTG_GS_ADD, s));
-      NTG_TRY(mask_launch_f32(p, g->AD, s));
-      int grid = (int)(E < 2048 ? E : 2048);
-      { k_head_grad<<<grid, 128, 0, s>>>(g->AD, p->multf, hp, g->lx3, E, g->dYb, g->dY); NTG_COUNT_LAUNCH(); }
-    }
-  } else {
-    { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T, len, 2.0f / (float)len, g->dYb, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
-  }
-  // layer 3
-  NTG_TRY(gemm(g, g->H2b, 1, H, g->dYb, O, 1, nullptr, nullptr, nullptr, 0, H, O, E, g->splits, g->G + g->oW3));
-  { k_colsum<<<(O + 31) / 32, 256, 0, s>>>(g->dY, E, O, g->G + g->ob3); NTG_COUNT_LAUNCH(); }
-  NTG_TRY(gemm(g, g->dYb, O, 1, g->Pb + g->oW3, 1, O, g->dH, nullptr, nullptr, 0, E, H, O, 1, nullptr));
-  { k_relu_back<<<grid_for(E * H, 256), 256, 0, s>>>(g->dH, g->H2b, E * H, g->dZ, g->dZb); NTG_COUNT_LAUNCH(); }
-  // layer 2
-  NTG_TRY(gemm(g, g->H1b, 1, H, g->dZb, H, 1, nullptr, nullptr, nullptr, 0, H, H, E, g->splits, g->G + g->oW2));
-  { k_colsum<<<(H + 31) / 32, 256, 0, s>>>(g->dZ, E, H, g->G + g->ob2); NTG_COUNT_LAUNCH(); }
-  NTG_TRY(gemm(g, g->dZb, H, 1, g->Pb + g->oW2, 1, H, g->dH, nullptr, nullptr, 0, E, H, H, 1, nullptr));
-  { k_relu_back<<<grid_for(E * H, 256), 256, 0, s>>>(g->dH, g->H1b, E * H, g->dZ, g->dZb); NTG_COUNT_LAUNCH(); }
-  // layer 1
-  NTG_TRY(gemm(g, X, 1, g->F, g->dZb, H, 1, nullptr, nullptr, nullptr, 0, g->F, H, E, g->splits, g->G + g->oW1));
-  { k_colsum<<<(H + 31) / 32, 256, 0, s>>>(g->dZ, E, H, g->G + g->ob1); NTG_COUNT_LAUNCH(); }
+  int* err = g->plan->dev_err;
+  const int64_t F = g->F, H = g->H, O = g->O, ldt = g->ldt;
+  const int ab = (int)std::min<int64_t>((E + 31) / 32, 4096);
+  // dY -> BF16 row-major (A of dH2) and transposed (B of dW3)
+  { k_act_back<512><<<ab, 256, 0, s>>>(g->dY, nullptr, E, nullptr, g->dYb, g->dYT, ldt); NTG_COUNT_LAUNCH(); }
+  { k_colsum<<<(int)((O + 31) / 32), 256, 0, s>>>(g->dY, E, (int)O, g->G + g->ob3); NTG_COUNT_LAUNCH(); }
+  // dW3 [H x O] = H2^T dY
+  NTG_TRY(tc_gemm_bf16(g->H2T, ldt, g->dYT, ldt, H, O, E, g->G + g->oW3, O, nullptr, 0, nullptr, 0, nullptr, 0,
+                       wsplits(g, H, O), g->split, 0, err, s));
+  // dH2 = dY W3^T ; dZ2 = dH2 * (H2 > 0)
+  NTG_TRY(tc_gemm_bf16(g->dYb, O, g->W3b, O, E, H, O, g->dH, H, nullptr, 0, nullptr, 0, nullptr, 0, 1, nullptr, 0,
+                       err, s));
+  { k_act_back<64><<<ab, 256, 0, s>>>(g->dH, g->H2b, E, g->dZ, g->dZb, g->dZT, ldt); NTG_COUNT_LAUNCH(); }
+  { k_colsum<<<(int)((H + 31) / 32), 256, 0, s>>>(g->dZ, E, (int)H, g->G + g->ob2); NTG_COUNT_LAUNCH(); }
+  // dW2 [H x H] = H1^T dZ2
+  NTG_TRY(tc_gemm_bf16(g->H1T, ldt, g->dZT, ldt, H, H, E, g->G + g->oW2, H, nullptr, 0, nullptr, 0, nullptr, 0,
+                       wsplits(g, H, H), g->split, 0, err, s));
+  // dH1 = dZ2 W2^T ; dZ1 = dH1 * (H1 > 0)
+  NTG_TRY(tc_gemm_bf16(g->dZb, H, g->W2b, H, E, H, H, g->dH, H, nullptr, 0, nullptr, 0, nullptr, 0, 1, nullptr, 0,
+                       err, s));
+  { k_act_back<64><<<ab, 256, 0, s>>>(g->dH, g->H1b, E, g->dZ, nullptr, g->dZT, ldt); NTG_COUNT_LAUNCH(); }
+  { k_colsum<<<(int)((H + 31) / 32), 256, 0, s>>>(g->dZ, E, (int)H, g->G + g->ob1); NTG_COUNT_LAUNCH(); }
+  // dW1 [F x H] = X^T dZ1
+  NTG_TRY(tc_gemm_bf16(g->XT, ldt, g->dZT, ldt, F, H, E, g->G + g->oW1, H, nullptr, 0, nullptr, 0, nullptr, 0,
+                       wsplits(g, F, H), g->split, 0, err, s));
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+static int transpose_x(ntg_guess* g, const __nv_bfloat16* X, int64_t E) {
+  const int64_t tiles = ((E + 31) / 32) * ((g->F + 31) / 32);
+  const int grid = (int)std::min<int64_t>(tiles, (int64_t)num_sms() * 8);
+  { k_transpose_bf16<<<grid, dim3(32, 8), 0, g->plan->stream>>>(X, E, g->F, g->XT, g->ldt); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
+// dY of the online loss: the relative energy + L2 error of the assembled
+// guess against the target T (after guess_forward on all elements)
+static int energy_grad(ntg_guess* g) {
+  ntg_plan* p = g->plan;
+  cudaStream_t s = p->stream;
+  const int G = grid_for(g->n, 256);
+  { k_head<<<G, 256, 0, s>>>(g->Y, newest(g), g->hscale, p->multf, g->n, g->D); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(gs_launch_f32(p, g->D, NTG_GS_ADD, s));
+  NTG_TRY(mask_launch_f32(p, g->D, s));
+  { k_sub_inplace<<<G, 256, 0, s>>>(g->D, g->T, g->n); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(ax_launch_f32(p, g->AD, g->D, nullptr, 0, s));
+  const float ge = (float)(2.0 / g->tat), gl = (float)(2.0 / g->tt);
+  { k_energy_grad_field<<<G, 256, 0, s>>>(g->D, g->AD, g->n, ge, gl, p->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(gs_launch_f32(p, g->AD, NTG_GS_ADD, s));
+  NTG_TRY(mask_launch_f32(p, g->AD, s));
+  { k_head_grad<<<G, 256, 0, s>>>(g->AD, p->multf, g->hscale, g->n, g->dY); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
   return NTG_OK;
 }
@@ -577,9 +409,9 @@ static int guess_adam(ntg_guess* g) {
   g->t += 1;
   const float c1 = 1.0f / (1.0f - powf(g->beta1, (float)g->t));
   const float c2 = 1.0f / (1.0f - powf(g->beta2, (float)g->t));
-  { k_adam<<<grid_for(g->np, 256), 256, 0, g->plan->stream>>>(g->P, g->Pb, g->G, g->m1, g->m2, g->np, g->lr, g->beta1, g->beta2, c1, c2, g->eps); NTG_COUNT_LAUNCH(); }
+  { k_adam<<<grid_for(g->np, 256), 256, 0, g->plan->stream>>>(g->P, g->G, g->m1, g->m2, g->np, g->lr, g->beta1, g->beta2, c1, c2, g->eps); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
-  return NTG_OK;
+  return refresh_weights(g);
 }
 
 static int poll_red(ntg_guess* g, int slot, double* out) {
@@ -590,15 +422,29 @@ static int poll_red(ntg_guess* g, int slot, double* out) {
   return NTG_OK;
 }
 
+// the bounded waits of the tensor-core kernels report through the plan's
+// error flag
+static int check_tc_error(ntg_guess* g) {
+  cudaStream_t s = g->plan->stream;
+  NTG_CUDA_TRY(cudaMemcpyAsync(&g->hs->status, g->plan->dev_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NTG_CUDA_TRY(cudaStreamSynchronize(s));
+  if (g->hs->status) {
+    NTG_CUDA_TRY(cudaMemsetAsync(g->plan->dev_err, 0, sizeof(int), s));
+    set_error("learned guess: a tensor-core kernel's bounded wait ran out");
+    return NTG_ERR_CUDA;
+  }
+  return NTG_OK;
+}
+
 // X from the history (newest first) and b, with RMS scalings
-static int build_x(ntg_guess* g, const double* b, double* s_out) {
+static int build_x(ntg_guess* g, const double* b) {
   cudaStream_t s = g->plan->stream;
   double bb = 0;
   { k_sumsq<double><<<grid_for(g->n, 256), 256, 0, s>>>(b, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
   NTG_TRY(poll_red(g, 2, &bb));
   const double sb = sqrt(bb / (double)g->n);
-  const int newest = (g->head - 1 + g->nhist) % g->nhist;
-  double sx = g->hrms[newest];
+  const int nw = (g->head - 1 + g->nhist) % g->nhist;
+  double sx = g->hrms[nw];
   if (!(sx > 0)) sx = 1.0;
   PrepArgs pa;
   pa.nhist = g->nhist;
@@ -611,7 +457,7 @@ static int build_x(ntg_guess* g, const double* b, double* s_out) {
   pa.bscale = (float)(sb > 0 ? 1.0 / sb : 1.0);
   { k_prep_x<<<grid_for(g->E * g->F, 256), 256, 0, s>>>(pa, g->E, g->lx3, g->X); NTG_COUNT_LAUNCH(); }
   NTG_CUDA_TRY(cudaGetLastError());
-  *s_out = sx;
+  g->hscale = (float)sx;
   return NTG_OK;
 }
 
@@ -621,7 +467,9 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
   clear_error();
   NTG_CHECK_ARG(plan && out, "ntg_guess_create: null argument");
   NTG_CHECK_ARG(history >= 1 && history <= 7, "ntg_guess_create: history must be in [1, 7]");
-  NTG_CHECK_ARG(hidden >= 8 && hidden <= 512, "ntg_guess_create: hidden must be in [8, 512]");
+  NTG_CHECK_ARG(hidden == 64, "ntg_guess_create: hidden must be 64");
+  NTG_CHECK_ARG(plan->lx == 8, "ntg_guess_create: the nodal head is built for lx = 8 (512 nodes)");
+  NTG_CHECK_ARG(plan->dev_err, "ntg_guess_create: plan without an error flag");
   *out = nullptr;
   ntg_guess* g = new ntg_guess();
   g->plan = plan;
@@ -629,33 +477,47 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
   g->H = hidden;
   g->lx3 = plan->lx * plan->lx * plan->lx;
   g->F = (history + 1) * g->lx3;
-  g->O = history;  // per-element weights of the stored solutions
+  g->O = g->lx3;  // nodal output head
   g->E = plan->nelv;
   g->n = plan->n;
-  const int64_t F = g->F, H = g->H, O = g->O, E = g->E;
+  g->ldt = (g->E + 7) / 8 * 8;
+  const int64_t F = g->F, H = g->H, O = g->O, E = g->E, ldt = g->ldt;
   g->oW1 = 0; g->ob1 = F * H; g->oW2 = g->ob1 + H; g->ob2 = g->oW2 + H * H; g->oW3 = g->ob2 + H;
   g->ob3 = g->oW3 + H * O; g->np = g->ob3 + O;
   int st = NTG_OK;
   do {
     if ((st = dev_alloc(&g->P, g->np)) || (st = dev_alloc(&g->G, g->np)) || (st = dev_alloc(&g->m1, g->np)) ||
-        (st = dev_alloc(&g->m2, g->np)) || (st = dev_alloc(&g->Pb, g->np)))
+        (st = dev_alloc(&g->m2, g->np)))
       break;
-    if ((st = dev_alloc(&g->X, E * F)) || (st = dev_alloc(&g->H1b, E * H)) || (st = dev_alloc(&g->H2b, E * H)) ||
-        (st = dev_alloc(&g->dYb, E * O)) || (st = dev_alloc(&g->dZb, E * H)) || (st = dev_alloc(&g->Y, E * O)) ||
-        // T, D, AD hold nodal fields (E * lx^3): the target solution, the
-        // combined guess's error and its A image; T also takes E * O raw targets
-        (st = dev_alloc(&g->T, std::max(g->n, E * O))) || (st = dev_alloc(&g->dY, E * O)) ||
-        (st = dev_alloc(&g->dH, E * H)) || (st = dev_alloc(&g->dZ, E * H)) || (st = dev_alloc(&g->D, g->n)) ||
-        (st = dev_alloc(&g->AD, g->n)) || (st = dev_alloc(&g->wpool, 8)) || (st = dev_alloc(&g->gw, 8)))
+    if ((st = dev_alloc(&g->W1T, F * H)) || (st = dev_alloc(&g->W2T, H * H)) || (st = dev_alloc(&g->W3T, H * O)) ||
+        (st = dev_alloc(&g->W2b, H * H)) || (st = dev_alloc(&g->W3b, H * O)))
       break;
-    const int64_t split_len = (int64_t)g->splits * std::max(F * H, H * O);
-    if ((st = dev_alloc(&g->split, split_len))) break;
+    if ((st = dev_alloc(&g->X, E * F)) || (st = dev_alloc(&g->XT, F * ldt)) || (st = dev_alloc(&g->H1b, E * H)) ||
+        (st = dev_alloc(&g->H2b, E * H)) || (st = dev_alloc(&g->H1T, H * ldt)) || (st = dev_alloc(&g->H2T, H * ldt)))
+      break;
+    if ((st = dev_alloc(&g->dYb, E * O)) || (st = dev_alloc(&g->dYT, O * ldt)) || (st = dev_alloc(&g->dZb, E * H)) ||
+        (st = dev_alloc(&g->dZT, H * ldt)))
+      break;
+    // Y, T, dY, D, AD hold nodal fields (E * lx^3 = n) or E * O raw values
+    if ((st = dev_alloc(&g->Y, E * O)) || (st = dev_alloc(&g->T, std::max(g->n, E * O))) ||
+        (st = dev_alloc(&g->dY, E * O)) || (st = dev_alloc(&g->dH, E * H)) || (st = dev_alloc(&g->dZ, E * H)) ||
+        (st = dev_alloc(&g->D, g->n)) || (st = dev_alloc(&g->AD, g->n)))
+      break;
+    g->split_len = (int64_t)1 << 24;  // 64 MB of split-K partials
+    if ((st = dev_alloc(&g->split, g->split_len))) break;
     for (int i = 0; i < history && !st; ++i) st = dev_alloc(&g->hist[i], g->n);
     if (st) break;
-    if ((st = dev_alloc(&g->xloc, g->n)) || (st = dev_alloc(&g->sc, 1))) break;
+    if ((st = dev_alloc(&g->sc, 1))) break;
     if (cudaMemset(g->sc, 0, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
+    // the transposed buffers' padding columns (ldt > E) stay zero
+    if (cudaMemset(g->XT, 0, sizeof(__nv_bfloat16) * F * ldt) != cudaSuccess ||
+        cudaMemset(g->H1T, 0, sizeof(__nv_bfloat16) * H * ldt) != cudaSuccess ||
+        cudaMemset(g->H2T, 0, sizeof(__nv_bfloat16) * H * ldt) != cudaSuccess ||
+        cudaMemset(g->dZT, 0, sizeof(__nv_bfloat16) * H * ldt) != cudaSuccess ||
+        cudaMemset(g->dYT, 0, sizeof(__nv_bfloat16) * O * ldt) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     if (cudaMallocHost(&g->hs, sizeof(Scalars)) != cudaSuccess) { st = NTG_ERR_ALLOC; break; }
-    // He-uniform weights from SplitMix64, zero biases
+    // He-uniform weights from SplitMix64, zero biases; the output layer
+    // starts at zero, so the untrained guess is exactly the newest solution
     std::vector<float> hp(g->np, 0.0f);
     auto fill = [&](int64_t off, int64_t cnt, int64_t fan_in, uint64_t stream_id) {
       const double lim = std::sqrt(6.0 / (double)fan_in);
@@ -670,14 +532,10 @@ int ntg_guess_create(ntg_plan* plan, int history, int hidden, uint64_t seed, ntg
     };
     fill(g->oW1, F * H, F, 11);
     fill(g->oW2, H * H, H, 12);
-    fill(g->oW3, H * O, H, 13);
-    // the output layer starts at zero: the untrained guess is exactly the
-    // newest solution, with no element-to-element jumps
-    for (int64_t i = 0; i < H * O; ++i) hp[g->oW3 + i] = 0.0f;
     if (cudaMemcpy(g->P, hp.data(), sizeof(float) * g->np, cudaMemcpyHostToDevice) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
     cudaMemset(g->m1, 0, sizeof(float) * g->np);
     cudaMemset(g->m2, 0, sizeof(float) * g->np);
-    { k_f2bf<<<grid_for(g->np, 256), 256, 0, plan->stream>>>(g->P, g->Pb, g->np); NTG_COUNT_LAUNCH(); }
+    if ((st = refresh_weights(g))) break;
     if (cudaStreamSynchronize(plan->stream) != cudaSuccess) { st = NTG_ERR_CUDA; break; }
   } while (0);
   if (st) {
@@ -713,8 +571,7 @@ int ntg_guess_params(ntg_guess* g, float* params_d, int set) {
   cudaStream_t s = g->plan->stream;
   if (set) {
     NTG_CUDA_TRY(cudaMemcpyAsync(g->P, params_d, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, s));
-    { k_f2bf<<<grid_for(g->np, 256), 256, 0, s>>>(g->P, g->Pb, g->np); NTG_COUNT_LAUNCH(); }
-    NTG_CUDA_TRY(cudaGetLastError());
+    NTG_TRY(refresh_weights(g));
   } else {
     NTG_CUDA_TRY(cudaMemcpyAsync(params_d, g->P, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, s));
   }
@@ -722,13 +579,29 @@ int ntg_guess_params(ntg_guess* g, float* params_d, int set) {
 }
 
 // Raw network access (rows of X are BF16 bit patterns, row length
-// (history + 1) * lx^3): Y = net(X) for E <= nelv rows.
+// (history + 1) * lx^3, 16-byte aligned): Y = net(X) for E <= nelv rows,
+// [E x lx^3].
 int ntg_guess_forward_raw(ntg_guess* g, const uint16_t* X_d, int64_t E, float* Y_d) {
   clear_error();
   NTG_CHECK_ARG(g && X_d && Y_d && E >= 1 && E <= g->E, "ntg_guess_forward_raw: bad argument");
   NTG_TRY(guess_forward(g, reinterpret_cast<const __nv_bfloat16*>(X_d), E));
   NTG_CUDA_TRY(cudaMemcpyAsync(Y_d, g->Y, sizeof(float) * E * g->O, cudaMemcpyDeviceToDevice, g->plan->stream));
-  return NTG_OK;
+  return check_tc_error(g);
+}
+
+static int raw_step(ntg_guess* g, const uint16_t* X_d, const float* T_d, int64_t E, double* loss, int adam) {
+  const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
+  cudaStream_t s = g->plan->stream;
+  NTG_TRY(guess_forward(g, X, E));
+  NTG_TRY(transpose_x(g, X, E));
+  const int64_t len = E * g->O;
+  { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, T_d, len, 2.0f / (float)len, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(guess_backward(g, E));
+  if (adam) NTG_TRY(guess_adam(g));
+  double sse = 0;
+  NTG_TRY(poll_red(g, 1, &sse));
+  *loss = sse / (double)len;
+  return check_tc_error(g);
 }
 
 // Gradients of the MSE loss mean((net(X) - T)^2) into grad_d (flat, the
@@ -736,13 +609,9 @@ int ntg_guess_forward_raw(ntg_guess* g, const uint16_t* X_d, int64_t E, float* Y
 int ntg_guess_grad_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int64_t E, float* grad_d, double* loss) {
   clear_error();
   NTG_CHECK_ARG(g && X_d && T_d && grad_d && loss && E >= 1 && E <= g->E, "ntg_guess_grad_raw: bad argument");
-  const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
-  NTG_TRY(guess_forward(g, X, E));
-  NTG_TRY(guess_backward(g, X, T_d, E, 0));
+  NTG_TRY(raw_step(g, X_d, T_d, E, loss, 0));
   NTG_CUDA_TRY(cudaMemcpyAsync(grad_d, g->G, sizeof(float) * g->np, cudaMemcpyDeviceToDevice, g->plan->stream));
-  double sse = 0;
-  NTG_TRY(poll_red(g, 1, &sse));
-  *loss = sse / (double)(E * g->O);
+  NTG_CUDA_TRY(cudaStreamSynchronize(g->plan->stream));
   return NTG_OK;
 }
 
@@ -750,14 +619,7 @@ int ntg_guess_grad_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int6
 int ntg_guess_train_raw(ntg_guess* g, const uint16_t* X_d, const float* T_d, int64_t E, double* loss) {
   clear_error();
   NTG_CHECK_ARG(g && X_d && T_d && loss && E >= 1 && E <= g->E, "ntg_guess_train_raw: bad argument");
-  const __nv_bfloat16* X = reinterpret_cast<const __nv_bfloat16*>(X_d);
-  NTG_TRY(guess_forward(g, X, E));
-  NTG_TRY(guess_backward(g, X, T_d, E, 0));
-  NTG_TRY(guess_adam(g));
-  double sse = 0;
-  NTG_TRY(poll_red(g, 1, &sse));
-  *loss = sse / (double)(E * g->O);
-  return NTG_OK;
+  return raw_step(g, X_d, T_d, E, loss, 1);
 }
 
 int ntg_guess_predict(ntg_guess* g, const double* b_d, double* x_d, int* ready) {
@@ -765,19 +627,14 @@ int ntg_guess_predict(ntg_guess* g, const double* b_d, double* x_d, int* ready) 
   NTG_CHECK_ARG(g && b_d && x_d && ready, "ntg_guess_predict: null argument");
   *ready = 0;
   if (g->hcount < g->nhist) return NTG_OK;
-  double sx = 1.0;
-  NTG_TRY(build_x(g, b_d, &sx));
+  NTG_TRY(build_x(g, b_d));
   NTG_TRY(guess_forward(g, g->X, g->E));
   cudaStream_t s = g->plan->stream;
-  // average the element-local prediction over shared nodes, then mask
-  if (g->pool) {
-    { k_pool_weights<<<1, 256, 0, s>>>(g->Y, g->E, g->nhist, g->wpool); NTG_COUNT_LAUNCH(); }
-    { k_global_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->wpool, hist_ptrs(g), g->n, nullptr, nullptr, x_d); NTG_COUNT_LAUNCH(); }
-  } else {
-    { k_head_combine<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, hist_ptrs(g), g->lx3, g->n, g->plan->mult, x_d); NTG_COUNT_LAUNCH(); }
-    NTG_TRY(gs_launch(g->plan, x_d, NTG_GS_ADD, s));
-  }
+  // x_{k-1} + s Y, averaged over shared nodes, then masked
+  { k_head64<<<grid_for(g->n, 256), 256, 0, s>>>(g->Y, newest(g), (double)g->hscale, g->plan->mult, g->n, x_d); NTG_COUNT_LAUNCH(); }
+  NTG_TRY(gs_launch(g->plan, x_d, NTG_GS_ADD, s));
   NTG_TRY(mask_launch(g->plan, x_d, s));
+  NTG_TRY(check_tc_error(g));
   *ready = 1;
   return NTG_OK;
 }
@@ -788,10 +645,9 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
   cudaStream_t s = g->plan->stream;
   double last = -1.0;
   if (g->hcount >= g->nhist && train_steps > 0) {
-    double sx = 1.0;
-    NTG_TRY(build_x(g, b_d, &sx));
-    // target: the solution itself (the head combines stored solutions)
-    { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, nullptr, 1.0, g->n, g->T, nullptr); NTG_COUNT_LAUNCH(); }
+    NTG_TRY(build_x(g, b_d));
+    NTG_TRY(transpose_x(g, g->X, g->E));
+    { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, g->n, g->T, nullptr); NTG_COUNT_LAUNCH(); }
     const int energy = g->loss_mode == 1;
     if (energy) {
       // normalisers of the relative losses: (T, A T) with the element-local
@@ -806,16 +662,23 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
     }
     for (int it = 0; it < train_steps; ++it) {
       NTG_TRY(guess_forward(g, g->X, g->E));
-      NTG_TRY(guess_backward(g, g->X, g->T, g->E, energy));
+      if (energy) {
+        NTG_TRY(energy_grad(g));
+      } else {
+        const int64_t len = g->E * g->O;
+        { k_loss_grad<<<grid_for(len, 256), 256, 0, s>>>(g->Y, g->T, len, 2.0f / (float)len, g->dY, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
+      }
+      NTG_TRY(guess_backward(g, g->E));
       NTG_TRY(guess_adam(g));
     }
     double sse = 0;
     NTG_TRY(poll_red(g, 1, &sse));
     last = energy ? sse : sse / (double)(g->E * g->O);
+    NTG_TRY(check_tc_error(g));
   }
   // push x into the history ring
   float* slot = g->hist[g->head];
-  { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, nullptr, 1.0, g->n, nullptr, slot); NTG_COUNT_LAUNCH(); }
+  { k_target<<<grid_for(g->n, 256), 256, 0, s>>>(x_d, g->n, nullptr, slot); NTG_COUNT_LAUNCH(); }
   double xx = 0;
   { k_sumsq<float><<<grid_for(g->n, 256), 256, 0, s>>>(slot, g->n, g->plan->red_part, g->sc); NTG_COUNT_LAUNCH(); }
   NTG_TRY(poll_red(g, 2, &xx));
@@ -823,13 +686,6 @@ int ntg_guess_observe(ntg_guess* g, const double* b_d, const double* x_d, int tr
   g->head = (g->head + 1) % g->nhist;
   if (g->hcount < g->nhist) g->hcount++;
   if (loss) *loss = last;
-  return NTG_OK;
-}
-
-int ntg_guess_set_head(ntg_guess* g, int pooled) {
-  clear_error();
-  NTG_CHECK_ARG(g, "ntg_guess_set_head: null argument");
-  g->pool = pooled ? 1 : 0;
   return NTG_OK;
 }
 
@@ -844,7 +700,7 @@ int ntg_guess_set_loss(ntg_guess* g, int energy) {
 // ntg_guess_state_len floats [P | Adam m1 | Adam m2 | history ring, slot by
 // slot], the integers {Adam step, ring head, ring count, 0} and the ring's
 // RMS scales (8 doubles).  dir = 0 stores, dir = 1 loads (the BF16 weight
-// copy is rebuilt from P, so a restored network computes bit for bit as
+// copies are rebuilt from P, so a restored network computes bit for bit as
 // the saved one).
 int64_t ntg_guess_state_len(const ntg_guess* g) { return g ? 3 * g->np + (int64_t)g->nhist * g->n : 0; }
 
@@ -870,8 +726,7 @@ int ntg_guess_state(ntg_guess* g, float* buf_d, long long* ints, double* hrms, i
     for (int q = 0; q < 3; ++q) NTG_CUDA_TRY(cudaMemcpyAsync(parts[q], buf_d + q * np, sizeof(float) * np, k, s));
     for (int h = 0; h < g->nhist; ++h)
       NTG_CUDA_TRY(cudaMemcpyAsync(g->hist[h], buf_d + 3 * np + h * n, sizeof(float) * n, k, s));
-    { k_f2bf<<<grid_for(np, 256), 256, 0, s>>>(g->P, g->Pb, np); NTG_COUNT_LAUNCH(); }
-    NTG_CUDA_TRY(cudaGetLastError());
+    NTG_TRY(refresh_weights(g));
     g->t = ints[0];
     g->head = (int)ints[1];
     g->hcount = (int)ints[2];

@@ -41,6 +41,7 @@
 
 #include "common.cuh"
 #include "reduce.cuh"
+#include "schwarz.cuh"
 
 namespace ntg {
 
@@ -108,11 +109,6 @@ __global__ void k_coef_means(const double* __restrict__ h1, double h1c, const do
 // the r and s passes (two each) free of bank conflicts and the tile stride
 // TPER keeps warps that span two elements free as well; the single t pass
 // takes two-way conflicts (no stride choice avoids all three passes).
-// linear (Q1) basis at the GLL nodes, for the coarse level
-struct CoarsePhi {
-  float p[2][NTG_LXMAX];  // p[0][i] = (1 - xi_i) / 2, p[1][i] = (1 + xi_i) / 2
-};
-
 // the reference interval's extended 1D eigenvectors, as output pairs
 template <int LE>
 struct FdmRef {
@@ -714,6 +710,9 @@ struct ntg_schwarz {
   size_t smem_xy = 0, smem_z = 0;
   int mass_term = 0;
   float* dw = nullptr;  // additive diagonal term of the Brinkman mass part (n)
+  // lx = 8: FDM local solves on the tensor cores (schwarz_tc.cu) when on
+  ntg::sw::FdmTc ftc{};
+  int fdm_tc = 0;
 };
 
 using namespace ntg;
@@ -751,6 +750,7 @@ static void schwarz_free(ntg_schwarz* s) {
   dev_free(s->hld); dev_free(s->esc); dev_free(s->hc); dev_free(s->ze);
   for (int d = 0; d < 3; ++d) dev_free(s->cS[d]);
   dev_free(s->clam); dev_free(s->corner); dev_free(s->cwork); dev_free(s->uc); dev_free(s->dw);
+  ntg::sw::fdm_tc_free(&s->ftc);
 }
 
 // Generalised symmetric eigenproblem K s = lam M s (M SPD, n small): with
@@ -1023,7 +1023,11 @@ int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s,
       break;
     case 8:
       timer_start(TM_FDM, s);
-      NTG_TRY(sw::fdm_launch<8>(w, r, s, sc));
+      if (w->fdm_tc)
+        NTG_TRY(sw::fdm_tc_launch(w->ftc, r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
+                                  w->coarse_ready ? w->corner : nullptr, w->ph, p->dev_err, s));
+      else
+        NTG_TRY(sw::fdm_launch<8>(w, r, s, sc));
       timer_stop(TM_FDM, s);
       if (w->coarse_ready) {
         timer_start(TM_CRS, s);
@@ -1087,6 +1091,11 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
     fdm_1d(p, 2.0, 2.0, 2.0, s->Sref.data(), s->lamref.data());
     st = p->lx == 4 ? sw::fdm_prepare<4>(s) : p->lx == 6 ? sw::fdm_prepare<6>(s) : sw::fdm_prepare<8>(s);
     if (st) break;
+    if (p->lx == 8 && p->dev_err) {
+      // prepared, off by default: measured slower than the FP32-core kernel
+      if ((st = sw::fdm_tc_prepare(s->Sref.data(), s->lamref.data(), &s->ftc))) break;
+      s->fdm_tc = 0;
+    }
     st = ntg_schwarz_update(s);
   } while (0);
   dev_free(dl);
@@ -1122,6 +1131,15 @@ int ntg_schwarz_update(ntg_schwarz* s) {
     dev_free(hBa);
   }
   if (s->coarse) return coarse_setup(s);
+  return NTG_OK;
+}
+
+// FDM local solves of lx = 8: 1 = tensor cores, 0 = the FP32-core kernel (default)
+int ntg_schwarz_set_fdm_path(ntg_schwarz* s, int tensor_cores) {
+  clear_error();
+  NTG_CHECK_ARG(s, "ntg_schwarz_set_fdm_path: null argument");
+  NTG_CHECK_ARG(!tensor_cores || s->ftc.img, "ntg_schwarz_set_fdm_path: the tensor-core path needs lx = 8");
+  s->fdm_tc = tensor_cores ? 1 : 0;
   return NTG_OK;
 }
 

@@ -130,8 +130,27 @@ def coarse_apply(m, r, box, h1, h2, mask):
     return P @ (np.linalg.pinv(A) @ rc)
 
 
-def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False):
-    """z = M r for an oracle Mesh `m` built as a box of `box` = (Ex, Ey, Ez)."""
+def plane_operator_bf16(lx):
+    """The in-plane operator of the tensor-core FDM path: K~[(a,b),(f,g)] =
+    bf16(S^[a][f] S^[b][g]) with S^ the reference (h = 2) extended
+    eigenvectors, the product rounded to float32 first (as the kernel's
+    table is built).  Returns (K~ as float64 [LE^2 x LE^2], S^, lam^)."""
+    from oracle import mlp_ref
+    S, lam = ext_1d(lx, 2.0, 2.0, 2.0)
+    LE = lx + 2
+    # index (a, b) -> a + LE b and (f, g) -> f + LE g (a and f fastest)
+    K = np.einsum("af,bg->bagf", S, S).reshape(LE * LE, LE * LE)
+    Kb = mlp_ref.bf16(K.astype(np.float32)).astype(np.float64)
+    return Kb, S, lam
+
+
+def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False, plane_bf16=False):
+    """z = M r for an oracle Mesh `m` built as a box of `box` = (Ex, Ey, Ez).
+
+    plane_bf16: the local solves as the tensor-core path computes them: the
+    reference pair scaled by the element lengths, with the in-plane
+    operator S^ x S^ rounded to BF16 (plane_operator_bf16); the data stay in
+    FP64 here (the kernel's two-term BF16 split carries 16 bits)."""
     Ex, Ey, Ez = box
     lx = m.lx
     N, LE = lx - 1, lx + 2
@@ -140,6 +159,8 @@ def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False):
     G = np.zeros((Ex * N + 1, Ey * N + 1, Ez * N + 1))  # indexed (gx, gy, gz)
     h2e = np.zeros(m.nelv) if h2 is None else np.asarray(h2).reshape(m.nelv, -1).mean(1)
     dims = (Ex, Ey, Ez)
+    if plane_bf16:
+        Kb, Sr, lamr = plane_operator_bf16(lx)
     for e in range(m.nelv):
         c = (e % Ex, (e // Ex) % Ey, e // (Ex * Ey))
         strides = (1, Ex, Ex * Ey)
@@ -165,9 +186,22 @@ def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False):
                     en = ec[0] + Ex * (ec[1] + Ey * ec[2])
                     rext[a, b, cc] = r4[en, loc[2], loc[1], loc[0]]
         Sx, Sy, Sz = Ss
-        t = np.einsum("pa,qb,sc,pqs->abc", Sx, Sy, Sz, rext)
-        t /= h1 * (Ls[0][:, None, None] + Ls[1][None, :, None] + Ls[2][None, None, :]) + h2e[e]
-        zext = np.einsum("ap,bq,cs,pqs->abc", Sx, Sy, Sz, t)
+        if plane_bf16:
+            hx, hy, hz = hl[e]
+            # rext[a, b, c] -> X[(a + LE b), c]
+            X = rext.transpose(1, 0, 2).reshape(LE * LE, LE)
+            Y1 = Kb.T @ X                                   # [(f + LE g), c]
+            y = Y1 @ Sr                                     # [(f g), h]
+            fgl = (4.0 / hx ** 2) * lamr[None, :] + (4.0 / hy ** 2) * lamr[:, None]  # [g, f]
+            den = h1 * (fgl.reshape(-1)[:, None] + (4.0 / hz ** 2) * lamr[None, :]) + h2e[e]
+            z = (8.0 / (hx * hy * hz)) * y / den
+            W1 = z @ Sr.T                                   # [(f g), c']
+            W = Kb @ W1                                     # [(a + LE b), c']
+            zext = W.reshape(LE, LE, LE).transpose(1, 0, 2)
+        else:
+            t = np.einsum("pa,qb,sc,pqs->abc", Sx, Sy, Sz, rext)
+            t /= h1 * (Ls[0][:, None, None] + Ls[1][None, :, None] + Ls[2][None, None, :]) + h2e[e]
+            zext = np.einsum("ap,bq,cs,pqs->abc", Sx, Sy, Sz, t)
         for a in range(LE):
             for b in range(LE):
                 for cc in range(LE):
