@@ -246,11 +246,14 @@ int ntg_schwarz_set_coarse(ntg_schwarz* sw, int enable);
 /* penalisation): z += w D^-1 r with D the assembled diagonal and w the     */
 /* node's mass fraction (h2 B) / D in [0, 1].                               */
 int ntg_schwarz_set_mass_term(ntg_schwarz* sw, int enable);
-/* lx = 8: the FDM local solves' in-plane transforms on the tcgen05 tensor  */
-/* cores (1: one shared 100 x 100 plane operator in BF16, data split into  */
-/* two BF16 terms, FP32 accumulation; the third direction in FP32) or on   */
-/* the FP32 cores (0, the default).  Both are symmetric preconditioners.   */
-int ntg_schwarz_set_fdm_path(ntg_schwarz* sw, int tensor_cores);
+/* FDM local solves: 0 (default) = FP32 cores with even-odd 1D transforms  */
+/* (the reference eigenvectors are symmetric / antisymmetric about the     */
+/* extended interval's centre: half the FMAs); 2 = FP32 cores, full 1D     */
+/* products; 1 = lx = 8 only, the in-plane transforms on the tcgen05       */
+/* tensor cores (one shared 100 x 100 plane operator in BF16, data split   */
+/* into two BF16 terms, FP32 accumulation; the third direction in FP32).   */
+/* All three are symmetric preconditioners.                                */
+int ntg_schwarz_set_fdm_path(ntg_schwarz* sw, int path);
 int ntg_schwarz_destroy(ntg_schwarz* sw);
 /* z = M r (FP32; assembled and masked) */
 int ntg_schwarz_apply(ntg_schwarz* sw, float* z_d, const float* r_d);

@@ -370,10 +370,10 @@ class schwarz_t:
         coarse level's Dirichlet faces after coef_t.set_mask)."""
         check(lib().ntg_schwarz_update(self._h))
 
-    def set_fdm_path(self, tensor_cores: bool = True):
-        """lx = 8: FDM in-plane transforms on the tensor cores or on the FP32
-        cores (the default)."""
-        check(lib().ntg_schwarz_set_fdm_path(self._h, int(bool(tensor_cores))))
+    def set_fdm_path(self, path=0):
+        """FDM local solves: 0 (default) FP32 cores with even-odd transforms,
+        1 tensor cores (lx = 8), 2 FP32 cores with full 1D products."""
+        check(lib().ntg_schwarz_set_fdm_path(self._h, int(path)))
 
     def set_mass_term(self, enable: bool = True):
         """Add w D^-1 r (D the assembled diagonal, w the node's mass fraction):

@@ -33,6 +33,7 @@
 // order, the extended results of the elements whose extended box covers it --
 // so every copy of a shared node is bit-identical without a gather-scatter
 // pass, and no atomics are involved.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -126,6 +127,7 @@ struct FdmCfg {
   static constexpr int TPER = LX == 8 ? 1714 : LX == 6 ? 576 : 257;
   static constexpr int NSC = 8;  // per-element scalars (six used)
   static constexpr int EPB = LX == 4 ? 16 : 8, THREADS = EPB * TPE, MINB = LX == 8 ? 3 : 4;
+  static constexpr int MINB_EO = LX == 8 ? 2 : 3;  // the even-odd form keeps the folded lines in registers
   // coarse restriction partials (8 per thread): in the tile rows' padding
   // (a in [LE, RS), two rows per thread) when it is wide enough, else after the tiles
   static constexpr bool HOLES = 2 * (RS - LE) >= 8;
@@ -195,8 +197,83 @@ __device__ __forceinline__ void fdm_pair_reg(const float* __restrict__ M, const 
   }
 }
 
-template <int LX>
-__global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
+// Even-odd forms of the same transforms.  The reference extended interval
+// is symmetric about its centre, so its eigenvectors alternate between
+// symmetric (f even) and antisymmetric (f odd): S[LE-1-p][f] = (-1)^f S[p][f]
+// (checked on the host before this path is chosen).  Then
+//   forward  y_f = sum_{p<H} S[p][f] (x_p + (-1)^f x_{LE-1-p}),
+//   backward x_p = E_p + O_p, x_{LE-1-p} = E_p - O_p with
+//            E_p = sum_{f even} S[p][f] z_f, O_p = sum_{f odd} S[p][f] z_f,
+// half the FMAs of the full LE x LE products.  Both read the forward pair
+// table M = P (M[fp*2LE + 2p + k] = S[p][2fp + k]) at p < H only.
+template <int LE>
+__device__ __forceinline__ void eo_fold(float2 (&in)[LE]) {  // in[p] <- x_p + x_q, in[q] <- x_p - x_q (q = LE-1-p)
+#pragma unroll
+  for (int p = 0; p < LE / 2; ++p) {
+    const float2 a = in[p], b = in[LE - 1 - p];
+    in[p] = make_float2(a.x + b.x, a.y + b.y);
+    in[LE - 1 - p] = make_float2(a.x - b.x, a.y - b.y);
+  }
+}
+template <int LE, int ST>
+__device__ __forceinline__ void fdm_fwd_eo(const float* __restrict__ M, float2 (&in)[LE], float* d1, float* d2) {
+  constexpr int H = LE / 2;
+  eo_fold<LE>(in);
+#pragma unroll
+  for (int fp = 0; fp < H; ++fp) {
+    const float* row = M + fp * 2 * LE;
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+      const float2 m2 = *reinterpret_cast<const float2*>(row + 2 * p);
+      a0 = __ffma2_rn(dup<LE>(m2.x), in[p], a0);
+      a1 = __ffma2_rn(dup<LE>(m2.y), in[LE - 1 - p], a1);
+    }
+    d1[(2 * fp) * ST] = a0.x;
+    d2[(2 * fp) * ST] = a0.y;
+    d1[(2 * fp + 1) * ST] = a1.x;
+    d2[(2 * fp + 1) * ST] = a1.y;
+  }
+}
+template <int LE>
+__device__ __forceinline__ void fdm_fwd_eo_reg(const float* __restrict__ M, float2 (&in)[LE], float2 (&out)[LE]) {
+  constexpr int H = LE / 2;
+  eo_fold<LE>(in);
+#pragma unroll
+  for (int fp = 0; fp < H; ++fp) {
+    const float* row = M + fp * 2 * LE;
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < H; ++p) {
+      const float2 m2 = *reinterpret_cast<const float2*>(row + 2 * p);
+      a0 = __ffma2_rn(dup<LE>(m2.x), in[p], a0);
+      a1 = __ffma2_rn(dup<LE>(m2.y), in[LE - 1 - p], a1);
+    }
+    out[2 * fp] = a0;
+    out[2 * fp + 1] = a1;
+  }
+}
+template <int LE, int ST>
+__device__ __forceinline__ void fdm_bwd_eo(const float* __restrict__ M, const float2 (&in)[LE], float* d1, float* d2) {
+  constexpr int H = LE / 2;
+#pragma unroll
+  for (int p = 0; p < H; ++p) {
+    float2 e = make_float2(0.f, 0.f), o = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int fp = 0; fp < H; ++fp) {
+      const float2 m2 = *reinterpret_cast<const float2*>(M + fp * 2 * LE + 2 * p);
+      e = __ffma2_rn(dup<LE>(m2.x), in[2 * fp], e);
+      o = __ffma2_rn(dup<LE>(m2.y), in[2 * fp + 1], o);
+    }
+    d1[p * ST] = e.x + o.x;
+    d2[p * ST] = e.y + o.y;
+    d1[(LE - 1 - p) * ST] = e.x - o.x;
+    d2[(LE - 1 - p) * ST] = e.y - o.y;
+  }
+}
+
+template <int LX, bool EO>
+__global__ void __launch_bounds__(FdmCfg<LX>::THREADS, EO ? FdmCfg<LX>::MINB_EO : FdmCfg<LX>::MINB)
     k_fdm(const float* __restrict__ r, float* __restrict__ ze, const float* __restrict__ esc, int Ex, int Ey,
           int Ez, const Scalars* sc, float* __restrict__ corner, CoarsePhi ph,
           const __grid_constant__ FdmRef<LX + 2> R) {
@@ -282,7 +359,8 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + RS * u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[p], l2[p]);
-      fdm_pair<LE, 1>(sP, in, l1, l2);
+      if constexpr (EO) fdm_fwd_eo<LE, 1>(sP, in, l1, l2);
+      else fdm_pair<LE, 1>(sP, in, l1, l2);
     }
     __syncthreads();
     // s forward: lines (a, c) = (u, v) along b
@@ -291,7 +369,8 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[RS * p], l2[RS * p]);
-      fdm_pair<LE, RS>(sP, in, l1, l2);
+      if constexpr (EO) fdm_fwd_eo<LE, RS>(sP, in, l1, l2);
+      else fdm_pair<LE, RS>(sP, in, l1, l2);
     }
     __syncthreads();
     // t forward, scale (c_e / D_e), t back: lines (a, b) = (u, v) along c
@@ -303,13 +382,15 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[PS * p], l2[PS * p]);
       float2 t[LE];
-      fdm_pair_reg<LE>(sP, in, t);
+      if constexpr (EO) fdm_fwd_eo_reg<LE>(sP, in, t);
+      else fdm_pair_reg<LE>(sP, in, t);
 #pragma unroll
       for (int f = 0; f < LE; ++f) {
         const float lf = h1 * sz * slam[f];
         in[f] = make_float2(__fdividef(ce * t[f].x, la1 + lf), __fdividef(ce * t[f].y, la2 + lf));
       }
-      fdm_pair<LE, PS>(sQ, in, l1, l2);
+      if constexpr (EO) fdm_bwd_eo<LE, PS>(sP, in, l1, l2);
+      else fdm_pair<LE, PS>(sQ, in, l1, l2);
     }
     __syncthreads();
     // s back
@@ -318,7 +399,8 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[RS * p], l2[RS * p]);
-      fdm_pair<LE, RS>(sQ, in, l1, l2);
+      if constexpr (EO) fdm_bwd_eo<LE, RS>(sP, in, l1, l2);
+      else fdm_pair<LE, RS>(sQ, in, l1, l2);
     }
     __syncthreads();
     // r back
@@ -327,7 +409,8 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, FdmCfg<LX>::MINB)
       float* l2 = A + RS * u + PS * v2;
 #pragma unroll
       for (int p = 0; p < LE; ++p) in[p] = make_float2(l1[p], l2[p]);
-      fdm_pair<LE, 1>(sQ, in, l1, l2);
+      if constexpr (EO) fdm_bwd_eo<LE, 1>(sP, in, l1, l2);
+      else fdm_pair<LE, 1>(sQ, in, l1, l2);
     }
     __syncthreads();
     // coarse restriction of the element: 8 threads sum the partials in order
@@ -713,6 +796,7 @@ struct ntg_schwarz {
   // lx = 8: FDM local solves on the tensor cores (schwarz_tc.cu) when on
   ntg::sw::FdmTc ftc{};
   int fdm_tc = 0;
+  int fdm_eo = 0;  // even-odd 1D transforms (chosen when the reference eigenvectors have parity)
 };
 
 using namespace ntg;
@@ -925,12 +1009,40 @@ static int coarse_setup(ntg_schwarz* s) {
 namespace ntg {
 namespace sw {
 
+// 1 when the reference eigenvectors have the parity the even-odd
+// transforms rely on: S[LE-1-p][f] = (-1)^f S[p][f]
+inline int fdm_has_parity(const ntg_schwarz* w);
+
+// persistent grid of the selected FP32-core variant: blocks resident on all SMs
+template <int LX>
+int fdm_prepare_grid(ntg_schwarz* w);
+
 template <int LX>
 int fdm_prepare(ntg_schwarz* w) {
   using C = FdmCfg<LX>;
-  NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  return fdm_prepare_grid<LX>(w);
+}
+
+inline int fdm_has_parity(const ntg_schwarz* w) {
+  const int LE = w->LE;
+  double smax = 0.0, dev = 0.0;
+  for (int q = 0; q < LE * LE; ++q) smax = std::max(smax, std::fabs(w->Sref[q]));
+  for (int p = 0; p < LE; ++p)
+    for (int f = 0; f < LE; ++f)
+      dev = std::max(dev, std::fabs(w->Sref[(LE - 1 - p) * LE + f] - ((f & 1) ? -1.0 : 1.0) * w->Sref[p * LE + f]));
+  return dev <= 1e-9 * smax ? 1 : 0;
+}
+
+template <int LX>
+int fdm_prepare_grid(ntg_schwarz* w) {
+  using C = FdmCfg<LX>;
   int per_sm = 0;
-  NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX>, C::THREADS, C::SMEM));
+  if (w->fdm_eo)
+    NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, true>, C::THREADS, C::SMEM));
+  else
+    NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, false>, C::THREADS, C::SMEM));
   const int64_t batches = (w->plan->nelv + C::EPB - 1) / C::EPB;
   const int64_t cap = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);
   w->fdm_grid = (int)(batches < cap ? batches : cap);
@@ -950,8 +1062,12 @@ int fdm_launch(ntg_schwarz* w, const float* r, cudaStream_t s, const Scalars* sc
     }
     R.lam[a] = (float)w->lamref[a];
   }
-  k_fdm<LX><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
-                                                      w->coarse_ready ? w->corner : nullptr, w->ph, R);
+  if (w->fdm_eo)
+    k_fdm<LX, true><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
+                                                             w->coarse_ready ? w->corner : nullptr, w->ph, R);
+  else
+    k_fdm<LX, false><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
+                                                              w->coarse_ready ? w->corner : nullptr, w->ph, R);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
@@ -1089,6 +1205,7 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
     s->Sref.assign((size_t)LE2, 0.0);
     s->lamref.assign((size_t)LE, 0.0);
     fdm_1d(p, 2.0, 2.0, 2.0, s->Sref.data(), s->lamref.data());
+    s->fdm_eo = sw::fdm_has_parity(s);
     st = p->lx == 4 ? sw::fdm_prepare<4>(s) : p->lx == 6 ? sw::fdm_prepare<6>(s) : sw::fdm_prepare<8>(s);
     if (st) break;
     if (p->lx == 8 && p->dev_err) {
@@ -1134,12 +1251,19 @@ int ntg_schwarz_update(ntg_schwarz* s) {
   return NTG_OK;
 }
 
-// FDM local solves of lx = 8: 1 = tensor cores, 0 = the FP32-core kernel (default)
-int ntg_schwarz_set_fdm_path(ntg_schwarz* s, int tensor_cores) {
+// FDM local solves: 0 = FP32 cores, even-odd transforms when the reference
+// eigenvectors have parity (default); 1 = tensor cores (lx = 8); 2 = FP32
+// cores, full 1D products
+int ntg_schwarz_set_fdm_path(ntg_schwarz* s, int path) {
   clear_error();
-  NTG_CHECK_ARG(s, "ntg_schwarz_set_fdm_path: null argument");
-  NTG_CHECK_ARG(!tensor_cores || s->ftc.img, "ntg_schwarz_set_fdm_path: the tensor-core path needs lx = 8");
-  s->fdm_tc = tensor_cores ? 1 : 0;
+  NTG_CHECK_ARG(s && path >= 0 && path <= 2, "ntg_schwarz_set_fdm_path: bad argument");
+  NTG_CHECK_ARG(path != 1 || s->ftc.img, "ntg_schwarz_set_fdm_path: the tensor-core path needs lx = 8");
+  s->fdm_tc = path == 1 ? 1 : 0;
+  if (path != 1) {
+    s->fdm_eo = path == 0 ? sw::fdm_has_parity(s) : 0;
+    const int lx = s->plan->lx;
+    NTG_TRY(lx == 4 ? sw::fdm_prepare_grid<4>(s) : lx == 6 ? sw::fdm_prepare_grid<6>(s) : sw::fdm_prepare_grid<8>(s));
+  }
   return NTG_OK;
 }
 

@@ -18,10 +18,14 @@ def T(a, dev, dtype=torch.float64):
     return torch.from_numpy(np.ascontiguousarray(a)).to(device=dev, dtype=dtype)
 
 
-@pytest.mark.parametrize("shape", [(3, 2, 2, 8, 0.05, 1), (3, 2, 2, 8, 0.05, 0), (2, 3, 2, 4, 0.0, 0),
-                                   (4, 1, 2, 6, 0.05, 0), (5, 3, 2, 8, 0.05, 1)])
+@pytest.mark.parametrize("shape", [(3, 2, 2, 8, 0.05, 1), (3, 2, 2, 8, 0.05, 0), (3, 2, 2, 8, 0.05, 2),
+                                   (2, 3, 2, 4, 0.0, 0), (2, 3, 2, 4, 0.0, 2), (4, 1, 2, 6, 0.05, 0),
+                                   (5, 3, 2, 8, 0.05, 1)])
 def test_schwarz_apply_matches_oracle(pkg, orc, dev, shape):
-    ex, ey, ez, lx, amp, tensor_cores = shape
+    """path 0: FP32 cores, even-odd transforms; 2: FP32 cores, full products;
+    1: tensor cores (lx = 8)."""
+    ex, ey, ez, lx, amp, path = shape
+    tensor_cores = path == 1
     m = orc.build_mesh(ex, ey, ez, lx, amp=amp, seed=2)
     c = pkg.coef_t.box(ex, ey, ez, lx, amp=amp, seed=2, device=dev)
     mask = orc.mask_face_xmax(ex, ey, ez, lx)
@@ -30,8 +34,7 @@ def test_schwarz_apply_matches_oracle(pkg, orc, dev, shape):
     h2 = rng.uniform(0.0, 2.0, m.n)
     c.set_coefs(h1c=0.5, h2=T(h2, dev), ifh2=True)
     sw = pkg.schwarz_t(c)
-    if lx == 8:
-        sw.set_fdm_path(bool(tensor_cores))
+    sw.set_fdm_path(path)
     r = orc.apply_mask_zero(orc.gs_op(m, rng.standard_normal(m.n)) * m.mult, mask).astype(np.float32)
     z = torch.empty(m.n, dtype=torch.float32, device=dev)
     sw.apply(z, T(r, dev, torch.float32))
@@ -43,7 +46,7 @@ def test_schwarz_apply_matches_oracle(pkg, orc, dev, shape):
     assert err <= (1e-4 if tensor_cores else 2e-5), err
     if tensor_cores:
         # against the FP32-core path: the plane operator's BF16 rounding
-        sw.set_fdm_path(False)
+        sw.set_fdm_path(0)
         z32 = torch.empty_like(z)
         sw.apply(z32, T(r, dev, torch.float32))
         torch.cuda.synchronize()
@@ -59,7 +62,7 @@ def test_schwarz_is_symmetric(pkg, orc, dev, tensor_cores):
     c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.05, seed=3, device=dev)
     c.set_coefs(h1c=1.0, ifh2=False)
     sw = pkg.schwarz_t(c)
-    sw.set_fdm_path(bool(tensor_cores))
+    sw.set_fdm_path(int(tensor_cores))
     rng = np.random.default_rng(4)
     u = (orc.gs_op(m, rng.standard_normal(m.n)) * m.mult).astype(np.float32)
     v = (orc.gs_op(m, rng.standard_normal(m.n)) * m.mult).astype(np.float32)
@@ -246,7 +249,7 @@ def test_tensor_core_fdm_keeps_the_iteration_count(pkg, orc, dev):
     its, xs = {}, {}
     for tcore in (1, 0):
         sw = pkg.schwarz_t(c, coarse=True)
-        sw.set_fdm_path(bool(tcore))
+        sw.set_fdm_path(int(tcore))
         ksp = pkg.krylov_solver_factory(c, "cg_mixed", 20000, 1e-10)
         ksp.set_inner(2.2e-4, 1)
         ksp.set_schwarz(sw)
