@@ -212,6 +212,8 @@ int ntg_gs_op_f32(ntg_plan* plan, float* u_d, int op);
 /* bc_list_apply_scalar(bclst, x, n): zero the masked entries
    (sources/adjoint/adjoint_pnpn.f90:726) */
 int ntg_bc_apply_scalar(ntg_plan* plan, double* x_d);
+/* the same for an FP32 field */
+int ntg_bc_apply_scalar_f32(ntg_plan* plan, float* x_d);
 
 /* ---------------------------------------------------------------------- */
 /* pc_t (Jacobi): update() builds 1/gs(diag A) in FP64 and FP32;          */

@@ -75,6 +75,7 @@ SIGNATURES = {
     "ntg_gs_op": (_i, [_vp, _vp, _i]),
     "ntg_gs_op_f32": (_i, [_vp, _vp, _i]),
     "ntg_bc_apply_scalar": (_i, [_vp, _vp]),
+    "ntg_bc_apply_scalar_f32": (_i, [_vp, _vp]),
     "ntg_pc_jacobi_update": (_i, [_vp]),
     "ntg_pc_jacobi_solve": (_i, [_vp, _vp, _vp]),
     "ntg_pc_jacobi_get": (_i, [_vp, _vp]),

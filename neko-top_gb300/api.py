@@ -256,7 +256,10 @@ class ax_helm_t:
 
 
 def bc_list_apply_scalar(coef: coef_t, x):
-    check(lib().ntg_bc_apply_scalar(coef.handle, _ptr(x, n=coef.n, name="x")))
+    if x.dtype == torch.float32:
+        check(lib().ntg_bc_apply_scalar_f32(coef.handle, _ptr(x, torch.float32, coef.n, "x")))
+    else:
+        check(lib().ntg_bc_apply_scalar(coef.handle, _ptr(x, n=coef.n, name="x")))
 
 
 class jacobi_t:

@@ -116,3 +116,10 @@ extern "C" int ntg_bc_apply_scalar(ntg_plan* plan, double* x_d) {
   NTG_CHECK_ARG(plan && x_d, "ntg_bc_apply_scalar: null argument");
   return mask_launch(plan, x_d, plan->stream);
 }
+
+// the same for an FP32 field (the FP32 iteration of the mixed solvers)
+extern "C" int ntg_bc_apply_scalar_f32(ntg_plan* plan, float* x_d) {
+  clear_error();
+  NTG_CHECK_ARG(plan && x_d, "ntg_bc_apply_scalar_f32: null argument");
+  return mask_launch_f32(plan, x_d, plan->stream);
+}

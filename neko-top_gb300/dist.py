@@ -20,6 +20,10 @@ CUDA tensors, gloo for CPU tensors).
   rcb_partition   balanced recursive coordinate bisection of the elements
   DistPCG         Jacobi-PCG in FP64 on the distributed operator, every dot
                   weighted by the global multiplicity
+  GhostSlab, CoarseQ1, DistSchwarz, DistMixedCG
+                  the fast solver sharded: FP32 PCG with FP64 reliable updates
+                  and the two-level Schwarz on slab ranks (ghost planes for
+                  the overlap, a global coarse level; see below)
 
 Determinism: a shared face node has exactly two owning slabs, and the
 exchange adds the partner's partial to the rank's own, a + b on one side and
@@ -42,6 +46,7 @@ from __future__ import annotations
 
 import math
 
+import numpy as np
 import torch
 import torch.distributed as dist
 
@@ -280,6 +285,9 @@ class LibraryOps:
     def ax(self, w, u):
         self._ax.compute(w, u, self.coef)
 
+    def ax32(self, w, u):  # FP32 operator (the library picks it from the dtype)
+        self._ax.compute(w, u, self.coef)
+
     def gs(self, u):
         self._gs.op(u)
 
@@ -289,3 +297,333 @@ class LibraryOps:
     def dinv_local(self):
         self._jac.update()
         return self._jac.dinv()
+
+
+class LibraryGhostOps:
+    """The one-level Schwarz of the CUDA library on a rank's ghosted slab:
+    a coef_t of the slab's element planes plus the ghost planes (a box of
+    ex x ey x planes elements, x fastest), its mask and coefficients set by
+    the caller, and a schwarz_t without the coarse level."""
+
+    def __init__(self, coef, box):
+        from . import api
+        coef.box_dims = tuple(box)
+        self.coef = coef
+        self.sw = api.schwarz_t(coef, coarse=False)
+
+    def update(self):
+        self.sw.update()
+
+    def schwarz(self, z, r):
+        self.sw.apply(z, r)
+
+
+# ---------------------------------------------------------------------------
+# The fast solver sharded: FP32-inner / FP64-refined CG with the two-level
+# overlapping Schwarz preconditioner on slab ranks.
+#
+# Halo.  The Schwarz local solve of an element reads its box extended by one
+# node layer into every neighbour, and its result reaches one node layer
+# into every neighbour.  A slab rank therefore runs the one-level part on its
+# own element planes plus up to two ghost planes on each side, filled from
+# the neighbouring slabs: the first ghost plane's elements contribute to the
+# rank's boundary nodes, and their extended inputs reach into the second
+# ghost plane.  The results on the rank's own nodes then equal the
+# single-rank ones (the second ghost plane's results, which miss their outer
+# inputs, only land on ghost nodes and are dropped).  Every rank must own at
+# least two planes.  The coarse level (Q1 on the element vertices) is global
+# and small: each rank restricts its own elements' residual, the vertex-grid
+# partials are summed over ranks, every rank solves the same separable
+# coarse problem, and each prolongs onto its own elements.
+# ---------------------------------------------------------------------------
+
+
+class GhostSlab:
+    """A slab rank's element planes plus `g` ghost planes on each side
+    (clipped to the box).  fill(u) returns the ghosted array with the ghost
+    planes received from the neighbouring slabs; own is the slice of the
+    rank's elements in it."""
+
+    def __init__(self, part: SlabPartition, lx: int, g: int = 2):
+        if part.world > 1 and part.z1 - part.z0 < g:
+            raise ValueError(f"every slab rank must own at least {g} element planes")
+        self.part, self.g = part, g
+        self.per = part.ex * part.ey * lx ** 3
+        self.gz0, self.gz1 = max(0, part.z0 - g), min(part.ez, part.z1 + g)
+        self.lo, self.hi = part.z0 - self.gz0, self.gz1 - part.z1
+        own_planes = part.z1 - part.z0
+        self.own = slice(self.lo * self.per, (self.lo + own_planes) * self.per)
+        self.n = (self.gz1 - self.gz0) * self.per
+
+    def fill(self, u: torch.Tensor) -> torch.Tensor:
+        p, per, g = self.part, self.per, self.g
+        ug = torch.zeros(self.n, dtype=u.dtype, device=u.device)
+        ug[self.own] = u
+        reqs, bufs = [], []
+        if self.lo:  # my first g planes go down, the lower neighbour's last planes come up
+            s = u[: g * per].contiguous()
+            r = torch.empty(self.lo * per, dtype=u.dtype, device=u.device)
+            reqs += [dist.isend(s, p.rank - 1), dist.irecv(r, p.rank - 1)]
+            bufs.append((slice(0, self.lo * per), r, s))
+        if self.hi:
+            s = u[u.numel() - g * per:].contiguous()
+            r = torch.empty(self.hi * per, dtype=u.dtype, device=u.device)
+            reqs += [dist.isend(s, p.rank + 1), dist.irecv(r, p.rank + 1)]
+            bufs.append((slice(self.n - self.hi * per, self.n), r, s))
+        for q in reqs:
+            q.wait()
+        for sl, r, _ in bufs:
+            ug[sl] = r
+        return ug
+
+
+def element_lengths(x, y, z, lx):
+    """Mean distance between opposite faces of each element along r, s, t
+    (E x 3, float64), from the node coordinates (Neko layout)."""
+    E = x.numel() // lx ** 3
+    X = torch.stack([x, y, z]).to(torch.float64).reshape(3, E, lx, lx, lx)  # (d, e, k, j, i)
+    out = []
+    for a0, a1 in ((np.s_[..., 0], np.s_[..., -1]),
+                   (np.s_[:, :, :, 0, :], np.s_[:, :, :, -1, :]),
+                   (np.s_[:, :, 0, :, :], np.s_[:, :, -1, :, :])):
+        d = X[a1] - X[a0]
+        out.append(torch.sqrt((d * d).sum(0)).reshape(E, -1).mean(1))
+    return torch.stack(out, 1)
+
+
+def _gll_nodes(lx):
+    """GLL points on [-1, 1] (Newton on (1 - x^2) P_N'(x) from Chebyshev points)."""
+    N = lx - 1
+    x = -np.cos(np.pi * np.arange(lx) / N)
+    for _ in range(100):
+        p0, p1 = np.ones(lx), x.copy()
+        for k in range(2, N + 1):
+            p0, p1 = p1, ((2 * k - 1) * x * p1 - (k - 1) * p0) / k
+        dx = (x * p1 - p0) / (lx * p1)
+        x = x - dx
+        if np.abs(dx).max() < 1e-15:
+            break
+    return x
+
+
+class CoarseQ1:
+    """The coarse level of the two-level Schwarz on the global vertex grid of
+    an ex x ey x ez box (the library's coarse part, restated in torch for the
+    sharded solver): restriction P^T (r mult) by the trilinear vertex basis
+    at the GLL nodes, the separable Q1 operator
+      A_c = h1 (Mz x My x Kx + Mz x Ky x Mx + Kz x My x Mx) + h2 Mz x My x Mx
+    from the slab-mean element lengths with Dirichlet vertices removed on
+    fully masked faces, solved by fast diagonalisation (the constant null
+    mode of an all-Neumann box dropped), and prolongation P."""
+
+    def __init__(self, E, slab_lengths, h1, h2, dirichlet, lx, device="cpu", dtype=torch.float32):
+        self.E, self.lx = tuple(E), lx
+        xi = _gll_nodes(lx)
+        phi = np.stack([0.5 * (1 - xi), 0.5 * (1 + xi)])
+        self.phi = torch.tensor(phi, dtype=dtype, device=device)
+        self.S, self.act, lams = [], [], []
+        for d in range(3):
+            hs = np.asarray(slab_lengths[d], dtype=np.float64)
+            nv = E[d] + 1
+            K, M = np.zeros((nv, nv)), np.zeros((nv, nv))
+            for s, h in enumerate(hs):
+                K[s:s + 2, s:s + 2] += np.array([[1.0, -1.0], [-1.0, 1.0]]) / h
+                M[s:s + 2, s:s + 2] += np.array([[2.0, 1.0], [1.0, 2.0]]) * h / 6.0
+            a = np.arange(1 if dirichlet[2 * d] else 0, nv - (1 if dirichlet[2 * d + 1] else 0))
+            Ka, Ma = K[np.ix_(a, a)], M[np.ix_(a, a)]
+            L = np.linalg.cholesky(Ma)
+            Li = np.linalg.inv(L)
+            lam, V = np.linalg.eigh(Li @ Ka @ Li.T)
+            self.S.append(torch.tensor(Li.T @ V, dtype=torch.float64, device=device))
+            self.act.append(torch.tensor(a, device=device))
+            lams.append(lam)
+        D = h1 * (lams[0][None, None, :] + lams[1][None, :, None] + lams[2][:, None, None]) + h2  # (z, y, x)
+        dmin = 1e-6 * (h1 * sum(l.max() for l in lams) + h2)
+        Dinv = np.where(np.abs(D) > dmin, 1.0 / np.where(np.abs(D) > dmin, D, 1.0), 0.0)
+        self.Dinv = torch.tensor(Dinv, dtype=torch.float64, device=device)
+        self.dtype = dtype
+
+    def restrict(self, rw, ecoord):
+        """Vertex-grid partials (ez+1, ey+1, ex+1) of the elements with
+        weighted residual rw (E_own x lx^3, r times mult) at box positions
+        ecoord (E_own x 3: ex, ey, ez)."""
+        lx, ph = self.lx, self.phi
+        r4 = rw.reshape(-1, lx, lx, lx).to(ph.dtype)
+        c = torch.einsum("ekji,ck,bj,ai->ecba", r4, ph, ph, ph).to(torch.float64)  # corners (vz, vy, vx)
+        Ex, Ey, Ez = self.E
+        g = torch.zeros(Ez + 1, Ey + 1, Ex + 1, dtype=torch.float64, device=rw.device)
+        for vz in (0, 1):
+            for vy in (0, 1):
+                for vx in (0, 1):
+                    iz, iy, ix = ecoord[:, 2] + vz, ecoord[:, 1] + vy, ecoord[:, 0] + vx
+                    flat = (iz * (Ey + 1) + iy) * (Ex + 1) + ix
+                    g.view(-1).index_add_(0, flat, c[:, vz, vy, vx])
+        return g
+
+    def solve(self, g):
+        """A_c^+ g on the active vertices (zero on Dirichlet vertices)."""
+        ax, ay, az = self.act
+        Sx, Sy, Sz = self.S
+        r = g[az][:, ay][:, :, ax]
+        t = torch.einsum("zyx,xa,yb,zc->cba", r, Sx, Sy, Sz) * self.Dinv
+        u = torch.einsum("cba,xa,yb,zc->zyx", t, Sx, Sy, Sz)
+        out = torch.zeros_like(g)
+        out[az[:, None, None], ay[None, :, None], ax[None, None, :]] = u
+        return out
+
+    def prolong(self, uc, ecoord):
+        """P uc on the elements at ecoord: (E_own x lx^3)."""
+        lx, ph = self.lx, self.phi.to(torch.float64)
+        corners = torch.stack([torch.stack([torch.stack([uc[ecoord[:, 2] + vz, ecoord[:, 1] + vy, ecoord[:, 0] + vx]
+                                                         for vx in (0, 1)], 1) for vy in (0, 1)], 1)
+                               for vz in (0, 1)], 1)  # (e, vz, vy, vx)
+        z = torch.einsum("ecba,ck,bj,ai->ekji", corners, ph, ph, ph)
+        return z.reshape(-1, lx ** 3).reshape(-1).to(self.dtype)
+
+
+def slab_element_coords(part: SlabPartition, device="cpu"):
+    """Box positions (ex, ey, ez) of a slab rank's elements (x fastest)."""
+    e = torch.arange(part.e0, part.e1, device=device)
+    return torch.stack([e % part.ex, (e // part.ex) % part.ey, e // (part.ex * part.ey)], 1)
+
+
+def slab_mean_lengths(part: SlabPartition, hl: torch.Tensor):
+    """Mean element length of every x-, y- and z-slab of the box, over all
+    ranks (sums and counts all-reduced): the coarse operator's 1D lengths."""
+    coords = slab_element_coords(part, hl.device)
+    out = []
+    for d, nd in enumerate((part.ex, part.ey, part.ez)):
+        s = torch.zeros(2 * nd, dtype=torch.float64, device=hl.device)
+        s[:nd].index_add_(0, coords[:, d], hl[:, d].to(torch.float64))
+        s[nd:].index_add_(0, coords[:, d], torch.ones_like(hl[:, d], dtype=torch.float64))
+        dist.all_reduce(s)
+        out.append((s[:nd] / s[nd:]).cpu().numpy())
+    return out
+
+
+class DistSchwarz:
+    """Two-level overlapping Schwarz across slab ranks (FP32): z = mask(
+    one-level part on the ghosted slab + P A_c^+ P^T (r mult)).  ghost_ops
+    provides schwarz(z_g, r_g): the one-level Schwarz (masked) on the
+    rank's ghosted slab as one box."""
+
+    def __init__(self, part: SlabPartition, ghost: GhostSlab, ghost_ops, ops, mult, coarse: CoarseQ1 = None):
+        self.part, self.ghost, self.gops, self.ops = part, ghost, ghost_ops, ops
+        self.mult32 = mult.to(torch.float32)
+        self.coarse = coarse
+        self.ecoord = slab_element_coords(part, mult.device)
+
+    def apply(self, z, r):
+        rg = self.ghost.fill(r)
+        zg = torch.empty_like(rg)
+        self.gops.schwarz(zg, rg)
+        z.copy_(zg[self.ghost.own])
+        if self.coarse is not None:
+            g = self.coarse.restrict(r * self.mult32, self.ecoord)
+            dist.all_reduce(g)
+            z.add_(self.coarse.prolong(self.coarse.solve(g), self.ecoord))
+            self.ops.mask(z)
+        return z
+
+
+class DistMixedCG:
+    """The fast solver sharded: PCG iterated in FP32 (operator, Schwarz
+    preconditioner, vectors) with FP64 reliable updates -- when the FP32
+    residual has dropped by delta since the last replacement (or reached the
+    tolerance) the FP32 correction is folded into the FP64 solution and the
+    residual recomputed in FP64 -- on the element-partitioned operator.  Dots
+    in FP64, per-rank partials added in rank order.  solve(x, f) as
+    DistPCG.solve; returns (iterations, ||r0||, ||r||, ||f||, FP64
+    residual evaluations)."""
+
+    def __init__(self, ops, iface, precond, mult, rtol=1e-10, abstol=0.0, delta=1e-3, max_iter=20000):
+        self.ops, self.iface, self.pc = ops, iface, precond
+        self.mult = mult
+        self.mult32 = mult.to(torch.float32)
+        self.rtol, self.abstol, self.delta, self.max_iter = rtol, abstol, delta, max_iter
+
+    def apply64(self, w, u):
+        self.ops.ax(w, u)
+        self.ops.gs(w)
+        self.iface.exchange_add(w)
+        self.ops.mask(w)
+        return w
+
+    def apply32(self, w, u):
+        self.ops.ax32(w, u)
+        self.ops.gs(w)
+        self.iface.exchange_add(w)
+        self.ops.mask(w)
+        return w
+
+    def solve(self, x, f):
+        d64 = lambda a, b: dist_dot(a.to(torch.float64), b.to(torch.float64), self.mult)
+        fn = math.sqrt(d64(f, f))
+        tol = max(self.abstol, self.rtol * fn)
+        w64 = torch.empty_like(x)
+        r64 = f - self.apply64(w64, x) if d64(x, x) != 0.0 else f.clone()
+        nrep = 1
+        rn = math.sqrt(d64(r64, r64))
+        r0 = rn
+        it = 0
+        if rn <= tol:
+            return it, r0, rn, fn, nrep
+        r = r64.to(torch.float32)
+        xc = torch.zeros_like(r)
+        z = torch.empty_like(r)
+        w = torch.empty_like(r)
+        self.pc.apply(z, r)
+        p = z.clone()
+        rz = d64(r, z)
+        ref = rn
+        while it < self.max_iter:
+            self.apply32(w, p)
+            alpha = rz / d64(p, w)
+            xc.add_(p, alpha=alpha)
+            r.sub_(w, alpha=alpha)
+            it += 1
+            rr = math.sqrt(d64(r, r))
+            if rr <= self.delta * ref or rr <= tol:
+                # reliable update: fold the correction into x, FP64 residual
+                x.add_(xc.to(torch.float64))
+                xc.zero_()
+                r64 = f - self.apply64(w64, x)
+                nrep += 1
+                rn = math.sqrt(d64(r64, r64))
+                if rn <= tol:
+                    break
+                r = r64.to(torch.float32)
+                ref = rn
+            self.pc.apply(z, r)
+            rz_new = d64(r, z)
+            p.mul_(rz_new / rz).add_(z)
+            rz = rz_new
+        return it, r0, rn, fn, nrep
+
+
+def dirichlet_faces_dist(part: SlabPartition, mask_local, lx: int, device="cpu"):
+    """(x-, x+, y-, y+, z-, z+): a box face is Dirichlet for the coarse level
+    when all its local nodes are masked, counted over every rank's own
+    elements (mask_local: the rank's 1-based Dirichlet indices; device: where
+    the process group's collectives run)."""
+    N, l3 = lx - 1, lx ** 3
+    cnt = torch.zeros(6, dtype=torch.float64)
+    if mask_local is not None and len(mask_local):
+        l = torch.as_tensor(np.asarray(mask_local, dtype=np.int64) - 1)
+        e = l // l3 + part.e0
+        q = l % l3
+        idx = (q % lx, (q // lx) % lx, q // (lx * lx))
+        c = (e % part.ex, (e // part.ex) % part.ey, e // (part.ex * part.ey))
+        E = (part.ex, part.ey, part.ez)
+        for d in range(3):
+            cnt[2 * d] = float(((idx[d] == 0) & (c[d] == 0)).sum())
+            cnt[2 * d + 1] = float(((idx[d] == N) & (c[d] == E[d] - 1)).sum())
+    cnt = cnt.to(device)
+    dist.all_reduce(cnt)
+    cnt = cnt.cpu()
+    E = (part.ex, part.ey, part.ez)
+    out = []
+    for d in range(3):
+        face = E[(d + 1) % 3] * E[(d + 2) % 3] * lx * lx
+        out += [bool(cnt[2 * d] == face), bool(cnt[2 * d + 1] == face)]
+    return out
