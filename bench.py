@@ -251,6 +251,12 @@ SEQUENCES = {
                     "x=8; 400 solves to 1e-10, online training on 1-200, evaluation on 201-400"),
 }
 DESIGN_EVERY = 20  # the design field moves every 20 solves
+GUESS_DESC = {
+    "learned_only": "the learned network's guess as the initial guess, behind the zero-guess guard",
+    "learned": "the learned network's guess as an extra direction of Neko's residual projection, L={L}",
+    "projection": "Neko's residual projection, L={L}",
+    "zero": "zero initial guess",
+}
 
 
 class SequenceCase:
@@ -344,8 +350,12 @@ def run_headline_sequence(args, ws, rank, local):
         assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), (t, mon)
         return x, mon, used
 
-    # training half and warm-up
+    # training half and warm-up; the network as it enters the design window
+    # of the timed solves is kept for the comparison runs
+    net_snap = None
     for t in range(t0):
+        if t == last_change(t0) and seq.net is not None:
+            net_snap = seq.net.state()
         x, mon, used = solve(t, case.rhs(t))
         (its_train if t < ntrain else its_eval).append(mon.iter)
         if t >= ntrain:
@@ -436,53 +446,61 @@ def run_headline_sequence(args, ws, rank, local):
 
     # comparison modes on the same timed solves (same design window)
     def window_run(guess, method="cg_mixed", pc_=pc, delta_=delta, seed_from=None, nt=K):
+        """The same K solves with another guess mode, timed the same way
+        (one bracket of CUDA events around all of them, design updates
+        included).  Projection modes replay the design window from its
+        start; a learned mode starts from the trained network as it was at
+        the window's start."""
         case.set_design(last_change(t0))
         s2 = new_seq(guess, method, pc_, delta_)
+        s2.training = False
+        if s2.net is not None:
+            s2.net.load_state(net_snap)
         start = last_change(t0)
-        if guess in ("zero",) or method == "cg":
+        if guess == "zero" or method == "cg":
             start = t0
         if seed_from is not None:
             for t in range(last_change(t0), t0):
                 s2.record(case.rhs(t), seed_from[t])
         for t in range(start, t0):
             s2.solve(case.rhs(t))
-        its, secs, xs = [], [], []
+        fs2 = [case.rhs(t) for t in range(t0, t0 + nt)]
+        chis2 = {t: case.chi(t) for t in range(t0, t0 + nt) if t % DESIGN_EVERY == 0}
+        torch.cuda.synchronize()
+        mons2, xs = [], []
+        a, b = ev(), ev()
+        a.record()
         for q, t in enumerate(range(t0, t0 + nt)):
             if t % DESIGN_EVERY == 0:
-                case.set_design(t)
+                case.set_design(t, chis2[t])
                 s2.coefficients_changed()
-            f = case.rhs(t)
-            torch.cuda.synchronize()
-            a, b = ev(), ev()
-            a.record()
-            x, mon, used, fn = s2.solve(f)
-            b.record()
-            torch.cuda.synchronize()
-            assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), (guess, t, mon)
-            its.append(mon.iter)
-            secs.append(a.elapsed_time(b) / 1e3)
+            x, mon, used, fn = s2.solve(fs2[q])
+            mons2.append((mon, fn))
             if method == "cg":
                 xs.append(x.clone())
-        del s2
+        b.record()
+        torch.cuda.synchronize()
+        for mon, fn in mons2:
+            assert mon.status == pkg.NTG_OK and mon.res_final <= RTOL * fn * (1 + 1e-9), (guess, mon)
+        del s2, fs2
         torch.cuda.empty_cache()
-        return its, secs, xs
+        return [m.iter for m, _ in mons2], a.elapsed_time(b) / 1e3 / nt, xs
 
     extra = {}
     t_ours = t_timed / K
     if not args.no_compare:
-        for g in ("projection", "zero"):
-            if g == mode:
+        for g in ("learned_only", "learned", "projection", "zero"):
+            if g == mode or (g.startswith("learned") and net_snap is None):
                 continue
-            its, secs, _ = window_run(g)
-            extra[g] = {"iters_mean": round(statistics.mean(its), 2), "s_per_solve": round(statistics.mean(secs), 5)}
+            its, sec, _ = window_run(g)
+            extra[g] = {"iters_mean": round(statistics.mean(its), 2), "s_per_solve": round(sec, 5)}
     # the plain FP64 drop-in (Jacobi-PCG + Neko's projection, L = 20) on the
     # first solves of the timed window, its basis seeded with this design
     # window's earlier solutions
     fp64 = None
     if args.fp64_sample > 0:
-        its, secs, xs = window_run("projection", "cg", "jacobi", None, seed_from=keep, nt=args.fp64_sample)
+        its, t64, xs = window_run("projection", "cg", "jacobi", None, seed_from=keep, nt=args.fp64_sample)
         errs = [float(torch.linalg.norm(keep[t0 + q] - xs[q]) / torch.linalg.norm(xs[q])) for q in range(len(xs))]
-        t64 = statistics.mean(secs)
         ours_same = statistics.mean(float(m[0].iter) for m in mons[:len(xs)])
         fp64 = {"method": "FP64 Jacobi-PCG + residual projection (L=%d), the plain drop-in" % args.proj_l,
                 "s_per_solve": round(t64, 4), "iters_mean": round(statistics.mean(its), 1), "solves": len(xs),
@@ -543,7 +561,7 @@ def run_headline_sequence(args, ws, rank, local):
         "data": "synthetic (seeded generators; no dataset)",
         "config": {"workload": f"{args.config_seq} sequence: {case.cfg['desc']}", "n_local_dofs": n,
                    "n_unique_dofs": coef.nu,
-                   "method": f"guess '{mode}' (learned network inside Neko's residual projection, L={args.proj_l}) + "
+                   "method": f"guess '{mode}' ({GUESS_DESC[mode].format(L=args.proj_l)}) + "
                              f"cg_mixed (FP32 PCG, {pc} preconditioner, FP64 reliable updates at delta={delta:g})",
                    "step": f"one solve of the evaluation half to 1e-10 (solves {t0 + 1}-{t0 + K} of {nsol}; "
                            f"{ntrain} training solves and {W} warm-up solves before)",
@@ -1354,8 +1372,9 @@ def main(argv=None):
                    help="time the FP64 terms either side of each solve (residuals, advection, forcing)")
     p.add_argument("--seq-modes", default="zero,projection,learned,learned_only",
                    help="initial-guess modes of --sequence (comma separated)")
-    p.add_argument("--guess", default="learned", choices=["zero", "projection", "learned", "learned_only"],
-                   help="initial-guess mode of the headline sequence")
+    p.add_argument("--guess", default="learned_only", choices=["zero", "projection", "learned", "learned_only"],
+                   help="initial-guess mode of the headline sequence (learned_only: the network's guess as x0, "
+                        "behind the zero-guess guard; learned: the guess as an extra projection direction)")
     p.add_argument("--train-steps", type=int, default=30, help="Adam steps per training solve")
     p.add_argument("--short-eval", action="store_true",
                    help="headline sequence: skip the untimed rest of the evaluation half")

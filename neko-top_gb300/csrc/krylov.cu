@@ -622,6 +622,7 @@ struct ntg_ksp {
   int inner_max_iter = 400;
   int check_every = 16;
   int guess_guard = 0;
+  int ax_ready = 0;  // the guard left A x0 (FP64, assembled, masked) in v64.w for this solve
   ntg_schwarz* sw = nullptr;  // explicit FP32 preconditioner of the cg_mixed / gmres iterations
   int restart = 30;            // gmres restart length
   ntg::GmresWork* gm = nullptr;
@@ -795,7 +796,7 @@ static int ksp_solve_mixed_ru(ntg_ksp* k, double* x, const double* f, ntg_monito
   hs->delta = k->inner_rtol;
   NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
   if (xx != 0.0) {
-    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    if (!k->ax_ready) NTG_TRY(op_apply(p, k->v64.w, x, s));  // else the guess guard's A x0 is in v64.w
     fpax++;
   }
   float* y32 = k->din;
@@ -895,7 +896,7 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
   hs->delta = k->inner_rtol;
   NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
   if (xx != 0.0) {
-    NTG_TRY(op_apply(p, k->v64.w, x, s));
+    if (!k->ax_ready) NTG_TRY(op_apply(p, k->v64.w, x, s));  // else the guess guard's A x0 is in v64.w
     fpax++;
   }
   float* y32 = k->din;
@@ -1154,6 +1155,8 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
       if (!(ksp->hs->rr <= ksp->hs->ff)) {
         NTG_CUDA_TRY(cudaMemsetAsync(x_d, 0, sizeof(double) * p->n, s));
         rejected = 1;
+      } else {
+        ksp->ax_ready = 1;  // the mixed CG reuses this A x0 for its initial residual
       }
     }
   }
@@ -1175,6 +1178,7 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
     mon->guess_rejected = rejected;
     if (rejected) mon->fp64_ax += 1;
   }
+  ksp->ax_ready = 0;
   return st;
 }
 

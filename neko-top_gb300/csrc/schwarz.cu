@@ -881,6 +881,40 @@ static void gen_eig(int n, const std::vector<double>& K, const std::vector<doubl
   lam = w;
 }
 
+// Order the reference eigenpairs by parity: the interval is symmetric about
+// its centre, so each eigenvector (distinct eigenvalues) is symmetric or
+// antisymmetric; put the symmetric ones at even positions and the
+// antisymmetric ones at odd positions, each group by ascending eigenvalue,
+// as the even-odd transforms expect.  A reordering of eigenpairs leaves the
+// local solve unchanged.  Left as is when the split is not half and half.
+static void parity_order(int LE, std::vector<double>& S, std::vector<double>& lam) {
+  double smax = 0.0;
+  for (double v : S) smax = std::max(smax, std::fabs(v));
+  std::vector<int> sym, anti;
+  for (int f = 0; f < LE; ++f) {
+    double ds = 0.0, da = 0.0;
+    for (int p = 0; p < LE; ++p) {
+      ds = std::max(ds, std::fabs(S[(LE - 1 - p) * LE + f] - S[p * LE + f]));
+      da = std::max(da, std::fabs(S[(LE - 1 - p) * LE + f] + S[p * LE + f]));
+    }
+    if (ds <= 1e-9 * smax) sym.push_back(f);
+    else if (da <= 1e-9 * smax) anti.push_back(f);
+    else return;
+  }
+  if ((int)sym.size() != LE / 2 || (int)anti.size() != LE / 2) return;
+  auto by_lam = [&](int a, int b) { return lam[a] < lam[b]; };
+  std::sort(sym.begin(), sym.end(), by_lam);
+  std::sort(anti.begin(), anti.end(), by_lam);
+  std::vector<double> S2(S.size()), l2(lam.size());
+  for (int q = 0; q < LE; ++q) {
+    const int f = (q & 1) ? anti[q / 2] : sym[q / 2];
+    l2[q] = lam[f];
+    for (int p = 0; p < LE; ++p) S2[p * LE + q] = S[p * LE + f];
+  }
+  S.swap(S2);
+  lam.swap(l2);
+}
+
 // (Re)build the coarse level: Dirichlet faces from the plan's mask, slab
 // lengths, 1D operators and their eigenvectors, h1/h2 means of the element means.
 static int coarse_setup(ntg_schwarz* s) {
@@ -1205,6 +1239,7 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
     s->Sref.assign((size_t)LE2, 0.0);
     s->lamref.assign((size_t)LE, 0.0);
     fdm_1d(p, 2.0, 2.0, 2.0, s->Sref.data(), s->lamref.data());
+    parity_order(LE, s->Sref, s->lamref);
     s->fdm_eo = sw::fdm_has_parity(s);
     st = p->lx == 4 ? sw::fdm_prepare<4>(s) : p->lx == 6 ? sw::fdm_prepare<6>(s) : sw::fdm_prepare<8>(s);
     if (st) break;
