@@ -148,12 +148,13 @@ def measured_traffic(kernel, n, ncoef):
     (profiles/traffic.json), scaled to n local DOFs; None when the capture
     was taken with a different coefficient set."""
     try:
-        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))[kernel]
+        tab = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
     except Exception:
         return None
-    if t.get("coefficients", 0) != ncoef:
-        return None
-    return int(round(t["bytes_per_launch"] * n / t["n_local_dofs"]))
+    for key, t in tab.items():
+        if isinstance(t, dict) and key.split("/")[0] == kernel and t.get("coefficients", 0) == ncoef:
+            return int(round(t["bytes_per_launch"] * n / t["n_local_dofs"]))
+    return None
 
 
 def peaks():
@@ -226,7 +227,9 @@ def run_kernels_only(args, pkg, coef, f, dev):
         pkg.gs_t(coef).op(w)
     ksp = pkg.krylov_solver_factory(coef, "cg_mixed", 24, RTOL)
     if args.pc in ("schwarz", "schwarz2"):
-        ksp.set_schwarz(pkg.schwarz_t(coef, coarse=args.pc == "schwarz2"))
+        sw = pkg.schwarz_t(coef, coarse=args.pc == "schwarz2")
+        sw.set_fdm_path(args.fdm_path)
+        ksp.set_schwarz(sw)
     x = torch.zeros(n, dtype=torch.float64, device=dev)
     mon = ksp.solve(x, f)
     torch.cuda.synchronize()
@@ -536,7 +539,9 @@ def run_headline_sequence(args, ws, rank, local):
                     "achieved": round(b_fdm / (fdm["avg_us"] * 1e-6) / 1e9, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                     "frac": round(b_fdm / (fdm["avg_us"] * 1e-6) / 1e9 / pk["hbm_gbs"], 4), "peak_source": pk_kind,
                     "bytes_per_launch": b_fdm, "avg_us": fdm["avg_us"],
-                    "traffic": measured_traffic("k_fdm", n, 0)}
+                    "traffic": measured_traffic("k_fdm", n, 0),
+                    "algorithmic_note": "4 B per local DOF of r read + (lx+2)^3 x 4 B per element of extended results "
+                                        "written + 6 scalars per element"}
     ax64 = ktimes.get("ax_fp64")
     t_k64 = ax64["avg_us"] * 1e-6 if ax64 else ax["fp64_s"]
     roof64 = {"kernel": "k_ax_helm<double,8> (FP64 Ax: residual replacements, projection)", "bound": "fp64",
@@ -1348,6 +1353,8 @@ def main(argv=None):
                         "sequences: 1e-3 with schwarz2)")
     p.add_argument("--pc", choices=["auto", "jacobi", "schwarz", "schwarz2"], default="auto",
                    help="FP32 preconditioner of cg_mixed (auto: two-level Schwarz for Poisson, Jacobi for Brinkman)")
+    p.add_argument("--fdm-path", type=int, default=0, choices=[0, 1, 2],
+                   help="Schwarz FDM kernel: 0 FP32 even-odd (default), 1 tensor cores, 2 FP32 full products")
     p.add_argument("--mass-term", action="store_true",
                    help="Schwarz: additive diagonal term for the Brinkman mass part")
     p.add_argument("--inner-rtol", type=float, default=1e-4)

@@ -94,6 +94,7 @@ class coef_t:
         self.nelv, self.lx, self.n, self.nu, self.nshared = ne.value, l.value, nn.value, nu.value, nsh.value
         self.device = x.device
         self.mask = None
+        self.x, self.y, self.z, self.gid = x, y, z, glb_ids
         self._xyz = (x, y, z)  # for the derivative metrics, derived on first use
         self._metrics = False
 

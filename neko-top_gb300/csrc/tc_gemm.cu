@@ -148,6 +148,40 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int q = 0; q < 16; ++q) v[q] = 0.f;
     }
     if (!good || row >= M) continue;
+    // whole 16-column chunks go out as 16-byte stores (a thread owns a row)
+    const int64_t col0 = n0 + c;
+    if (!ep.split && col0 + 16 <= N && ((!ep.C || (ep.ldc % 4 == 0 && (reinterpret_cast<uintptr_t>(ep.C) & 15) == 0)) &&
+                                                   (!ep.Cb || (ep.ldcb % 8 == 0 && (reinterpret_cast<uintptr_t>(ep.Cb) & 15) == 0)))) {
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float x = v[q];
+        if (ep.bias) x += ep.bias[col0 + q];
+        if (ep.relu) x = x > 0.f ? x : 0.f;
+        v[q] = x;
+      }
+      if (ep.C) {
+        float4* dst = reinterpret_cast<float4*>(ep.C + row * ep.ldc + col0);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+      if (ep.Cb) {
+        uint4 pk[2];
+        uint32_t* w = reinterpret_cast<uint32_t*>(pk);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * q], v[2 * q + 1]);
+          w[q] = *reinterpret_cast<const uint32_t*>(&h2);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(ep.Cb + row * ep.ldcb + col0);
+        dst[0] = pk[0];
+        dst[1] = pk[1];
+      }
+      if (ep.CbT) {  // consecutive lanes hold consecutive rows: coalesced per column
+#pragma unroll
+        for (int q = 0; q < 16; ++q) ep.CbT[(col0 + q) * ep.ldt + row] = __float2bfloat16(v[q]);
+      }
+      continue;
+    }
 #pragma unroll
     for (int q = 0; q < 16; ++q) {
       const int64_t col = n0 + c + q;
