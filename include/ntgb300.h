@@ -226,15 +226,48 @@ int ntg_pc_jacobi_solve(ntg_plan* plan, double* z_d, const double* r_d);
 int ntg_pc_jacobi_get(const ntg_plan* plan, double* dinv_d);
 
 /* ---------------------------------------------------------------------- */
+/* Meshes from Neko's binary .nmsh files (the reference's cases load their  */
+/* meshes as "mesh_file": "*.nmsh", e.g. examples/brinkman_term/            */
+/* brinkman_term.case:4).  Host buffers; vertices in tensor corner order    */
+/* (v = i + 2j + 4k; the file stores each layer cyclically); zones as      */
+/* stored, 9 int32 each (e, f, p_e, p_f, pt_ids[4], type; f 1-based: r-,   */
+/* r+, s-, s+, t-, t+; labeled zones, type 7, carry the label in p_f);     */
+/* curves as stored (element, 12 x 5 float64, 12 int32 types).  nv = 8 for */
+/* gdim 3, 4 for gdim 2.                                                     */
+/* ---------------------------------------------------------------------- */
+int ntg_nmsh_info(const char* path, int32_t* nelv, int32_t* gdim, int32_t* nzones, int32_t* ncurves);
+/* el_idx: nelv; v_idx: nelv x nv; xyz: nelv x nv x 3; zones: nzones x 9;  */
+/* curve_el: ncurves; curve_data: ncurves x 60; curve_type: ncurves x 12   */
+int ntg_nmsh_read(const char* path, int32_t* el_idx, int32_t* v_idx, double* xyz, int32_t* zones,
+                  int32_t* curve_el, double* curve_data, int32_t* curve_type);
+int ntg_nmsh_write(const char* path, int32_t nelv, int32_t gdim, const int32_t* el_idx, const int32_t* v_idx,
+                   const double* xyz, int32_t nzones, const int32_t* zones, int32_t ncurves,
+                   const int32_t* curve_el, const double* curve_data, const int32_t* curve_type);
+/* GLL node coordinates (x fastest per element) of straight-sided hexahedra */
+/* from their tensor-ordered vertices (xyz_d: device, nelv x 8 x 3)         */
+int ntg_nodes_from_vertices(int64_t nelv, int lx, const double* xyz_d, double* x_d, double* y_d, double* z_d,
+                            void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Overlapping additive Schwarz preconditioner in FP32 (fast-diagonalisation */
 /* local solves on each element extended by one node layer), the one-level */
 /* part of the Schwarz-multigrid pressure preconditioner ('hsmg') the      */
 /* reference's cases select (examples/rugby_ball/rugby_ball.case:46-52).   */
-/* Structured boxes only: ex*ey*ez elements numbered x fastest (as built by */
-/* ntg_mesh_box); lx in {4, 6, 8}.                                          */
+/* lx in {4, 6, 8}.  ntg_schwarz_create: structured boxes, ex*ey*ez       */
+/* elements numbered x fastest (as built by ntg_mesh_box).                  */
+/* ntg_schwarz_create_general: any conforming hexahedral mesh (read from   */
+/* .nmsh, neighbours in any orientation): each element is extended across  */
+/* its six faces only (the face neighbours' nodes one step in, found       */
+/* through the plan's global node ids; edge and corner positions excluded, */
+/* as Neko's Schwarz smoother does on general meshes), and the coarse      */
+/* level is the Galerkin Q1 operator P^T A P on the element vertices,      */
+/* inverted densely (at most 8192 active vertices).  Every other call      */
+/* below takes either kind; the tensor-core FDM path is box-only.          */
 /* ---------------------------------------------------------------------- */
 int ntg_schwarz_create(ntg_plan* plan, int ex, int ey, int ez, const double* x_d, const double* y_d,
                        const double* z_d, ntg_schwarz** sw);
+int ntg_schwarz_create_general(ntg_plan* plan, const double* x_d, const double* y_d, const double* z_d,
+                               ntg_schwarz** sw);
 /* refresh the element means of h1 / h2 after ntg_coef_set (and, with the  */
 /* coarse level on, its Dirichlet faces from the plan's mask and h1/h2)    */
 int ntg_schwarz_update(ntg_schwarz* sw);

@@ -22,6 +22,7 @@ path, with the same names and argument meaning:
     pnpn_step_t.step                                             (the pressure + velocity solve sequence, :714-801)
     mma_t.update / KKT                                           (sources/mma/mma.f90, on the GPU)
     fld_file_t.write / read                                      (Nek5000 binary field files, fld_file_output_t)
+    nmsh.read / write / coef_from_nmsh / face_mask               (Neko's .nmsh mesh files, the cases' "mesh_file")
     load_case, solver_from_case, build_solver                    (solver wiring from the case file, adjoint_scheme.f90:693-851)
 
 Field arguments are CUDA tensors (torch) laid out like Neko's x(lx,ly,lz,nelv):
@@ -46,6 +47,7 @@ from .api import (PDE_filter_t, RAMP_mapping_t, SolveSequence, adjoint_minimum_d
 
 from . import dist  # noqa: E402  (element-partitioned solves across ranks)
 from . import dofmap  # noqa: E402  (global node ids from element-vertex connectivity)
+from . import nmsh  # noqa: E402  (Neko's .nmsh mesh files)
 
 __all__ = [
     "GS_OP_ADD", "GS_OP_MUL", "GS_OP_MIN", "GS_OP_MAX", "KSP_CG", "KSP_CG_MIXED", "KSP_FCG_MIXED", "KSP_GMRES",
@@ -54,7 +56,7 @@ __all__ = [
     "krylov_solver_factory", "ksp_monitor_t", "projection_t", "RAMP_mapping_t", "PDE_filter_t",
     "simple_brinkman_source_term_t", "cadd_mask", "invcol1_mask", "cmult_mask", "col2_mask", "col3_mask",
     "sub3_mask", "glsc2_mask", "glsc3", "permeability", "sens_min_dissipation", "build_box", "mask_face_xmax",
-    "learned_guess_t", "SolveSequence", "profiler_start_region", "profiler_end_region", "profiler_region", "ar1_modes", "schwarz_t", "dist", "dofmap", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
+    "learned_guess_t", "SolveSequence", "profiler_start_region", "profiler_end_region", "profiler_region", "ar1_modes", "schwarz_t", "dist", "dofmap", "nmsh", "opgrad", "dudxyz", "cdtp", "conv1", "curl",
     "adv_lin_no_dealias_t", "adv_lin_dealias_t", "adjoint_minimum_dissipation_source_term_t", "pnpn_prs_res_t", "pnpn_vel_res_t", "pnpn_step_t", "mma_t", "fld_file_t", "load_case", "solver_from_case",
     "solver_config_t", "build_solver",
 ]

@@ -63,6 +63,11 @@ SIGNATURES = {
     "ntg_ksp_set_tol": (_i, [_vp, _d, _d]),
     "ntg_ksp_set_schwarz": (_i, [_vp, _vp]),
     "ntg_schwarz_create": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "ntg_schwarz_create_general": (_i, [_vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "ntg_nmsh_info": (_i, [C.c_char_p, _vp, _vp, _vp, _vp]),
+    "ntg_nmsh_read": (_i, [C.c_char_p, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ntg_nmsh_write": (_i, [C.c_char_p, C.c_int32, C.c_int32, _vp, _vp, _vp, C.c_int32, _vp, C.c_int32, _vp, _vp, _vp]),
+    "ntg_nodes_from_vertices": (_i, [C.c_int64, _i, _vp, _vp, _vp, _vp, _vp]),
     "ntg_schwarz_update": (_i, [_vp]),
     "ntg_schwarz_set_coarse": (_i, [_vp, _i]),
     "ntg_schwarz_set_mass_term": (_i, [_vp, _i]),

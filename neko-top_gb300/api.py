@@ -348,17 +348,29 @@ class _ksp:
 
 class schwarz_t:
     """Overlapping additive Schwarz preconditioner (FP32, fast-diagonalisation
-    local solves) for a structured box coef_t built by coef_t.box.  With
-    ``coarse=True`` it adds the coarse-grid correction on the element
-    vertices (two-level Schwarz; the coarse part of Neko's 'hsmg')."""
+    local solves).  With ``coarse=True`` it adds the coarse-grid correction
+    on the element vertices (two-level Schwarz; the coarse part of Neko's
+    'hsmg').  A structured box coef_t (coef_t.box) takes the box form
+    (overlap across faces, edges and corners; separable coarse solve); any
+    other mesh (coef_t.from_vertices, nmsh.coef_from_nmsh), or
+    ``general=True``, the general form (overlap across the six faces, found
+    through the global node ids; Galerkin coarse operator, at most 8192
+    active vertices)."""
 
-    def __init__(self, coef: coef_t, coarse: bool = False):
-        if not hasattr(coef, "box_dims"):
-            raise ValueError("schwarz_t needs a structured box mesh (coef_t.box)")
-        ex, ey, ez = coef.box_dims
+    def __init__(self, coef: coef_t, coarse: bool = False, general: bool | None = None):
+        if general is None:
+            general = not hasattr(coef, "box_dims")
         h = C.c_void_p()
-        check(lib().ntg_schwarz_create(coef.handle, ex, ey, ez, _ptr(coef.x), _ptr(coef.y), _ptr(coef.z),
-                                       C.byref(h)))
+        if general:
+            check(lib().ntg_schwarz_create_general(coef.handle, _ptr(coef.x), _ptr(coef.y), _ptr(coef.z),
+                                                   C.byref(h)))
+        else:
+            if not hasattr(coef, "box_dims"):
+                raise ValueError("the box form of schwarz_t needs a structured box mesh (coef_t.box)")
+            ex, ey, ez = coef.box_dims
+            check(lib().ntg_schwarz_create(coef.handle, ex, ey, ez, _ptr(coef.x), _ptr(coef.y), _ptr(coef.z),
+                                           C.byref(h)))
+        self.general = bool(general)
         self._h = h
         self.coef = coef
         self.coarse = bool(coarse)

@@ -272,10 +272,14 @@ __device__ __forceinline__ void fdm_bwd_eo(const float* __restrict__ M, const fl
   }
 }
 
-template <int LX, bool EO>
+// GEN: a general mesh (Ex = nelv, Ey = Ez = 1): the ghost layers come from
+// the face-neighbour table (edge and corner positions stay zero) and the
+// coarse restriction weighs nodes by minv = 1 / multiplicity.
+template <int LX, bool EO, bool GEN>
 __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, EO ? FdmCfg<LX>::MINB_EO : FdmCfg<LX>::MINB)
     k_fdm(const float* __restrict__ r, float* __restrict__ ze, const float* __restrict__ esc, int Ex, int Ey,
           int Ez, const Scalars* sc, float* __restrict__ corner, CoarsePhi ph,
+          const int32_t* __restrict__ ghost, const float* __restrict__ minv,
           const __grid_constant__ FdmRef<LX + 2> R) {
   using C = FdmCfg<LX>;
   constexpr int LE = C::LE, LE2 = C::LE2, LE3 = C::LE3, N = LX - 1, RS = C::RS, PS = C::PS, TPE = C::TPE;
@@ -307,7 +311,62 @@ __global__ void __launch_bounds__(FdmCfg<LX>::THREADS, EO ? FdmCfg<LX>::MINB_EO 
     const bool live = e < nelv;
     if (tl < NSC) es[tl] = live ? esc[(int64_t)e * NSC + tl] : 1.f;
     // gather R_e r: columns (a, b) = (u, v1), (u, v2) over c
-    if (live) {
+    if (GEN && live) {
+      const int64_t eb = (int64_t)e * LX3;
+      const int32_t* gh = ghost + eb / LX * 6;  // (e * 6) * LX2
+      const bool ia = u >= 1 && u <= LX;
+      float part[8];
+#pragma unroll
+      for (int v = 0; v < 8; ++v) part[v] = 0.f;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const int vb = q ? v2 : v1;
+        const bool ib = vb >= 1 && vb <= LX;
+        float* Ac = A + u + RS * vb;
+        if (ia && ib) {
+          // own column with the t-face ghosts at its ends
+          const int i = u - 1, j = vb - 1;
+          const int32_t g0 = gh[4 * LX2 + i + LX * j], g1 = gh[5 * LX2 + i + LX * j];
+          Ac[0] = g0 >= 0 ? r[g0] : 0.f;
+          Ac[PS * (LE - 1)] = g1 >= 0 ? r[g1] : 0.f;
+          const float* rc = r + eb + i + LX * j;
+          const float* mc = minv + eb + i + LX * j;
+          float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+          for (int c = 1; c < LE - 1; ++c) {
+            const float val = rc[(c - 1) * LX2];
+            Ac[PS * c] = val;
+            if (corner) {
+              const float wv = val * mc[(c - 1) * LX2];
+              s0 = fmaf(sp[0][c - 1], wv, s0);
+              s1 = fmaf(sp[1][c - 1], wv, s1);
+            }
+          }
+          if (corner) {
+#pragma unroll
+            for (int v = 0; v < 8; ++v) part[v] = fmaf(sp[v & 1][i] * sp[(v >> 1) & 1][j], (v >> 2) ? s1 : s0, part[v]);
+          }
+        } else if (ia || ib) {
+          // an r-face (a at the border) or s-face (b at the border) ghost column
+          const int32_t* gf = ia ? gh + (vb == 0 ? 2 : 3) * LX2 + (u - 1) : gh + (u == 0 ? 0 : 1) * LX2 + (vb - 1);
+          Ac[0] = 0.f;
+          Ac[PS * (LE - 1)] = 0.f;
+#pragma unroll
+          for (int c = 1; c < LE - 1; ++c) {
+            const int32_t gi = gf[LX * (c - 1)];
+            Ac[PS * c] = gi >= 0 ? r[gi] : 0.f;
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < LE; ++c) Ac[PS * c] = 0.f;
+        }
+      }
+      if (corner) {
+#pragma unroll
+        for (int v = 0; v < 8; ++v) *crs_slot<LX>(A, red, el, tl, v) = part[v];
+      }
+    }
+    if (!GEN && live) {
       const int exy = e / Ex, ex = e - exy * Ex, ez = exy / Ey, ey = exy - ez * Ey;
       int i = u - 1, dx = 0;
       if (i < 0) { dx = -1; i = N - 1; } else if (i > N) { dx = 1; i = 1; }
@@ -797,6 +856,8 @@ struct ntg_schwarz {
   ntg::sw::FdmTc ftc{};
   int fdm_tc = 0;
   int fdm_eo = 0;  // even-odd 1D transforms (chosen when the reference eigenvectors have parity)
+  // general mesh: face-neighbour tables, global-node prolongation, Galerkin coarse level
+  ntg::sw::GenTopo* gen = nullptr;
 };
 
 using namespace ntg;
@@ -835,6 +896,8 @@ static void schwarz_free(ntg_schwarz* s) {
   for (int d = 0; d < 3; ++d) dev_free(s->cS[d]);
   dev_free(s->clam); dev_free(s->corner); dev_free(s->cwork); dev_free(s->uc); dev_free(s->dw);
   ntg::sw::fdm_tc_free(&s->ftc);
+  ntg::sw::gen_free(s->gen);
+  s->gen = nullptr;
 }
 
 // Generalised symmetric eigenproblem K s = lam M s (M SPD, n small): with
@@ -1054,8 +1117,13 @@ int fdm_prepare_grid(ntg_schwarz* w);
 template <int LX>
 int fdm_prepare(ntg_schwarz* w) {
   using C = FdmCfg<LX>;
-  NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
-  NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  if (w->gen) {
+    NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+    NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  } else {
+    NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+    NTG_CUDA_TRY(cudaFuncSetAttribute(k_fdm<LX, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+  }
   return fdm_prepare_grid<LX>(w);
 }
 
@@ -1073,10 +1141,17 @@ template <int LX>
 int fdm_prepare_grid(ntg_schwarz* w) {
   using C = FdmCfg<LX>;
   int per_sm = 0;
-  if (w->fdm_eo)
-    NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, true>, C::THREADS, C::SMEM));
-  else
-    NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, false>, C::THREADS, C::SMEM));
+  if (w->gen) {
+    if (w->fdm_eo)
+      NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, true, true>, C::THREADS, C::SMEM));
+    else
+      NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, false, true>, C::THREADS, C::SMEM));
+  } else {
+    if (w->fdm_eo)
+      NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, true, false>, C::THREADS, C::SMEM));
+    else
+      NTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fdm<LX, false, false>, C::THREADS, C::SMEM));
+  }
   const int64_t batches = (w->plan->nelv + C::EPB - 1) / C::EPB;
   const int64_t cap = (int64_t)num_sms() * (per_sm > 0 ? per_sm : 1);
   w->fdm_grid = (int)(batches < cap ? batches : cap);
@@ -1096,12 +1171,23 @@ int fdm_launch(ntg_schwarz* w, const float* r, cudaStream_t s, const Scalars* sc
     }
     R.lam[a] = (float)w->lamref[a];
   }
-  if (w->fdm_eo)
-    k_fdm<LX, true><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
-                                                             w->coarse_ready ? w->corner : nullptr, w->ph, R);
-  else
-    k_fdm<LX, false><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
-                                                              w->coarse_ready ? w->corner : nullptr, w->ph, R);
+  float* corner = w->coarse_ready ? w->corner : nullptr;
+  if (w->gen) {
+    const int32_t* gh = w->gen->ghost;
+    const float* minv = w->plan->multf;
+    if (w->fdm_eo)
+      k_fdm<LX, true, true><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, 1, 1, sc, corner,
+                                                                     w->ph, gh, minv, R);
+    else
+      k_fdm<LX, false, true><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, 1, 1, sc, corner,
+                                                                      w->ph, gh, minv, R);
+  } else if (w->fdm_eo) {
+    k_fdm<LX, true, false><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc, corner,
+                                                                    w->ph, nullptr, nullptr, R);
+  } else {
+    k_fdm<LX, false, false><<<w->fdm_grid, C::THREADS, C::SMEM, s>>>(r, w->ze, w->esc, w->Ex, w->Ey, w->Ez, sc,
+                                                                     corner, w->ph, nullptr, nullptr, R);
+  }
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
@@ -1141,9 +1227,47 @@ inline int coarse_launch(ntg_schwarz* w, cudaStream_t s, const Scalars* sc) {
 }  // namespace sw
 }  // namespace ntg
 
+namespace ntg {
+namespace sw {
+
+// the general-mesh application: FDM with the face-neighbour gather, the
+// dense coarse level, the global-node prolongation
+template <int LX>
+int apply_gen(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, bool dot, double* part,
+              int rz_mode) {
+  timer_start(TM_FDM, s);
+  NTG_TRY(fdm_launch<LX>(w, r, s, sc));
+  timer_stop(TM_FDM, s);
+  if (w->coarse_ready) {
+    timer_start(TM_CRS, s);
+    NTG_TRY(gen_coarse_launch(w->gen, w->corner, s, sc));
+    timer_stop(TM_CRS, s);
+  }
+  timer_start(TM_PULL, s);
+  NTG_TRY(gen_pull_launch(w->gen, w->ze, z, r, w->dw, w->ph, dot, part, rz_mode, sc, s));
+  timer_stop(TM_PULL, s);
+  return NTG_OK;
+}
+
+}  // namespace sw
+}  // namespace ntg
+
 int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
                        double* part, int rz_mode) {
   ntg_plan* p = w->plan;
+  if (w->gen) {
+    const bool dot = mult != nullptr;
+    switch (p->lx) {
+      case 4: NTG_TRY(sw::apply_gen<4>(w, z, r, s, sc, dot, part, rz_mode)); break;
+      case 6: NTG_TRY(sw::apply_gen<6>(w, z, r, s, sc, dot, part, rz_mode)); break;
+      case 8: NTG_TRY(sw::apply_gen<8>(w, z, r, s, sc, dot, part, rz_mode)); break;
+      default:
+        set_error("schwarz: lx=%d not compiled (4, 6, 8)", p->lx);
+        return NTG_ERR_UNSUPPORTED;
+    }
+    NTG_CUDA_TRY(cudaGetLastError());
+    return mask_guarded_f32(p, z, s, sc);
+  }
   switch (p->lx) {
     case 4:
       timer_start(TM_FDM, s);
@@ -1199,14 +1323,11 @@ int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s,
 
 extern "C" {
 
-int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, const double* y_d, const double* z_d,
-                       ntg_schwarz** out) {
-  clear_error();
-  NTG_CHECK_ARG(p && out && x_d && y_d && z_d, "ntg_schwarz_create: null argument");
-  NTG_CHECK_ARG(ex > 0 && ey > 0 && ez > 0 && (int64_t)ex * ey * ez == p->nelv,
-                "ntg_schwarz_create: ex*ey*ez must equal the plan's element count (structured box, x fastest)");
-  NTG_CHECK_ARG(p->lx == 4 || p->lx == 6 || p->lx == 8, "ntg_schwarz_create: lx must be 4, 6 or 8");
-  NTG_CHECK_ARG(p->nelv < (int64_t)1 << 30, "ntg_schwarz_create: element count must be below 2^30");
+}  // extern "C"
+
+// shared by the structured (box) and general-mesh constructors
+static int schwarz_create_impl(ntg_plan* p, int ex, int ey, int ez, bool general, const double* x_d,
+                               const double* y_d, const double* z_d, ntg_schwarz** out) {
   *out = nullptr;
   ntg_schwarz* s = new ntg_schwarz();
   s->plan = p;
@@ -1217,6 +1338,7 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
   int st = NTG_OK;
   double* dl = nullptr;
   do {
+    if (general && ((st = ensure_fp32(p)) || (st = sw::gen_create(p, &s->gen)))) break;
     if ((st = dev_alloc(&s->hld, (size_t)E * 3)) || (st = dev_alloc(&s->esc, (size_t)E * 8)) ||
         (st = dev_alloc(&s->hc, (size_t)E * 2)) || (st = dev_alloc(&s->ze, (size_t)E * LE2 * LE)) ||
         (st = dev_alloc(&dl, (size_t)E * 3)))
@@ -1243,7 +1365,7 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
     s->fdm_eo = sw::fdm_has_parity(s);
     st = p->lx == 4 ? sw::fdm_prepare<4>(s) : p->lx == 6 ? sw::fdm_prepare<6>(s) : sw::fdm_prepare<8>(s);
     if (st) break;
-    if (p->lx == 8 && p->dev_err) {
+    if (!general && p->lx == 8 && p->dev_err) {
       // prepared, off by default: measured slower than the FP32-core kernel
       if ((st = sw::fdm_tc_prepare(s->Sref.data(), s->lamref.data(), &s->ftc))) break;
       s->fdm_tc = 0;
@@ -1258,6 +1380,29 @@ int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, c
   }
   *out = s;
   return NTG_OK;
+}
+
+extern "C" {
+
+int ntg_schwarz_create(ntg_plan* p, int ex, int ey, int ez, const double* x_d, const double* y_d, const double* z_d,
+                       ntg_schwarz** out) {
+  clear_error();
+  NTG_CHECK_ARG(p && out && x_d && y_d && z_d, "ntg_schwarz_create: null argument");
+  NTG_CHECK_ARG(ex > 0 && ey > 0 && ez > 0 && (int64_t)ex * ey * ez == p->nelv,
+                "ntg_schwarz_create: ex*ey*ez must equal the plan's element count (structured box, x fastest)");
+  NTG_CHECK_ARG(p->lx == 4 || p->lx == 6 || p->lx == 8, "ntg_schwarz_create: lx must be 4, 6 or 8");
+  NTG_CHECK_ARG(p->nelv < (int64_t)1 << 30, "ntg_schwarz_create: element count must be below 2^30");
+  return schwarz_create_impl(p, ex, ey, ez, false, x_d, y_d, z_d, out);
+}
+
+// any conforming hexahedral mesh: neighbours from the plan's global node ids
+int ntg_schwarz_create_general(ntg_plan* p, const double* x_d, const double* y_d, const double* z_d,
+                               ntg_schwarz** out) {
+  clear_error();
+  NTG_CHECK_ARG(p && out && x_d && y_d && z_d, "ntg_schwarz_create_general: null argument");
+  NTG_CHECK_ARG(p->lx == 4 || p->lx == 6 || p->lx == 8, "ntg_schwarz_create_general: lx must be 4, 6 or 8");
+  NTG_CHECK_ARG(p->nelv < (int64_t)1 << 30, "ntg_schwarz_create_general: element count must be below 2^30");
+  return schwarz_create_impl(p, (int)p->nelv, 1, 1, true, x_d, y_d, z_d, out);
 }
 
 // refresh the element means of h1 / h2 after ntg_coef_set
@@ -1282,6 +1427,24 @@ int ntg_schwarz_update(ntg_schwarz* s) {
     NTG_CUDA_TRY(cudaStreamSynchronize(p->stream));
     dev_free(hBa);
   }
+  if (s->coarse && s->gen) {
+    s->coarse_ready = 0;
+    NTG_TRY(sw::gen_coarse_setup(p, s->gen));
+    if (s->gen->coarse_ready) {
+      if (!s->corner) NTG_TRY(dev_alloc(&s->corner, (size_t)p->nelv * 8));
+      if (!s->ph.p[1][p->lx - 1]) {
+        double xi[NTG_LXMAX], wq[NTG_LXMAX], Dm[NTG_LXMAX * NTG_LXMAX];
+        gll_basis(p->lx, xi, wq, Dm);
+        for (int i = 0; i < p->lx; ++i) {
+          s->ph.p[0][i] = (float)(0.5 * (1.0 - xi[i]));
+          s->ph.p[1][i] = (float)(0.5 * (1.0 + xi[i]));
+        }
+        s->ph.p[0][0] = 1.f; s->ph.p[1][0] = 0.f; s->ph.p[0][p->lx - 1] = 0.f; s->ph.p[1][p->lx - 1] = 1.f;
+      }
+      s->coarse_ready = 1;
+    }
+    return NTG_OK;
+  }
   if (s->coarse) return coarse_setup(s);
   return NTG_OK;
 }
@@ -1292,7 +1455,8 @@ int ntg_schwarz_update(ntg_schwarz* s) {
 int ntg_schwarz_set_fdm_path(ntg_schwarz* s, int path) {
   clear_error();
   NTG_CHECK_ARG(s && path >= 0 && path <= 2, "ntg_schwarz_set_fdm_path: bad argument");
-  NTG_CHECK_ARG(path != 1 || s->ftc.img, "ntg_schwarz_set_fdm_path: the tensor-core path needs lx = 8");
+  NTG_CHECK_ARG(path != 1 || s->ftc.img,
+                "ntg_schwarz_set_fdm_path: the tensor-core path needs lx = 8 on a structured box");
   s->fdm_tc = path == 1 ? 1 : 0;
   if (path != 1) {
     s->fdm_eo = path == 0 ? sw::fdm_has_parity(s) : 0;
@@ -1315,6 +1479,7 @@ int ntg_schwarz_set_coarse(ntg_schwarz* s, int enable) {
   NTG_TRY(cudaStreamSynchronize(s->plan->stream) == cudaSuccess ? NTG_OK : NTG_ERR_CUDA);
   s->coarse = enable ? 1 : 0;
   s->coarse_ready = 0;
+  if (s->gen) s->gen->coarse_ready = 0;
   return s->coarse ? ntg_schwarz_update(s) : NTG_OK;
 }
 

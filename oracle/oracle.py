@@ -222,6 +222,31 @@ def mesh_subset(m: Mesh, elems, dims=None) -> Mesh:
     return s
 
 
+def mesh_general(x, y, z, gid, lx) -> Mesh:
+    """The oracle Mesh of any hexahedral mesh given by its GLL node
+    coordinates and global node ids (nelv x lx^3 each, x fastest)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    nelv = x.size // lx ** 3
+    s = Mesh(nelv, 1, 1, lx, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), 0.0, 0)
+    s.x, s.y, s.z = x, np.ascontiguousarray(y, dtype=np.float64), np.ascontiguousarray(z, dtype=np.float64)
+    s.gid = np.ascontiguousarray(gid, dtype=np.int64)
+    _, s.w, s.D = gll(lx)
+    n = s.n
+    G = {k: np.zeros(n) for k in ("g11", "g12", "g13", "g22", "g23", "g33")}
+    s.B = np.zeros(n); s.jac = np.zeros(n)
+    lib().orc_geom(s.nelv, lx, s.x, s.y, s.z, G["g11"], G["g12"], G["g13"], G["g22"], G["g23"], G["g33"],
+                   s.B, _ptr(s.jac))
+    s.G = G
+    s.perm = np.zeros(n, dtype=np.int32)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    s.uid = np.zeros(n, dtype=np.int32)
+    s.nu = int(lib().orc_gs_build(n, s.gid, s.perm, offs, _ptr(s.uid)))
+    s.offs = offs[: s.nu + 1].copy()
+    s.mult = np.zeros(n)
+    lib().orc_mult(n, s.nu, s.perm, s.offs, s.mult)
+    return s
+
+
 def gs_op(m: Mesh, u: np.ndarray, op: int = 1) -> np.ndarray:
     v = np.ascontiguousarray(u, dtype=np.float64).copy()
     lib().orc_gs_op(v, m.nu, m.perm, m.offs, int(op))

@@ -220,3 +220,182 @@ def apply(m, r, box, h1=1.0, h2=None, mask=None, coarse=False, plane_bf16=False)
     if mask is not None and len(mask):
         z[np.asarray(mask) - 1] = 0.0
     return z
+
+
+# ---------------------------------------------------------------------------
+# General (unstructured, conforming) hexahedral meshes
+# ---------------------------------------------------------------------------
+
+def _face_nodes(lx, f, normal):
+    """Local indices of face f's nodes (r-, r+, s-, s+, t-, t+ = 0..5) in
+    tangential order (lower axis fastest), at normal index `normal`."""
+    d = f // 2
+    out = []
+    for t in range(lx):
+        for s in range(lx):
+            ijk = [s, t] if d == 0 else [s, t]
+            if d == 0:
+                i, j, k = normal, s, t
+            elif d == 1:
+                i, j, k = s, normal, t
+            else:
+                i, j, k = s, t, normal
+            out.append(i + lx * (j + lx * k))
+    return np.array(out)
+
+
+def face_ghosts(m):
+    """ghost[e, f, p]: the local index (into the whole field) of the node one
+    step inside the face neighbour of element e across face f, matching face
+    node p of e through the global ids; -1 on boundary faces.  Neighbours are
+    the elements holding all four corner ids of the face."""
+    lx, N, l3 = m.lx, m.lx - 1, m.lx ** 3
+    E = m.nelv
+    gid = m.gid.reshape(E, l3)
+    corner_sets = {}
+    for e in range(E):
+        for f in range(6):
+            fn = _face_nodes(lx, f, N if f % 2 else 0)
+            key = tuple(sorted(gid[e, fn[[0, N, N * lx, N * lx + N]]]))
+            corner_sets.setdefault(key, []).append((e, f))
+    ghost = -np.ones((E, 6, lx * lx), dtype=np.int64)
+    for key, lst in corner_sets.items():
+        if len(lst) == 1:
+            continue
+        assert len(lst) == 2, "non-conforming mesh"
+        for (ea, fa), (eb, fb) in (lst, lst[::-1]):
+            own = gid[ea, _face_nodes(lx, fa, N if fa % 2 else 0)]
+            other_face = _face_nodes(lx, fb, N if fb % 2 else 0)
+            other_in = _face_nodes(lx, fb, N - 1 if fb % 2 else 1)
+            pos = {g: q for q, g in enumerate(gid[eb, other_face])}
+            ghost[ea, fa] = [eb * l3 + other_in[pos[g]] for g in own]
+    return ghost
+
+
+def _ghost_ext_index(lx, f):
+    """(a, b, c) index arrays of the ghost layer beyond face f in the
+    extended box, in face-node order."""
+    LE = lx + 2
+    d, b0 = f // 2, (LE - 1 if f % 2 else 0)
+    s, t = np.meshgrid(np.arange(lx), np.arange(lx), indexing="xy")
+    s, t = s.ravel() + 1, t.ravel() + 1
+    b0v = np.full(s.shape, b0)
+    return [(b0v, s, t), (s, b0v, t), (s, t, b0v)][d]
+
+
+def coarse_galerkin(m, h1=1.0, h2=None, mask=None):
+    """The Galerkin Q1 coarse operator P^T A P on the element vertices
+    (active = not masked), with P the trilinear interpolation zeroed on
+    masked nodes.  Returns (A_c, vid) with vid[e, v] the active vertex of
+    corner v (i + 2j + 4k) of element e or -1."""
+    lx, N, l3, E = m.lx, m.lx - 1, m.lx ** 3, m.nelv
+    xi, _, _ = numpy_ref.gll(lx)
+    phi = np.stack([0.5 * (1 - xi), 0.5 * (1 + xi)])
+    phi[:, 0], phi[:, N] = (1.0, 0.0), (0.0, 1.0)
+    flag = np.zeros(m.n, dtype=bool)
+    if mask is not None and len(mask):
+        flag[np.asarray(mask) - 1] = True
+    masked_g = set(m.gid[flag].tolist())
+    corners = np.array([((v & 1) * N) + lx * (((v >> 1) & 1) * N) + lx * lx * ((v >> 2) * N) for v in range(8)])
+    cg = m.gid.reshape(E, l3)[:, corners]
+    verts = sorted({int(g) for g in cg.ravel() if int(g) not in masked_g})
+    index = {g: a for a, g in enumerate(verts)}
+    vid = np.array([[index.get(int(g), -1) for g in row] for row in cg])
+    q = np.arange(l3)
+    i, j, k = q % lx, (q // lx) % lx, q // (lx * lx)
+    basis = np.stack([phi[v & 1][i] * phi[(v >> 1) & 1][j] * phi[v >> 2][k] for v in range(8)])  # (8, l3)
+    keep = ~flag.reshape(E, l3)
+    h1f = h1 if np.ndim(h1) else None
+    h1c = 1.0 if h1f is not None else float(h1)
+    W = []
+    for v in range(8):
+        U = (basis[v][None, :] * keep).ravel()
+        W.append(numpy_ref_ax(m, U, h1f, h1c, h2).reshape(E, l3))
+    nv = len(verts)
+    A = np.zeros((nv, nv))
+    for e in range(E):
+        Ue = basis * keep[e][None, :]
+        Ae = Ue @ np.stack([W[v][e] for v in range(8)]).T  # [w, v]
+        for w in range(8):
+            if vid[e, w] < 0:
+                continue
+            for v in range(8):
+                if vid[e, v] >= 0:
+                    A[vid[e, w], vid[e, v]] += Ae[w, v]
+    A = 0.5 * (A + A.T)
+    if (mask is None or len(mask) == 0) and (h2 is None or not np.any(h2)):
+        A = A + np.trace(A) / nv / nv
+    return A, vid
+
+
+def numpy_ref_ax(m, u, h1, h1c, h2):
+    from oracle import oracle as orc
+    return orc.ax_helm(m, u, h1=h1, h1c=h1c, h2=h2)
+
+
+def apply_general(m, r, h1=1.0, h2=None, mask=None, coarse=False):
+    """z = M r on a general mesh: each element extended by one node layer
+    across its six faces only (the face neighbour's nodes one step inside,
+    edge and corner positions excluded), the local solves of `apply`
+    (element lengths, shared reference pair), the results summed per
+    global node; with coarse=True plus P A_c^-1 P^T r with the Galerkin
+    operator of coarse_galerkin; masked nodes zeroed."""
+    lx, N, LE, l3, E = m.lx, m.lx - 1, m.lx + 2, m.lx ** 3, m.nelv
+    hl = element_lengths(m)
+    ghost = face_ghosts(m)
+    r = np.asarray(r, dtype=np.float64)
+    r4 = r.reshape(E, lx, lx, lx)  # (e, k, j, i)
+    h1e = np.full(E, float(h1)) if not np.ndim(h1) else np.asarray(h1).reshape(E, -1).mean(1)
+    h2e = np.zeros(E) if h2 is None else np.asarray(h2).reshape(E, -1).mean(1)
+    acc = {}
+    gid = m.gid
+    for e in range(E):
+        Ss, Ls = [], []
+        for d in range(3):
+            S, lam = ext_1d(lx, hl[e, d], hl[e, d], hl[e, d])
+            Ss.append(S)
+            Ls.append(lam)
+        rext = np.zeros((LE, LE, LE))  # [a, b, c]
+        rext[1:-1, 1:-1, 1:-1] = r4[e].transpose(2, 1, 0)
+        for f in range(6):
+            a, b, c = _ghost_ext_index(lx, f)
+            src = ghost[e, f]
+            ok = src >= 0
+            rext[a[ok], b[ok], c[ok]] = r[src[ok]]
+        Sx, Sy, Sz = Ss
+        t = np.einsum("pa,qb,sc,pqs->abc", Sx, Sy, Sz, rext)
+        t /= h1e[e] * (Ls[0][:, None, None] + Ls[1][None, :, None] + Ls[2][None, None, :]) + h2e[e]
+        zext = np.einsum("ap,bq,cs,pqs->abc", Sx, Sy, Sz, t)
+        own = zext[1:-1, 1:-1, 1:-1].transpose(2, 1, 0).ravel()
+        for q in range(l3):
+            g = int(gid[e * l3 + q])
+            acc[g] = acc.get(g, 0.0) + own[q]
+        for f in range(6):
+            a, b, c = _ghost_ext_index(lx, f)
+            for p in range(lx * lx):
+                src = ghost[e, f, p]
+                if src >= 0:
+                    g = int(gid[src])
+                    acc[g] = acc.get(g, 0.0) + zext[a[p], b[p], c[p]]
+    z = np.array([acc[int(g)] for g in gid])
+    if coarse:
+        A, vid = coarse_galerkin(m, h1, h2, mask)
+        if A.shape[0]:
+            xi, _, _ = numpy_ref.gll(lx)
+            phi = np.stack([0.5 * (1 - xi), 0.5 * (1 + xi)])
+            q = np.arange(l3)
+            i, j, k = q % lx, (q // lx) % lx, q // (lx * lx)
+            basis = np.stack([phi[v & 1][i] * phi[(v >> 1) & 1][j] * phi[v >> 2][k] for v in range(8)])
+            rm = (r * m.mult).reshape(E, l3)
+            rc = np.zeros(A.shape[0])
+            for e in range(E):
+                cs = basis @ rm[e]
+                for v in range(8):
+                    if vid[e, v] >= 0:
+                        rc[vid[e, v]] += cs[v]
+            zc = np.linalg.solve(A, rc)
+            zcv = np.where(vid >= 0, zc[np.maximum(vid, 0)], 0.0)  # (E, 8)
+            z = z + (zcv @ basis).ravel()
+    if mask is not None and len(mask):
+        z[np.asarray(mask) - 1] = 0.0
+    return z
