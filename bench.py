@@ -801,9 +801,13 @@ def run_terms(args, local):
     # 29,184 FMA each; per GL point the adjoint term's 3 GL gradients (108 FMA),
     # mixing (36 + 9) and per component a D^T of u_i V (36 FMA + 36 products);
     # the linear term's 6 GL gradients (216 FMA) and fluxes (36); / 512 GLL points.
+    # Without dealiasing, per node (lx = 8): adjoint 3 gradients (72 FMA),
+    # opgrad mixing (36), fluxes V (9), u_i V (9 products) and three D^T (72);
+    # linear 6 gradients (144) and mixing (72).
     gl = 12 ** 3
     interp = 12 * 512 + 144 * 64 + 1728 * 8
     flops = {"vel_res": 3 * 120 + 48 + 24, "ax_helm_fp64": 116,
+             "adjoint_advection": 2 * (72 + 36 + 9 + 72) + 9, "linear_advection": 2 * (144 + 72),
              "adjoint_advection_dealias": (2 * (9 * interp + gl * (108 + 45 + 3 * 36)) + gl * (6 + 3 * 36)) / 512,
              "linear_advection_dealias": 2 * (9 * interp + gl * (216 + 36)) / 512}
     L = pkg.lib()

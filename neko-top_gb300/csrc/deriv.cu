@@ -249,6 +249,156 @@ __global__ void __launch_bounds__(Shape<LX, 3>::THREADS)
   }
 }
 
+// The adjoint advection without dealiasing in one element pass:
+//   f_i -= sum_j u_j opgrad_i(Ub_j) + sum_d cdtp_d(u_i Ub_d).
+// The cdtp fluxes of all three components share the contravariant fluxes
+// V_r = w3 (drdx . Ub), V_s = w3 (dsdx . Ub), V_t = w3 (dtdx . Ub):
+// component i's fluxes are u_i V_r, u_i V_s, u_i V_t.  Phase 1 takes the
+// reference gradients of Ub from its tiles, subtracts the opgrad part and
+// stores V; then per component the Ub tiles hold u_i V and D^T is applied.
+// Inputs and the cofactors are read once per node instead of by six
+// separate kernels; the FP64 operation count is the separate kernels' less
+// the repeated flux sums (198 instead of 216 per node).
+template <int LX>
+__global__ void __launch_bounds__(Shape<LX, 6>::THREADS)
+    k_adv_adj_nd(double* __restrict__ f0, double* __restrict__ f1, double* __restrict__ f2,
+                 const double* __restrict__ u0, const double* __restrict__ u1, const double* __restrict__ u2,
+                 const double* __restrict__ b0, const double* __restrict__ b1, const double* __restrict__ b2,
+                 int64_t nelv, const __grid_constant__ DMat<LX> M, const double* __restrict__ met, int64_t n) {
+  using S = Shape<LX, 6>;
+  constexpr int LX2 = S::LX2, LX3 = S::LX3, EPB = S::EPB;
+  __shared__ double sA[EPB][3][LX3];  // Ub, then u_i V_r, u_i V_s, u_i V_t
+  __shared__ double sV[EPB][3][LX3];  // V_r, V_s, V_t
+  const int tid = threadIdx.x, le = tid / LX2, ij = tid - le * LX2, i = ij % LX, j = ij / LX;
+  const bool worker = tid < S::NW;
+  const double* ub[3] = {b0, b1, b2};
+  const double* uu[3] = {u0, u1, u2};
+  double* ff[3] = {f0, f1, f2};
+  for (int64_t g = blockIdx.x; g * EPB < nelv; g += gridDim.x) {
+    const int64_t e = g * EPB + le;
+    const bool act = worker && e < nelv;
+    for (int k = 0; k < LX && worker; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sA[le][c][k * LX2 + ij] = act ? ub[c][e * LX3 + k * LX2 + ij] : 0.0;
+    __syncthreads();
+    if (act) {
+#pragma unroll 1
+      for (int k = 0; k < LX; ++k) {
+        const int64_t q = e * LX3 + k * LX2 + ij;
+        const int p = k * LX2 + ij;
+        double gr[3][3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rgrad<LX>(sA[le][c], M, i, j, k, gr[c][0], gr[c][1], gr[c][2]);
+        double m[9];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) m[t] = met[t * n + q];
+        const double w3 = M.w[i] * M.w[j] * M.w[k];
+        const double uq[3] = {u0[q], u1[q], u2[q]};
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          double acc = 0.0;
+#pragma unroll
+          for (int jj = 0; jj < 3; ++jj)
+            acc = fma(uq[jj], m[c] * gr[jj][0] + m[3 + c] * gr[jj][1] + m[6 + c] * gr[jj][2], acc);
+          ff[c][q] -= w3 * acc;
+        }
+        const double bq[3] = {sA[le][0][p], sA[le][1][p], sA[le][2][p]};
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          sV[le][d][p] = w3 * (m[3 * d] * bq[0] + m[3 * d + 1] * bq[1] + m[3 * d + 2] * bq[2]);
+      }
+    }
+#pragma unroll 1
+    for (int c = 0; c < 3; ++c) {
+      __syncthreads();
+      if (act) {
+        for (int k = 0; k < LX; ++k) {
+          const int p = k * LX2 + ij;
+          const double uc = uu[c][e * LX3 + p];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) sA[le][d][p] = uc * sV[le][d][p];
+        }
+      }
+      __syncthreads();
+      if (act) {
+        const double* fr = sA[le][0];
+        const double* fs = sA[le][1];
+        const double* ft = sA[le][2];
+#pragma unroll 1
+        for (int k = 0; k < LX; ++k) {
+          double acc = 0.0;
+#pragma unroll
+          for (int l = 0; l < LX; ++l) {
+            acc = fma(M.d[l * LX + i], fr[k * LX2 + j * LX + l], acc);
+            acc = fma(M.d[l * LX + j], fs[k * LX2 + l * LX + i], acc);
+            acc = fma(M.d[l * LX + k], ft[l * LX2 + j * LX + i], acc);
+          }
+          ff[c][e * LX3 + k * LX2 + ij] -= acc;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The linearised advection without dealiasing in one element pass:
+//   f_i -= B conv1(u_i; Ub) + B conv1(Ub_i; u)
+//        = w3 sum_d (Ub_d (drdx_d . grad u_i) + u_d (drdx_d . grad Ub_i)),
+// with u and Ub in six tiles, the cofactors read once per node.
+template <int LX>
+__global__ void __launch_bounds__(Shape<LX, 6>::THREADS)
+    k_adv_lin_nd(double* __restrict__ f0, double* __restrict__ f1, double* __restrict__ f2,
+                 const double* __restrict__ u0, const double* __restrict__ u1, const double* __restrict__ u2,
+                 const double* __restrict__ b0, const double* __restrict__ b1, const double* __restrict__ b2,
+                 int64_t nelv, const __grid_constant__ DMat<LX> M, const double* __restrict__ met, int64_t n) {
+  using S = Shape<LX, 6>;
+  constexpr int LX2 = S::LX2, LX3 = S::LX3, EPB = S::EPB;
+  __shared__ double sU[EPB][3][LX3], sB[EPB][3][LX3];
+  const int tid = threadIdx.x, le = tid / LX2, ij = tid - le * LX2, i = ij % LX, j = ij / LX;
+  const bool worker = tid < S::NW;
+  const double* ub[3] = {b0, b1, b2};
+  const double* uu[3] = {u0, u1, u2};
+  double* ff[3] = {f0, f1, f2};
+  for (int64_t g = blockIdx.x; g * EPB < nelv; g += gridDim.x) {
+    const int64_t e = g * EPB + le;
+    const bool act = worker && e < nelv;
+    for (int k = 0; k < LX && worker; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sU[le][c][k * LX2 + ij] = act ? uu[c][e * LX3 + k * LX2 + ij] : 0.0;
+        sB[le][c][k * LX2 + ij] = act ? ub[c][e * LX3 + k * LX2 + ij] : 0.0;
+      }
+    __syncthreads();
+    if (act) {
+#pragma unroll 1
+      for (int k = 0; k < LX; ++k) {
+        const int64_t q = e * LX3 + k * LX2 + ij;
+        const int p = k * LX2 + ij;
+        double m[9];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) m[t] = met[t * n + q];
+        const double w3 = M.w[i] * M.w[j] * M.w[k];
+        const double uq[3] = {sU[le][0][p], sU[le][1][p], sU[le][2][p]};
+        const double bq[3] = {sB[le][0][p], sB[le][1][p], sB[le][2][p]};
+#pragma unroll 1
+        for (int c = 0; c < 3; ++c) {
+          double gu[3], gb[3];
+          rgrad<LX>(sU[le][c], M, i, j, k, gu[0], gu[1], gu[2]);
+          rgrad<LX>(sB[le][c], M, i, j, k, gb[0], gb[1], gb[2]);
+          double acc = 0.0;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            acc = fma(bq[d], m[d] * gu[0] + m[3 + d] * gu[1] + m[6 + d] * gu[2], acc);
+            acc = fma(uq[d], m[d] * gb[0] + m[3 + d] * gb[1] + m[6 + d] * gb[2], acc);
+          }
+          ff[c][q] -= w3 * acc;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_mul3(double* __restrict__ a, double* __restrict__ b, double* __restrict__ c,
                        const double* __restrict__ s, int64_t n) {
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
@@ -423,24 +573,12 @@ int ntg_adjoint_advection_no_dealias(ntg_plan* p, double* fx, double* fy, double
   const double* ub[3] = {vxb, vyb, vzb};
   double* f[3] = {fx, fy, fz};
   cudaStream_t s = p->stream;
-  // f_i -= sum_j u_j opgrad_i(Ub_j)
-  NTG_TRY(dv::dispatch<1>(p->lx, [&](auto L) -> int {
+  // f_i -= sum_j u_j opgrad_i(Ub_j) + sum_d cdtp_d(u_i Ub_d), one element pass
+  NTG_TRY(dv::dispatch<6>(p->lx, [&](auto L) -> int {
     constexpr int LX = decltype(L)::value;
-    for (int jj = 0; jj < 3; ++jj) {
-      dv::k_grad<LX, 1, true><<<dv::grid_of<LX, 1>(p), dv::Shape<LX, 1>::THREADS, 0, s>>>(
-          fx, fy, fz, ub[jj], u[jj], p->nelv, dv::dmat<LX>(p), p->met, p->n);
-      NTG_COUNT_LAUNCH();
-    }
-    return NTG_OK;
-  }));
-  // f_i -= sum_d cdtp_d(u_i Ub_d)
-  NTG_TRY(dv::dispatch<3>(p->lx, [&](auto L) -> int {
-    constexpr int LX = decltype(L)::value;
-    for (int ii = 0; ii < 3; ++ii) {
-      dv::k_cdtp<LX, true><<<dv::grid_of<LX, 3>(p), dv::Shape<LX, 3>::THREADS, 0, s>>>(
-          f[ii], ub[0], ub[1], ub[2], u[ii], p->nelv, dv::dmat<LX>(p), p->met, p->n);
-      NTG_COUNT_LAUNCH();
-    }
+    dv::k_adv_adj_nd<LX><<<dv::grid_of<LX, 6>(p), dv::Shape<LX, 6>::THREADS, 0, s>>>(
+        f[0], f[1], f[2], u[0], u[1], u[2], ub[0], ub[1], ub[2], p->nelv, dv::dmat<LX>(p), p->met, p->n);
+    NTG_COUNT_LAUNCH();
     return NTG_OK;
   }));
   NTG_CUDA_TRY(cudaGetLastError());
@@ -457,14 +595,12 @@ int ntg_linear_advection_no_dealias(ntg_plan* p, double* fx, double* fy, double*
   const double* u[3] = {vx, vy, vz};
   const double* ub[3] = {vxb, vyb, vzb};
   double* f[3] = {fx, fy, fz};
-  // f_i -= B conv1(u_i; Ub) + B conv1(Ub_i; u)
-  NTG_TRY(dv::dispatch<2>(p->lx, [&](auto L) -> int {
+  // f_i -= B conv1(u_i; Ub) + B conv1(Ub_i; u), one element pass
+  NTG_TRY(dv::dispatch<6>(p->lx, [&](auto L) -> int {
     constexpr int LX = decltype(L)::value;
-    for (int ii = 0; ii < 3; ++ii) {
-      dv::k_conv<LX, 1><<<dv::grid_of<LX, 2>(p), dv::Shape<LX, 2>::THREADS, 0, p->stream>>>(
-          f[ii], u[ii], ub[0], ub[1], ub[2], ub[ii], u[0], u[1], u[2], p->nelv, dv::dmat<LX>(p), p->met, p->n);
-      NTG_COUNT_LAUNCH();
-    }
+    dv::k_adv_lin_nd<LX><<<dv::grid_of<LX, 6>(p), dv::Shape<LX, 6>::THREADS, 0, p->stream>>>(
+        f[0], f[1], f[2], u[0], u[1], u[2], ub[0], ub[1], ub[2], p->nelv, dv::dmat<LX>(p), p->met, p->n);
+    NTG_COUNT_LAUNCH();
     return NTG_OK;
   }));
   NTG_CUDA_TRY(cudaGetLastError());
