@@ -26,7 +26,7 @@
 // its Schwarz part on the GLL grid and its coarse-grid part.
 //
 // Kernels per application: k_fdm (gather, six 1D transforms, coarse
-// restriction), k_crs_xy / k_crs_z / k_crs_yx (coarse solve), k_pull
+// restriction), k_crs_restrict + six k_crs_mode directions (coarse solve), k_pull
 // (prolongation of both levels, optional (r, z)), then the Dirichlet mask.
 //
 // Determinism: the prolongation is a pull -- every local node sums, in a fixed
@@ -531,22 +531,15 @@ struct CoarseDims {
   float h1, h2, dmin;     // coefficients; eigenvalue sums below dmin are the null mode
 };
 
-// x then y forward transforms on one active z-plane; the plane's residual is
-// gathered from the corner sums of the adjacent elements (ascending element order)
-__global__ void __launch_bounds__(1024)
-    k_crs_xy(const float* __restrict__ corner, const float* __restrict__ Sx, const float* __restrict__ Sy,
-             float* __restrict__ work, CoarseDims d, const Scalars* sc) {
+// restricted residual on the active vertex grid (x fastest): per vertex the
+// corner sums of its adjacent elements, in ascending element order
+__global__ void k_crs_restrict(const float* __restrict__ corner, float* __restrict__ rc, CoarseDims d,
+                               const Scalars* sc) {
   if (sc && sc->done) return;
-  extern __shared__ __align__(16) float sm[];
-  const int m0 = d.m[0], m1 = d.m[1], zi = blockIdx.x, gz = d.lo[2] + zi;
-  float* T = sm;
-  float* U = T + m0 * m1;
-  float* sx = U + m0 * m1;
-  float* sy = sx + m0 * m0;
-  for (int q = threadIdx.x; q < m0 * m0; q += blockDim.x) sx[q] = Sx[q];
-  for (int q = threadIdx.x; q < m1 * m1; q += blockDim.x) sy[q] = Sy[q];
-  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
-    const int gx = d.lo[0] + q % m0, gy = d.lo[1] + q / m0;
+  const int64_t total = (int64_t)d.m[0] * d.m[1] * d.m[2];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int gx = d.lo[0] + (int)(q % d.m[0]), gy = d.lo[1] + (int)((q / d.m[0]) % d.m[1]);
+    const int gz = d.lo[2] + (int)(q / ((int64_t)d.m[0] * d.m[1]));
     float acc = 0.f;
     for (int ez = gz - 1; ez <= gz; ++ez) {
       if (ez < 0 || ez >= d.Ez) continue;
@@ -559,87 +552,43 @@ __global__ void __launch_bounds__(1024)
         }
       }
     }
-    T[q] = acc;
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
-    const int f = q % m0, y = q / m0;
-    float s = 0.f;
-    for (int x = 0; x < m0; ++x) s = fmaf(sx[x * m0 + f], T[y * m0 + x], s);
-    U[q] = s;
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
-    const int f = q % m0, g = q / m0;
-    float s = 0.f;
-    for (int y = 0; y < m1; ++y) s = fmaf(sy[y * m1 + g], U[y * m0 + f], s);
-    work[f + (int64_t)m0 * (g + (int64_t)m1 * zi)] = s;
+    rc[q] = acc;
   }
 }
 
-// z forward, scale by the inverse eigenvalue sums, z back, on one y-index g
-__global__ void __launch_bounds__(1024)
-    k_crs_z(float* __restrict__ work, const float* __restrict__ Sz, const float* __restrict__ lam, CoarseDims d,
-            const Scalars* sc) {
+// One direction of the coarse fast diagonalisation on the active vertex
+// grid, one thread per output: forward t_f = sum_x S[x][f] in_x, back
+// out_x = sum_f S[x][f] in_f (from the stored transpose), along direction
+// DIR (0 = x, 1 = y, 2 = z).
+// SCALE (z forward): divided by the eigenvalue sum, the null mode dropped;
+// UC (x back): written into the full vertex grid.  The operands stay in L2
+// (the grid is a few MB) and the lines of a warp share each S entry.
+template <int DIR, bool BACK, bool SCALE, bool UC>
+__global__ void __launch_bounds__(256)
+    k_crs_mode(const float* __restrict__ in, float* __restrict__ out, const float* __restrict__ S,
+               const float* __restrict__ lam, CoarseDims d, const Scalars* sc) {
   if (sc && sc->done) return;
-  extern __shared__ __align__(16) float sm[];
-  const int m0 = d.m[0], m1 = d.m[1], m2 = d.m[2], g = blockIdx.x;
-  float* V = sm;
-  float* W = V + m2 * m0;
-  float* sz = W + m2 * m0;
-  for (int q = threadIdx.x; q < m2 * m2; q += blockDim.x) sz[q] = Sz[q];
-  for (int q = threadIdx.x; q < m2 * m0; q += blockDim.x) {
-    const int f = q % m0, z = q / m0;
-    V[q] = work[f + (int64_t)m0 * (g + (int64_t)m1 * z)];
-  }
-  __syncthreads();
-  const float* lx = lam;
-  const float* ly = lam + m0;
-  const float* lz = lam + m0 + m1;
-  for (int q = threadIdx.x; q < m2 * m0; q += blockDim.x) {
-    const int f = q % m0, h = q / m0;
-    float s = 0.f;
-    for (int z = 0; z < m2; ++z) s = fmaf(sz[z * m2 + h], V[z * m0 + f], s);
-    const float D = d.h1 * (lx[f] + ly[g] + lz[h]) + d.h2;
-    W[q] = D > d.dmin ? s / D : 0.f;
-  }
-  __syncthreads();
-  for (int q = threadIdx.x; q < m2 * m0; q += blockDim.x) {
-    const int f = q % m0, z = q / m0;
-    float s = 0.f;
-    for (int h = 0; h < m2; ++h) s = fmaf(sz[z * m2 + h], W[h * m0 + f], s);
-    work[f + (int64_t)m0 * (g + (int64_t)m1 * z)] = s;
-  }
-}
-
-// y then x back transforms on one active z-plane, into the full vertex grid uc
-__global__ void __launch_bounds__(1024)
-    k_crs_yx(const float* __restrict__ work, const float* __restrict__ Sx, const float* __restrict__ Sy,
-             float* __restrict__ uc, CoarseDims d, const Scalars* sc) {
-  if (sc && sc->done) return;
-  extern __shared__ __align__(16) float sm[];
-  const int m0 = d.m[0], m1 = d.m[1], zi = blockIdx.x;
-  float* T = sm;
-  float* U = T + m0 * m1;
-  float* sx = U + m0 * m1;
-  float* sy = sx + m0 * m0;
-  for (int q = threadIdx.x; q < m0 * m0; q += blockDim.x) sx[q] = Sx[q];
-  for (int q = threadIdx.x; q < m1 * m1; q += blockDim.x) sy[q] = Sy[q];
-  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) T[q] = work[q + (int64_t)m0 * m1 * zi];
-  __syncthreads();
-  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
-    const int f = q % m0, y = q / m0;
-    float s = 0.f;
-    for (int g = 0; g < m1; ++g) s = fmaf(sy[y * m1 + g], T[g * m0 + f], s);
-    U[q] = s;
-  }
-  __syncthreads();
-  const int nx = d.Ex + 1, ny = d.Ey + 1;
-  for (int q = threadIdx.x; q < m0 * m1; q += blockDim.x) {
-    const int x = q % m0, y = q / m0;
-    float s = 0.f;
-    for (int f = 0; f < m0; ++f) s = fmaf(sx[x * m0 + f], U[y * m0 + f], s);
-    uc[(d.lo[0] + x) + (int64_t)nx * ((d.lo[1] + y) + (int64_t)ny * (d.lo[2] + zi))] = s;
+  const int m0 = d.m[0], m1 = d.m[1], m = d.m[DIR];
+  const int64_t stride = DIR == 0 ? 1 : DIR == 1 ? m0 : (int64_t)m0 * m1;
+  const int64_t total = (int64_t)m0 * m1 * d.m[2];
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)((q / stride) % m);
+    const float* src = in + (q - (int64_t)t * stride);
+    float acc = 0.f;
+    // forward S[u][t], back S^T[u][t] = S[t][u]: consecutive t read consecutive entries
+    const float* Mt = S + (BACK ? (int64_t)m * m : 0) + t;
+    for (int u = 0; u < m; ++u) acc = fmaf(Mt[(int64_t)u * m], src[u * stride], acc);
+    const int x = (int)(q % m0), y = (int)((q / m0) % m1), z = (int)(q / ((int64_t)m0 * m1));
+    if (SCALE) {
+      const float D = d.h1 * (lam[x] + lam[m0 + y] + lam[m0 + m1 + z]) + d.h2;
+      acc = D > d.dmin ? acc / D : 0.f;
+    }
+    if (UC) {
+      const int nx = d.Ex + 1, ny = d.Ey + 1;
+      out[(d.lo[0] + x) + (int64_t)nx * ((d.lo[1] + y) + (int64_t)ny * (d.lo[2] + z))] = acc;
+    } else {
+      out[q] = acc;
+    }
   }
 }
 
@@ -845,12 +794,11 @@ struct ntg_schwarz {
   int coarse = 0, coarse_ready = 0;
   ntg::sw::CoarseDims cd{};
   ntg::sw::CoarsePhi ph{};
-  float* cS[3] = {nullptr, nullptr, nullptr};  // m_d x m_d eigenvectors (S[x][f])
+  float* cS[3] = {nullptr, nullptr, nullptr};  // m_d x m_d eigenvectors S[x][f], then S^T[f][x]
   float* clam = nullptr;                       // m0 + m1 + m2 eigenvalues
   float* corner = nullptr;                     // E x 8 restricted corner sums
-  float* cwork = nullptr;                      // m0 m1 m2 transformed coarse residual
+  float* cwork = nullptr;                      // 2 x m0 m1 m2: the coarse residual through its transforms
   float* uc = nullptr;                         // (Ex+1)(Ey+1)(Ez+1) coarse correction
-  size_t smem_xy = 0, smem_z = 0;
   int mass_term = 0;
   float* dw = nullptr;  // additive diagonal term of the Brinkman mass part (n)
   // lx = 8: FDM local solves on the tensor cores (schwarz_tc.cu) when on
@@ -1054,9 +1002,14 @@ static int coarse_setup(ntg_schwarz* s) {
         Ma[i * m + j] = M[(lo + i) * nv + lo + j];
       }
     gen_eig(m, Ka, Ma, S, lam);
-    std::vector<float> Sf(S.begin(), S.end());
+    std::vector<float> Sf(2 * (size_t)m * m);
+    for (int x = 0; x < m; ++x)
+      for (int f = 0; f < m; ++f) {
+        Sf[(size_t)x * m + f] = (float)S[(size_t)x * m + f];
+        Sf[(size_t)m * m + (size_t)f * m + x] = (float)S[(size_t)x * m + f];
+      }
     dev_free(s->cS[d]);
-    NTG_TRY(dev_alloc(&s->cS[d], (size_t)m * m));
+    NTG_TRY(dev_alloc(&s->cS[d], 2 * (size_t)m * m));
     NTG_CUDA_TRY(cudaMemcpy(s->cS[d], Sf.data(), sizeof(float) * Sf.size(), cudaMemcpyHostToDevice));
     double lm = 0;
     for (double v : lam) {
@@ -1072,15 +1025,6 @@ static int coarse_setup(ntg_schwarz* s) {
   s->cd.h1 = (float)h1;
   s->cd.h2 = (float)h2;
   s->cd.dmin = (float)(1e-6 * (h1 * lmax + h2));
-  s->smem_xy = sizeof(float) * (2 * (size_t)m0 * m1 + (size_t)m0 * m0 + (size_t)m1 * m1);
-  s->smem_z = sizeof(float) * (2 * (size_t)m2 * m0 + (size_t)m2 * m2);
-  if (s->smem_xy > 227 * 1024 || s->smem_z > 227 * 1024) {
-    set_error("schwarz coarse level: vertex grid %d x %d x %d too large for one plane per block", m0, m1, m2);
-    return NTG_ERR_UNSUPPORTED;
-  }
-  NTG_CUDA_TRY(cudaFuncSetAttribute(sw::k_crs_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_xy));
-  NTG_CUDA_TRY(cudaFuncSetAttribute(sw::k_crs_yx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_xy));
-  NTG_CUDA_TRY(cudaFuncSetAttribute(sw::k_crs_z, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->smem_z));
   dev_free(s->clam);
   NTG_TRY(dev_alloc(&s->clam, lamall.size()));
   NTG_CUDA_TRY(cudaMemcpy(s->clam, lamall.data(), sizeof(float) * lamall.size(), cudaMemcpyHostToDevice));
@@ -1088,7 +1032,7 @@ static int coarse_setup(ntg_schwarz* s) {
   if (!s->corner) NTG_TRY(dev_alloc(&s->corner, (size_t)nelv * 8));
   if (!s->uc) NTG_TRY(dev_alloc(&s->uc, nv3));
   dev_free(s->cwork);
-  NTG_TRY(dev_alloc(&s->cwork, (size_t)m0 * m1 * m2));
+  NTG_TRY(dev_alloc(&s->cwork, 2 * (size_t)m0 * m1 * m2));
   NTG_CUDA_TRY(cudaMemset(s->uc, 0, sizeof(float) * nv3));
   double xi[NTG_LXMAX], wq[NTG_LXMAX], Dm[NTG_LXMAX * NTG_LXMAX];
   gll_basis(lx, xi, wq, Dm);
@@ -1199,15 +1143,27 @@ int pull_launch(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalar
   return NTG_OK;
 }
 
-// coarse solve (after the FDM kernel has written the corner sums): xy / z / yx
-// transforms into uc
+// coarse solve (after the FDM kernel has written the corner sums): the
+// restriction onto the vertex grid, then x, y, z forward (scaled), z, y, x back into uc
 inline int coarse_launch(ntg_schwarz* w, cudaStream_t s, const Scalars* sc) {
   const CoarseDims& d = w->cd;
-  k_crs_xy<<<d.m[2], 1024, w->smem_xy, s>>>(w->corner, w->cS[0], w->cS[1], w->cwork, d, sc);
+  const int64_t total = (int64_t)d.m[0] * d.m[1] * d.m[2];
+  const int g = grid_for(total, 256);
+  float* a = w->cwork;
+  float* b = w->cwork + total;
+  k_crs_restrict<<<g, 256, 0, s>>>(w->corner, a, d, sc);
   NTG_COUNT_LAUNCH();
-  k_crs_z<<<d.m[1], 1024, w->smem_z, s>>>(w->cwork, w->cS[2], w->clam, d, sc);
+  k_crs_mode<0, false, false, false><<<g, 256, 0, s>>>(a, b, w->cS[0], w->clam, d, sc);
   NTG_COUNT_LAUNCH();
-  k_crs_yx<<<d.m[2], 1024, w->smem_xy, s>>>(w->cwork, w->cS[0], w->cS[1], w->uc, d, sc);
+  k_crs_mode<1, false, false, false><<<g, 256, 0, s>>>(b, a, w->cS[1], w->clam, d, sc);
+  NTG_COUNT_LAUNCH();
+  k_crs_mode<2, false, true, false><<<g, 256, 0, s>>>(a, b, w->cS[2], w->clam, d, sc);
+  NTG_COUNT_LAUNCH();
+  k_crs_mode<2, true, false, false><<<g, 256, 0, s>>>(b, a, w->cS[2], w->clam, d, sc);
+  NTG_COUNT_LAUNCH();
+  k_crs_mode<1, true, false, false><<<g, 256, 0, s>>>(a, b, w->cS[1], w->clam, d, sc);
+  NTG_COUNT_LAUNCH();
+  k_crs_mode<0, true, false, true><<<g, 256, 0, s>>>(b, w->uc, w->cS[0], w->clam, d, sc);
   NTG_COUNT_LAUNCH();
   return NTG_OK;
 }
