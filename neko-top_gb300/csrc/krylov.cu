@@ -344,6 +344,29 @@ __global__ void k_resid(const double* __restrict__ f, const double* __restrict__
   grid_reduce<2>(v, part, sc, FinResid());
 }
 
+// x32 = (float)x
+__global__ void k_to_f32(const double* __restrict__ x, float* __restrict__ x32, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x32[i] = (float)x[i];
+}
+
+// the guard's residual from an FP32 operator image: w = (double)w32, r = f - w
+__global__ void k_resid_w32(const double* __restrict__ f, const float* __restrict__ w32, double* __restrict__ w,
+                            const double* __restrict__ mult, double* __restrict__ r, int64_t n,
+                            double* __restrict__ part, Scalars* sc) {
+  double ff = 0, rr = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double fi = f[i], wi = (double)w32[i];
+    w[i] = wi;
+    const double ri = fi - wi;
+    r[i] = ri;
+    ff += mult[i] * fi * fi;
+    rr += mult[i] * ri * ri;
+  }
+  double v[2] = {ff, rr};
+  grid_reduce<2>(v, part, sc, FinResid());
+}
+
 // inner right-hand side: rin = (float)(r / ||r||)
 __global__ void k_to_f32_scaled(const double* __restrict__ r, float* __restrict__ rin, int64_t n, const Scalars* sc) {
   const double s = 1.0 / sqrt(sc->rr);
@@ -622,7 +645,7 @@ struct ntg_ksp {
   int inner_max_iter = 400;
   int check_every = 16;
   int guess_guard = 0;
-  int ax_ready = 0;  // the guard left A x0 (FP64, assembled, masked) in v64.w for this solve
+  int ax_ready = 0;  // the guard left A x0 (assembled, masked) in v64.w for this solve: 1 FP64, 2 FP32 operator
   ntg_schwarz* sw = nullptr;  // explicit FP32 preconditioner of the cg_mixed / gmres iterations
   int restart = 30;            // gmres restart length
   ntg::GmresWork* gm = nullptr;
@@ -797,7 +820,7 @@ static int ksp_solve_mixed_ru(ntg_ksp* k, double* x, const double* f, ntg_monito
   NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
   if (xx != 0.0) {
     if (!k->ax_ready) NTG_TRY(op_apply(p, k->v64.w, x, s));  // else the guess guard's A x0 is in v64.w
-    fpax++;
+    if (k->ax_ready != 2) fpax++;  // 2: the FP32 operator's image
   }
   float* y32 = k->din;
   { k_ru_init<<<G, TPB, 0, s>>>(f, xx != 0.0 ? k->v64.w : nullptr, p->dinvf, p->mult, k->v64.r, k->v32.r, k->v32.p, y32, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
@@ -897,7 +920,7 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
   NTG_CUDA_TRY(cudaMemcpyAsync(k->sc, hs, sizeof(Scalars), cudaMemcpyHostToDevice, s));
   if (xx != 0.0) {
     if (!k->ax_ready) NTG_TRY(op_apply(p, k->v64.w, x, s));  // else the guess guard's A x0 is in v64.w
-    fpax++;
+    if (k->ax_ready != 2) fpax++;  // 2: the FP32 operator's image
   }
   float* y32 = k->din;
   float* r32 = k->v32.r;
@@ -1141,22 +1164,36 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
   if (mon) memset(mon, 0, sizeof(*mon));
   int rejected = 0;
   if (ksp->guess_guard) {
-    // a guess is kept only if its residual is below ||f||: one FP64
-    // operator application and two dots decide
+    // a guess is kept only if its residual is below ||f||: one operator
+    // application and two dots decide.  For the reliable-update mixed CG
+    // the operator is the FP32 one: its image of the guess becomes the
+    // initial residual, which the first FP64 residual replacement of that
+    // solver recomputes exactly (the FP64 operator costs 20x the FP32 one
+    // on GB300's FP64 pipe); every other solver takes the FP64 operator.
     ntg_plan* p = ksp->plan;
     cudaStream_t s = p->stream;
     double xx = 0.0;
     NTG_TRY(wdot(p, x_d, x_d, nullptr, p->n, &xx, s));
-    if (xx != 0.0) {
+    const bool fp32 = ksp->type == NTG_KSP_CG_MIXED;
+    if (xx != 0.0 && fp32) {
+      NTG_TRY(ensure_fp32(p));
+      { k_to_f32<<<grid_for(p->n, 256), 256, 0, s>>>(x_d, ksp->v32.p, p->n); NTG_COUNT_LAUNCH(); }
+      NTG_TRY(ax_launch_f32(p, ksp->v32.w, ksp->v32.p, nullptr, 0, s));
+      NTG_TRY(gs_add_guarded_f32(p, ksp->v32.w, s, nullptr));
+      NTG_TRY(mask_guarded_f32(p, ksp->v32.w, s, nullptr));
+      { k_resid_w32<<<grid_for(p->n, 256), 256, 0, s>>>(f_d, ksp->v32.w, ksp->v64.w, p->mult, ksp->v64.r, p->n, p->red_part, ksp->sc); NTG_COUNT_LAUNCH(); }
+    } else if (xx != 0.0) {
       NTG_TRY(op_apply(p, ksp->v64.w, x_d, s));
       { k_resid<<<grid_for(p->n, 256), 256, 0, s>>>(f_d, ksp->v64.w, p->mult, ksp->v64.r, p->n, p->red_part, ksp->sc); NTG_COUNT_LAUNCH(); }
+    }
+    if (xx != 0.0) {
       NTG_CUDA_TRY(cudaMemcpyAsync(ksp->hs, ksp->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, s));
       NTG_CUDA_TRY(cudaStreamSynchronize(s));
       if (!(ksp->hs->rr <= ksp->hs->ff)) {
         NTG_CUDA_TRY(cudaMemsetAsync(x_d, 0, sizeof(double) * p->n, s));
         rejected = 1;
       } else {
-        ksp->ax_ready = 1;  // the mixed CG reuses this A x0 for its initial residual
+        ksp->ax_ready = fp32 ? 2 : 1;  // the mixed CG reuses this A x0 for its initial residual
       }
     }
   }
@@ -1176,7 +1213,7 @@ int ntg_ksp_solve(ntg_ksp* ksp, double* x_d, const double* f_d, ntg_monitor* mon
   else st = ksp_solve_cg(ksp, x_d, f_d, mon);
   if (mon) {
     mon->guess_rejected = rejected;
-    if (rejected) mon->fp64_ax += 1;
+    if (rejected && ksp->type != NTG_KSP_CG_MIXED) mon->fp64_ax += 1;
   }
   ksp->ax_ready = 0;
   return st;
