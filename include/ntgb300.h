@@ -312,6 +312,10 @@ int ntg_ksp_set_tol(ntg_ksp* ksp, double rtol, double abstol);
 /* guess guard (default off): when the initial guess's residual exceeds the
    right-hand side's norm, restart from a zero guess and report
    NTG_GUESS_REJECTED in ntg_monitor.guess_rejected */
+/* cg_mixed with a structured-box Schwarz preconditioner: gather-scatter,  */
+/* mask and vector update of each iteration in one kernel (1, default) or */
+/* as three launches (0); the same sums in the same order either way.     */
+int ntg_ksp_set_fused_update(ntg_ksp* ksp, int on);
 int ntg_ksp_set_guess_guard(ntg_ksp* ksp, int on);
 /* how many iterations run between host convergence checks (default 16) */
 int ntg_ksp_set_check_every(ntg_ksp* ksp, int every);

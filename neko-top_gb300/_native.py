@@ -59,6 +59,7 @@ SIGNATURES = {
     "ntg_field_fourier": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, _i, _i, C.c_uint64, _vp, _vp]),
     "ntg_field_blobs": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, C.c_uint64, _i, _d, _vp, _vp]),
     "ntg_field_modes": (_i, [_vp, _vp, _vp, _i64, _pd, _pd, _i, _pi, _pd, _pd, _vp, _vp]),
+    "ntg_ksp_set_fused_update": (_i, [_vp, _i]),
     "ntg_ksp_set_guess_guard": (_i, [_vp, _i]),
     "ntg_ksp_set_tol": (_i, [_vp, _d, _d]),
     "ntg_ksp_set_schwarz": (_i, [_vp, _vp]),

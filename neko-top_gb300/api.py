@@ -319,6 +319,11 @@ class _ksp:
         """Restart from zero when the initial guess's residual exceeds ||f||."""
         check(lib().ntg_ksp_set_guess_guard(self._h, int(bool(on))))
 
+    def set_fused_update(self, on=True):
+        """cg_mixed with a structured-box Schwarz: gather-scatter, mask and
+        update of each iteration in one kernel (default) or three."""
+        check(lib().ntg_ksp_set_fused_update(self._h, int(bool(on))))
+
     def solve(self, x, f) -> ksp_monitor_t:
         """ksp%solve(Ax, x, f, n, coef, blst, gs): x = guess in, solution out;
         f = assembled, masked RHS."""

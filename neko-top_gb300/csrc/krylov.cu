@@ -582,6 +582,79 @@ __global__ void k_update_rr(float* __restrict__ y, const float* __restrict__ p, 
   grid_reduce<2>(v, part, sc, FinUpd());
 }
 
+// The update of k_update_rr with the gather-scatter and the mask of w done
+// in the same pass, on a structured box (elements x fastest): a thread owns
+// one row (j, k) of an element and sums, per node, the local w of every
+// element holding it -- the rows of the 1, 2 or 4 elements covering the row
+// in y and z, and the x neighbours' end values -- in ascending element
+// order (z-major, y, x), the order of the gather-scatter's groups, so every
+// copy of a node receives the same sum.  Then w is masked and y += alpha p,
+// r -= alpha w, (r, r)_mult as in k_update_rr; maskf is mult with the mask
+// in its sign (one stream for both).
+template <int LX>
+__global__ void __launch_bounds__(256)
+    k_update_box(float* __restrict__ y, const float* __restrict__ p, float* __restrict__ r,
+                 const float* __restrict__ w, const float* __restrict__ maskf, int Ex,
+                 int Ey, int Ez, double* __restrict__ part, Scalars* sc) {
+  constexpr int N = LX - 1, LX2 = LX * LX, LX3 = LX2 * LX;
+  if (sc->done) return;
+  const float alpha = (float)sc->alpha;
+  const int64_t nrow = (int64_t)Ex * Ey * Ez * LX2;
+  const int64_t sy = (int64_t)Ex * LX3, sz = (int64_t)Ex * Ey * LX3;
+  float rr = 0.f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nrow; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = t / LX2;
+    const int m = (int)(t - e * LX2), j = m % LX, k = m / LX;
+    const int64_t o = e * LX3 + (int64_t)m * LX;
+    const int64_t exy = e / Ex;
+    const int cx = (int)(e - exy * Ex), cz = (int)(exy / Ey), cy = (int)(exy - (int64_t)cz * Ey);
+    // covering rows, lower element first: offsets from the own row
+    int64_t zo[2] = {0, 0}, yo[2] = {0, 0};
+    int nz = 1, ny = 1;
+    if (k == 0 && cz > 0) { zo[0] = -sz + (int64_t)N * LX2; nz = 2; }
+    else if (k == N && cz < Ez - 1) { zo[1] = sz - (int64_t)N * LX2; nz = 2; }
+    if (j == 0 && cy > 0) { yo[0] = -sy + (int64_t)N * LX; ny = 2; }
+    else if (j == N && cy < Ey - 1) { yo[1] = sy - (int64_t)N * LX; ny = 2; }
+    const bool xl = cx > 0, xh = cx < Ex - 1;
+    float acc[LX];
+#pragma unroll
+    for (int i = 0; i < LX; ++i) acc[i] = 0.f;
+#pragma unroll
+    for (int vz = 0; vz < 2; ++vz) {
+      if (vz >= nz) break;
+#pragma unroll
+      for (int vy = 0; vy < 2; ++vy) {
+        if (vy >= ny) break;
+        const float* row = w + o + (nz == 2 ? zo[vz] : 0) + (ny == 2 ? yo[vy] : 0);
+        if (xl) acc[0] += row[N - LX3];
+#pragma unroll
+        for (int i = 0; i < LX; i += 2) {
+          const float2 v = *reinterpret_cast<const float2*>(row + i);
+          acc[i] += v.x;
+          acc[i + 1] += v.y;
+        }
+        if (xh) acc[N] += row[LX3];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < LX; i += 2) {
+      const float2 mk = *reinterpret_cast<const float2*>(maskf + o + i);  // mult, negative where masked
+      const float2 pp = *reinterpret_cast<const float2*>(p + o + i);
+      float2 yy = *reinterpret_cast<const float2*>(y + o + i);
+      float2 rv = *reinterpret_cast<const float2*>(r + o + i);
+      yy.x += alpha * pp.x;
+      yy.y += alpha * pp.y;
+      rv.x -= alpha * (mk.x > 0.f ? acc[i] : 0.f);
+      rv.y -= alpha * (mk.y > 0.f ? acc[i + 1] : 0.f);
+      *reinterpret_cast<float2*>(y + o + i) = yy;
+      *reinterpret_cast<float2*>(r + o + i) = rv;
+      rr += fabsf(mk.x) * rv.x * rv.x + fabsf(mk.y) * rv.y * rv.y;
+    }
+  }
+  double v[2] = {0.0, (double)rr};
+  grid_reduce<2>(v, part, sc, FinUpd());
+}
+
 __global__ void k_dir_z(float* __restrict__ p, const float* __restrict__ z, int64_t n, int init, const Scalars* sc) {
   if (sc->done) return;
   const float beta = init ? 0.f : (float)sc->beta;
@@ -646,6 +719,7 @@ struct ntg_ksp {
   int check_every = 16;
   int guess_guard = 0;
   int ax_ready = 0;  // the guard left A x0 (assembled, masked) in v64.w for this solve: 1 FP64, 2 FP32 operator
+  int box_update = 1;  // structured-box Schwarz: gather-scatter + mask + update in one kernel
   ntg_schwarz* sw = nullptr;  // explicit FP32 preconditioner of the cg_mixed / gmres iterations
   int restart = 30;            // gmres restart length
   ntg::GmresWork* gm = nullptr;
@@ -950,6 +1024,14 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
     if (mode == 2) { k_dir_z<<<G, TPB, 0, s>>>(p32, z32, n, 0, k->sc); NTG_COUNT_LAUNCH(); }
     return poll();
   };
+  // structured box (the Schwarz preconditioner's form): the gather-scatter of
+  // w folds into the update
+  int bx = 0, by = 0, bz = 0, box_lx = 0;
+  if (k->box_update && schwarz_box(k->sw, &bx, &by, &bz) && (p->lx == 4 || p->lx == 6 || p->lx == 8) &&
+      (int64_t)bx * by * bz == p->nelv) {
+    NTG_TRY(ensure_maskf(p));
+    box_lx = p->lx;
+  }
   NTG_TRY(poll());
   const double rr0 = hs->rr0, ff = hs->ff;
   if (!hs->done) {
@@ -977,10 +1059,21 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
     if (++guard > k->max_iter / k->check_every + 64) break;  // defensive: the device cap ends the loop first
     for (int c = 0; c < k->check_every; ++c) {
       NTG_TRY(ax_launch_f32(p, w32, p32, k->sc, 0, s));
-      NTG_TRY(gs_add_guarded_f32(p, w32, s, k->sc));
-      NTG_TRY(mask_guarded_f32(p, w32, s, k->sc));
       timer_start(TM_UPD32, s);
-      { k_update_rr<<<G, TPB, 0, s>>>(y32, p32, r32, w32, p->multf, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+      if (box_lx) {
+        // gather-scatter, mask and update in one pass over the box
+        const int GB = grid_for(n / p->lx, TPB);
+        if (box_lx == 8) k_update_box<8><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskf, bx, by, bz, p->red_part, k->sc);
+        else if (box_lx == 6) k_update_box<6><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskf, bx, by, bz, p->red_part, k->sc);
+        else k_update_box<4><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskf, bx, by, bz, p->red_part, k->sc);
+        NTG_COUNT_LAUNCH();
+      } else {
+        timer_stop(TM_UPD32, s);
+        NTG_TRY(gs_add_guarded_f32(p, w32, s, k->sc));
+        NTG_TRY(mask_guarded_f32(p, w32, s, k->sc));
+        timer_start(TM_UPD32, s);
+        { k_update_rr<<<G, TPB, 0, s>>>(y32, p32, r32, w32, p->multf, n, p->red_part, k->sc); NTG_COUNT_LAUNCH(); }
+      }
       timer_stop(TM_UPD32, s);
       timer_start(TM_PC32, s);
       NTG_TRY(precondition(0));
@@ -1148,6 +1241,15 @@ int ntg_ksp_set_tol(ntg_ksp* ksp, double rtol, double abstol) {
   NTG_CHECK_ARG(ksp && rtol >= 0 && abstol >= 0, "ntg_ksp_set_tol: bad argument");
   ksp->rtol = rtol;
   ksp->abstol = abstol;
+  return NTG_OK;
+}
+
+// the cg_mixed iteration with a structured-box Schwarz preconditioner folds
+// the gather-scatter and mask of A p into its update kernel (default on)
+int ntg_ksp_set_fused_update(ntg_ksp* ksp, int on) {
+  clear_error();
+  NTG_CHECK_ARG(ksp, "ntg_ksp_set_fused_update: null argument");
+  ksp->box_update = on ? 1 : 0;
   return NTG_OK;
 }
 

@@ -338,6 +338,26 @@ static Basis make_basis(int lx) {
   return b;
 }
 
+// mult with the Dirichlet mask folded into its sign: -mult on masked nodes
+__global__ void k_maskf(const int32_t* __restrict__ mask, int64_t nmask, const float* __restrict__ multf,
+                        float* __restrict__ maskf) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nmask; t += (int64_t)gridDim.x * blockDim.x)
+    maskf[mask[t]] = -multf[mask[t]];
+}
+
+// the multiplicity weights with the Dirichlet mask in their sign (mult on
+// free nodes, -mult on masked ones), for kernels that assemble, mask and
+// weigh in one pass
+int ensure_maskf(ntg_plan* p) {
+  if (p->maskf) return NTG_OK;
+  NTG_TRY(ensure_fp32(p));
+  NTG_TRY(dev_alloc(&p->maskf, (size_t)p->n));
+  NTG_CUDA_TRY(cudaMemcpyAsync(p->maskf, p->multf, sizeof(float) * p->n, cudaMemcpyDeviceToDevice, p->stream));
+  if (p->nmask > 0) { k_maskf<<<grid_for(p->nmask, 256), 256, 0, p->stream>>>(p->mask, p->nmask, p->multf, p->maskf); NTG_COUNT_LAUNCH(); }
+  NTG_CUDA_TRY(cudaGetLastError());
+  return NTG_OK;
+}
+
 int ensure_fp32(ntg_plan* p) {
   if (p->gf[0]) return NTG_OK;
   const int T = 256;
@@ -360,7 +380,7 @@ static void plan_free(ntg_plan* p) {
   dev_free(p->B); dev_free(p->mult); dev_free(p->multf);
   dev_free(p->perm); dev_free(p->offs); dev_free(p->sh_idx); dev_free(p->sh_off);
   dev_free(p->h1); dev_free(p->h1f); dev_free(p->hB); dev_free(p->hBf);
-  dev_free(p->mask); dev_free(p->dinv); dev_free(p->dinvf);
+  dev_free(p->mask); dev_free(p->maskf); dev_free(p->dinv); dev_free(p->dinvf);
   dev_free(p->red_part); dev_free(p->scal); dev_free(p->dev_err);
   dev_free(p->gs2); dev_free(p->gs4); dev_free(p->gs8); dev_free(p->gsx_idx); dev_free(p->gsx_off);
   dev_free(p->met); dev_free(p->binv); dev_free(p->dscr);
@@ -681,6 +701,8 @@ int ntg_plan_set_mask(ntg_plan* p, const int32_t* mask_d, int64_t nmask, int bas
   NTG_CHECK_ARG(p, "ntg_plan_set_mask: null plan");
   NTG_CHECK_ARG(nmask >= 0 && (nmask == 0 || mask_d), "ntg_plan_set_mask: bad mask");
   dev_free(p->mask);
+  dev_free(p->maskf);
+  p->maskf = nullptr;
   p->nmask = 0;
   p->jacobi_ready = 0;
   if (nmask == 0) return NTG_OK;

@@ -1196,6 +1196,14 @@ int apply_gen(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars*
 }  // namespace sw
 }  // namespace ntg
 
+int ntg::schwarz_box(const ntg_schwarz* w, int* ex, int* ey, int* ez) {
+  if (!w || w->gen) return 0;
+  *ex = w->Ex;
+  *ey = w->Ey;
+  *ez = w->Ez;
+  return 1;
+}
+
 int ntg::schwarz_apply(ntg_schwarz* w, float* z, const float* r, cudaStream_t s, Scalars* sc, const float* mult,
                        double* part, int rz_mode) {
   ntg_plan* p = w->plan;
