@@ -327,7 +327,10 @@ def run_headline_sequence(args, ws, rank, local):
         raise SystemExit(f"--warmup {W} --steps {K}: the evaluation half holds {nsol - ntrain} solves "
                          f"(W + 2K at most)")
     pc = "schwarz2" if args.pc in ("auto", "schwarz2") else args.pc
-    delta = args.delta if args.delta is not None else (1e-3 if pc == "schwarz2" else 0.1)
+    # 2.2e-4 = 1e-10^(1/3): three FP64 residuals per solve (measured on this
+    # sequence, zero guess: 0.498 s at 3e-4 against 0.518 s at 1e-3, 120 iterations
+    # either way; 127 iterations at 1e-4)
+    delta = args.delta if args.delta is not None else (2.2e-4 if pc == "schwarz2" else 0.1)
     mode = args.guess
 
     def new_seq(guess, method="cg_mixed", pc_=pc, delta_=delta):
@@ -685,7 +688,7 @@ def run_sequence(args, local):
 
     ev = lambda: torch.cuda.Event(enable_timing=True)
     pc = "schwarz2" if args.pc in ("auto", "schwarz2") else args.pc
-    delta = args.delta if args.delta is not None else (1e-3 if pc == "schwarz2" else 0.1)
+    delta = args.delta if args.delta is not None else (2.2e-4 if pc == "schwarz2" else 0.1)
     modes = tuple(args.seq_modes.split(","))
     res = {}
     for mode in modes:
@@ -1353,8 +1356,7 @@ def main(argv=None):
                         "c1/c2/c3/c5: single solves from a zero guess")
     p.add_argument("--method", choices=["cg_mixed", "fcg_mixed"], default="cg_mixed")
     p.add_argument("--delta", type=float, default=None,
-                   help="reliable-update threshold of cg_mixed (default: 2.2e-4 with schwarz2, 0.1 otherwise; "
-                        "sequences: 1e-3 with schwarz2)")
+                   help="reliable-update threshold of cg_mixed (default: 2.2e-4 with schwarz2, 0.1 otherwise)")
     p.add_argument("--pc", choices=["auto", "jacobi", "schwarz", "schwarz2"], default="auto",
                    help="FP32 preconditioner of cg_mixed (auto: two-level Schwarz for Poisson, Jacobi for Brinkman)")
     p.add_argument("--fdm-path", type=int, default=0, choices=[0, 1, 2],

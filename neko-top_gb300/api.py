@@ -1046,7 +1046,7 @@ def build_solver(coef: coef_t, cfg: solver_config_t, fast=True):
     if cfg.pc == "hsmg":
         ksp.set_schwarz(schwarz_t(coef, coarse=True))
         if kind == "cg_mixed":
-            ksp.set_inner(1e-3, 1)  # reliable-update spacing measured for the two-level Schwarz
+            ksp.set_inner(2.2e-4, 1)  # reliable-update spacing measured for the two-level Schwarz
     proj = projection_t(coef, cfg.projection_space_size, cfg.projection_hold_steps) \
         if cfg.projection_space_size > 0 else None
     return ksp, proj
