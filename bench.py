@@ -95,10 +95,14 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    _count = 0
+
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.proc = None
-        self.path = os.path.join(os.environ.get("NTG_CLOCKS_DIR", tempfile.gettempdir()), f"clocks_{os.getpid()}.csv")
+        ClockSampler._count += 1
+        self.path = os.path.join(os.environ.get("NTG_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"clocks_{os.getpid()}_{ClockSampler._count}.csv")
 
     def __enter__(self):
         try:
@@ -139,8 +143,8 @@ class ClockSampler:
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def measured_traffic(kernel, n, ncoef):
@@ -410,25 +414,34 @@ def run_headline_sequence(args, ws, rank, local):
     x_h = torch.empty(n, dtype=torch.float64).pin_memory()
     f_d = torch.empty(n, dtype=torch.float64, device=dev)
     t_e2e = 0.0
+    e2e_steps = []
+    clk_e2e = ClockSampler(local)
+    clk_e2e.__enter__()
     for t in range(t0 + K, t0 + 2 * K):
         f_h.copy_(case.rhs(t))  # prepared untimed
         chi_t = case.chi(t) if t % DESIGN_EVERY == 0 else None
         torch.cuda.synchronize()
         a, b = ev(), ev()
+        c1, c2 = ev(), ev()  # inside the step: the end of the H2D copy, the start of the D2H copy
         a.record()
         f_d.copy_(f_h, non_blocking=True)
+        c1.record()
         if chi_t is not None:
             case.set_design(t, chi_t)
             seq.coefficients_changed()
         seq.training = False
         x, mon, used, fn = seq.solve(f_d)
+        c2.record()
         x_h.copy_(x, non_blocking=True)
         b.record()
         torch.cuda.synchronize()
         t_e2e += a.elapsed_time(b) / 1e3
+        e2e_steps.append((round(a.elapsed_time(b), 1), round(a.elapsed_time(c1), 1), round(c2.elapsed_time(b), 1),
+                          mon.iter))
         assert mon.status == pkg.NTG_OK, mon
         its_eval.append(mon.iter)
         used_eval.append(used)
+    clk_e2e.__exit__(None, None, None)
     t_e2e = max_over_ranks(t_e2e, ws)
 
     # the rest of the evaluation half, untimed (iteration statistics)
@@ -592,7 +605,9 @@ def run_headline_sequence(args, ws, rank, local):
         "e2e": {"value": round(ws * K / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(n * 8),
                 "d2h_bytes_per_step": int(n * 8),
                 "note": "each step timed alone (CUDA events): H2D copy of its RHS from pinned memory, the solve "
-                        "through SolveSequence.solve, D2H copy of x; the RHS is prepared untimed between steps"},
+                        "through SolveSequence.solve, D2H copy of x; the RHS is prepared untimed between steps",
+                "steps_ms_h2d_d2h_iters": e2e_steps, "timed_iters": [m.iter for m, _, _ in mons],
+                "clocks": clk_e2e.summary()},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "setup_s": round(t_setup, 3),
