@@ -27,9 +27,10 @@
 // the fine Ax kernel computes (eight basis fields per element, masked nodes
 // zeroed), Dirichlet vertices (any copy masked) removed.  A_c is inverted
 // densely on the device (Gauss-Jordan in FP64, no pivoting: A_c is SPD)
-// and applied as an FP32 matrix-vector product; an all-Neumann operator
-// without mass term gets A_c + c 1 1^T (c = mean diagonal / nv), which
-// equals the pseudo-inverse on residuals with zero vertex sum.
+// and applied as an FP32 matrix-vector product; an operator with a constant
+// null mode (all-Neumann, no mass term: 1^T A_c 1 = 0) gets A_c + c 1 1^T
+// (c = mean diagonal / nv), which equals the pseudo-inverse on residuals
+// with zero vertex sum.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -420,7 +421,11 @@ int gen_coarse_setup(ntg_plan* p, GenTopo* g) {
       }
     }
     if (!(tr > 0.0)) { st = NTG_ERR_INVALID; set_error("schwarz (general mesh): coarse operator has no positive diagonal"); break; }
-    if (p->nmask == 0 && !p->ifh2) {
+    // a constant null mode (no Dirichlet vertex, no mass term): 1^T A_c 1
+    // vanishes against the diagonal; shift it as A_c + c 1 1^T
+    double sum = 0.0;
+    for (double a : Ah) sum += a;
+    if (std::fabs(sum) <= 1e-10 * tr) {
       const double c = tr / (double)nv / (double)nv;
       for (double& a : Ah) a += c;
     }

@@ -323,7 +323,7 @@ def coarse_galerkin(m, h1=1.0, h2=None, mask=None):
                 if vid[e, v] >= 0:
                     A[vid[e, w], vid[e, v]] += Ae[w, v]
     A = 0.5 * (A + A.T)
-    if (mask is None or len(mask) == 0) and (h2 is None or not np.any(h2)):
+    if abs(A.sum()) <= 1e-10 * np.trace(A):  # constant null mode: A + c 1 1^T
         A = A + np.trace(A) / nv / nv
     return A, vid
 

@@ -50,7 +50,7 @@ def general_coef(pkg, m, dev):
 
 
 CASES = [("box", 8, True, 0), ("box", 4, False, 2), ("box_reoriented", 8, True, 0), ("ogrid", 6, True, 0),
-         ("ogrid", 8, False, 0), ("ogrid", 8, True, 2), ("box_neumann", 6, True, 0)]
+         ("ogrid", 8, False, 0), ("ogrid", 8, True, 2), ("box_neumann", 6, True, 0), ("box_pure_neumann", 6, True, 0)]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -61,7 +61,7 @@ def test_general_apply_matches_oracle(pkg, orc, dev, case):
     rng = np.random.default_rng(5)
     if kind.startswith("box"):
         m = orc.build_mesh(3, 2, 2, lx, amp=0.05, seed=2)
-        mask = None if kind == "box_neumann" else orc.mask_face_xmax(3, 2, 2, lx)
+        mask = None if kind in ("box_neumann", "box_pure_neumann") else orc.mask_face_xmax(3, 2, 2, lx)
         if kind == "box_reoriented":
             flag = np.zeros(m.n)
             flag[mask - 1] = 1
@@ -75,7 +75,13 @@ def test_general_apply_matches_oracle(pkg, orc, dev, case):
     if mask is not None:
         c.set_mask(T(mask, dev, torch.int32), base=1)
     h2 = rng.uniform(0.0, 2.0, m.n)
-    c.set_coefs(h1c=0.5, h2=T(h2, dev), ifh2=True)
+    if kind == "box_pure_neumann":
+        # no Dirichlet vertex and no mass term: the coarse operator's constant
+        # null mode is shifted (A_c + c 1 1^T) on both sides
+        h2 = None
+        c.set_coefs(h1c=0.5, ifh2=False)
+    else:
+        c.set_coefs(h1c=0.5, h2=T(h2, dev), ifh2=True)
     sw = pkg.schwarz_t(c, coarse=coarse)
     assert sw.general
     sw.set_fdm_path(path)
