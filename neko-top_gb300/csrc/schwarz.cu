@@ -618,10 +618,11 @@ __global__ void k_mass_term(const double* __restrict__ hBa, const double* __rest
 // 2x2x2 combinations are summed z-major, y, x (= ascending element index).
 // A thread handles one row (j, k) of an element: per covering (y, z) choice
 // it reads the covering element's extended row (LE values, float2 pairs) and
-// the adjacent pair of each x neighbour.  DOT: also (r, z)_mult, reduced
-// deterministically and finalised by FinRz (the mask applied afterwards does
-// not change it: r vanishes on masked nodes).  cv.uc: plus the trilinear
-// prolongation of the coarse correction.
+// the adjacent pair of each x neighbour.  DOT: also (r, z)_mult, summed over
+// each node's owning copy (no multiplicity stream), reduced deterministically
+// and finalised by FinRz (the mask applied afterwards does not change it: r
+// vanishes on masked nodes); the mult argument only selects this variant.
+// cv.uc: plus the trilinear prolongation of the coarse correction.
 template <int LX, bool DOT>
 __global__ void __launch_bounds__(256, 4)
     k_pull(const float* __restrict__ ze, float* __restrict__ z, int Ex, int Ey, int Ez,
@@ -643,19 +644,12 @@ __global__ void __launch_bounds__(256, 4)
     const int e = (int)(t / LX2);
     const int m = (int)(t - (int64_t)e * LX2), j = m % LX, k = m / LX;
     const int64_t o = (int64_t)e * LX3 + (int64_t)m * LX;  // first node of the row in z / r / mult
-    float rv[LX], mv[LX];
+    float rv[LX];
     if (DOT || cv.dw) {
 #pragma unroll
       for (int q = 0; q < LX; q += 2) {
         const float2 r2 = *reinterpret_cast<const float2*>(r + o + q);
         rv[q] = r2.x; rv[q + 1] = r2.y;
-      }
-    }
-    if constexpr (DOT) {
-#pragma unroll
-      for (int q = 0; q < LX; q += 2) {
-        const float2 m2 = *reinterpret_cast<const float2*>(mult + o + q);
-        mv[q] = m2.x; mv[q + 1] = m2.y;
       }
     }
     const int exy = e / Ex, cx = e - exy * Ex, cz = exy / Ey, cy = exy - cz * Ey;
@@ -730,8 +724,14 @@ __global__ void __launch_bounds__(256, 4)
 #pragma unroll
     for (int q = 0; q < LX; q += 2) *reinterpret_cast<float2*>(z + o + q) = make_float2(acc[q], acc[q + 1]);
     if constexpr (DOT) {
+      // each global node once, from the element that owns it (the copy with
+      // no lower neighbour in any direction): the sum over unique nodes that
+      // the mult-weighted sum over local copies equals, without the mult stream
+      if ((j > 0 || cy == 0) && (k > 0 || cz == 0)) {
 #pragma unroll
-      for (int i = 0; i < LX; ++i) rz += mv[i] * rv[i] * acc[i];
+        for (int i = 0; i < LX; ++i)
+          if (i > 0 || cx == 0) rz += rv[i] * acc[i];
+      }
     }
   }
   if constexpr (DOT) {
