@@ -133,7 +133,7 @@ struct ntg_plan {
   // Dirichlet mask (0-based)
   int32_t* mask = nullptr;
   int64_t nmask = 0;
-  float* maskf = nullptr;  // n: multf with the mask in its sign, -multf on masked nodes (built on first use)
+  uint8_t* maskrow = nullptr;  // n / lx (lx <= 8): bit i of byte t set when node i of row t is masked (built on first use)
   // Jacobi
   double* dinv = nullptr;
   float* dinvf = nullptr;
@@ -195,7 +195,7 @@ template <typename T>
 int gs_cls_launch(ntg_plan* p, T* u, int op, cudaStream_t s, const Scalars* sc);
 int grid_for(int64_t work, int threads);
 int jacobi_update(ntg_plan* p);
-int ensure_maskf(ntg_plan* p);
+int ensure_maskrow(ntg_plan* p);
 // the element counts of a Schwarz preconditioner built on a structured box
 // (1), or 0 for one built on a general mesh
 int schwarz_box(const ntg_schwarz* w, int* ex, int* ey, int* ez);

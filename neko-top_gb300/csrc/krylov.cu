@@ -588,13 +588,14 @@ __global__ void k_update_rr(float* __restrict__ y, const float* __restrict__ p, 
 // element holding it -- the rows of the 1, 2 or 4 elements covering the row
 // in y and z, and the x neighbours' end values -- in ascending element
 // order (z-major, y, x), the order of the gather-scatter's groups, so every
-// copy of a node receives the same sum.  Then w is masked and y += alpha p,
-// r -= alpha w, (r, r)_mult as in k_update_rr; maskf is mult with the mask
-// in its sign (one stream for both).
+// copy of a node receives the same sum.  Then w is masked (one mask byte per
+// row) and y += alpha p, r -= alpha w; (r, r)_mult is summed over each
+// node's owning copy (no lower neighbour in any direction), which the
+// mult-weighted sum over copies equals, with no multiplicity stream.
 template <int LX>
 __global__ void __launch_bounds__(256)
     k_update_box(float* __restrict__ y, const float* __restrict__ p, float* __restrict__ r,
-                 const float* __restrict__ w, const float* __restrict__ maskf, int Ex,
+                 const float* __restrict__ w, const uint8_t* __restrict__ maskrow, int Ex,
                  int Ey, int Ez, double* __restrict__ part, Scalars* sc) {
   constexpr int N = LX - 1, LX2 = LX * LX, LX3 = LX2 * LX;
   if (sc->done) return;
@@ -636,19 +637,23 @@ __global__ void __launch_bounds__(256)
         if (xh) acc[N] += row[LX3];
       }
     }
+    const unsigned mb = maskrow[t];
+    const bool own_jk = (j > 0 || cy == 0) && (k > 0 || cz == 0);
 #pragma unroll
     for (int i = 0; i < LX; i += 2) {
-      const float2 mk = *reinterpret_cast<const float2*>(maskf + o + i);  // mult, negative where masked
       const float2 pp = *reinterpret_cast<const float2*>(p + o + i);
       float2 yy = *reinterpret_cast<const float2*>(y + o + i);
       float2 rv = *reinterpret_cast<const float2*>(r + o + i);
       yy.x += alpha * pp.x;
       yy.y += alpha * pp.y;
-      rv.x -= alpha * (mk.x > 0.f ? acc[i] : 0.f);
-      rv.y -= alpha * (mk.y > 0.f ? acc[i + 1] : 0.f);
+      rv.x -= alpha * (((mb >> i) & 1u) ? 0.f : acc[i]);
+      rv.y -= alpha * (((mb >> (i + 1)) & 1u) ? 0.f : acc[i + 1]);
       *reinterpret_cast<float2*>(y + o + i) = yy;
       *reinterpret_cast<float2*>(r + o + i) = rv;
-      rr += fabsf(mk.x) * rv.x * rv.x + fabsf(mk.y) * rv.y * rv.y;
+      if (own_jk) {
+        if (i > 0 || cx == 0) rr += rv.x * rv.x;
+        rr += rv.y * rv.y;  // node i + 1 > 0
+      }
     }
   }
   double v[2] = {0.0, (double)rr};
@@ -1029,7 +1034,7 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
   int bx = 0, by = 0, bz = 0, box_lx = 0;
   if (k->box_update && schwarz_box(k->sw, &bx, &by, &bz) && (p->lx == 4 || p->lx == 6 || p->lx == 8) &&
       (int64_t)bx * by * bz == p->nelv) {
-    NTG_TRY(ensure_maskf(p));
+    NTG_TRY(ensure_maskrow(p));
     box_lx = p->lx;
   }
   NTG_TRY(poll());
@@ -1063,9 +1068,9 @@ static int ksp_solve_mixed_ru_pc(ntg_ksp* k, double* x, const double* f, ntg_mon
       if (box_lx) {
         // gather-scatter, mask and update in one pass over the box
         const int GB = grid_for(n / p->lx, TPB);
-        if (box_lx == 8) k_update_box<8><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskf, bx, by, bz, p->red_part, k->sc);
-        else if (box_lx == 6) k_update_box<6><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskf, bx, by, bz, p->red_part, k->sc);
-        else k_update_box<4><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskf, bx, by, bz, p->red_part, k->sc);
+        if (box_lx == 8) k_update_box<8><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskrow, bx, by, bz, p->red_part, k->sc);
+        else if (box_lx == 6) k_update_box<6><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskrow, bx, by, bz, p->red_part, k->sc);
+        else k_update_box<4><<<GB, TPB, 0, s>>>(y32, p32, r32, w32, p->maskrow, bx, by, bz, p->red_part, k->sc);
         NTG_COUNT_LAUNCH();
       } else {
         timer_stop(TM_UPD32, s);

@@ -12,6 +12,8 @@
 #include <atomic>
 #include <mutex>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace ntg {
@@ -338,23 +340,25 @@ static Basis make_basis(int lx) {
   return b;
 }
 
-// mult with the Dirichlet mask folded into its sign: -mult on masked nodes
-__global__ void k_maskf(const int32_t* __restrict__ mask, int64_t nmask, const float* __restrict__ multf,
-                        float* __restrict__ maskf) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nmask; t += (int64_t)gridDim.x * blockDim.x)
-    maskf[mask[t]] = -multf[mask[t]];
-}
-
-// the multiplicity weights with the Dirichlet mask in their sign (mult on
-// free nodes, -mult on masked ones), for kernels that assemble, mask and
-// weigh in one pass
-int ensure_maskf(ntg_plan* p) {
-  if (p->maskf) return NTG_OK;
-  NTG_TRY(ensure_fp32(p));
-  NTG_TRY(dev_alloc(&p->maskf, (size_t)p->n));
-  NTG_CUDA_TRY(cudaMemcpyAsync(p->maskf, p->multf, sizeof(float) * p->n, cudaMemcpyDeviceToDevice, p->stream));
-  if (p->nmask > 0) { k_maskf<<<grid_for(p->nmask, 256), 256, 0, p->stream>>>(p->mask, p->nmask, p->multf, p->maskf); NTG_COUNT_LAUNCH(); }
-  NTG_CUDA_TRY(cudaGetLastError());
+// the Dirichlet mask as one bit per node, a byte per row of lx <= 8 nodes
+// (rows x fastest, n / lx bytes), for kernels that assemble and mask a row
+// in one pass; built on the host from the mask list
+int ensure_maskrow(ntg_plan* p) {
+  if (p->maskrow) return NTG_OK;
+  if (p->lx > 8) {
+    set_error("mask rows: lx=%d above 8", p->lx);
+    return NTG_ERR_UNSUPPORTED;
+  }
+  const int64_t rows = p->n / p->lx;
+  std::vector<uint8_t> bits((size_t)rows, 0);
+  if (p->nmask > 0) {
+    std::vector<int32_t> mk((size_t)p->nmask);
+    NTG_CUDA_TRY(cudaMemcpyAsync(mk.data(), p->mask, sizeof(int32_t) * mk.size(), cudaMemcpyDeviceToHost, p->stream));
+    NTG_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    for (int32_t l : mk) bits[l / p->lx] |= (uint8_t)(1u << (l % p->lx));
+  }
+  NTG_TRY(dev_alloc(&p->maskrow, (size_t)rows));
+  NTG_CUDA_TRY(cudaMemcpy(p->maskrow, bits.data(), (size_t)rows, cudaMemcpyHostToDevice));
   return NTG_OK;
 }
 
@@ -380,7 +384,7 @@ static void plan_free(ntg_plan* p) {
   dev_free(p->B); dev_free(p->mult); dev_free(p->multf);
   dev_free(p->perm); dev_free(p->offs); dev_free(p->sh_idx); dev_free(p->sh_off);
   dev_free(p->h1); dev_free(p->h1f); dev_free(p->hB); dev_free(p->hBf);
-  dev_free(p->mask); dev_free(p->maskf); dev_free(p->dinv); dev_free(p->dinvf);
+  dev_free(p->mask); dev_free(p->maskrow); dev_free(p->dinv); dev_free(p->dinvf);
   dev_free(p->red_part); dev_free(p->scal); dev_free(p->dev_err);
   dev_free(p->gs2); dev_free(p->gs4); dev_free(p->gs8); dev_free(p->gsx_idx); dev_free(p->gsx_off);
   dev_free(p->met); dev_free(p->binv); dev_free(p->dscr);
@@ -701,8 +705,8 @@ int ntg_plan_set_mask(ntg_plan* p, const int32_t* mask_d, int64_t nmask, int bas
   NTG_CHECK_ARG(p, "ntg_plan_set_mask: null plan");
   NTG_CHECK_ARG(nmask >= 0 && (nmask == 0 || mask_d), "ntg_plan_set_mask: bad mask");
   dev_free(p->mask);
-  dev_free(p->maskf);
-  p->maskf = nullptr;
+  dev_free(p->maskrow);
+  p->maskrow = nullptr;
   p->nmask = 0;
   p->jacobi_ready = 0;
   if (nmask == 0) return NTG_OK;
