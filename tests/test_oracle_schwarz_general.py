@@ -59,8 +59,8 @@ def zone_mask(lx, gid, faces):
 
 
 def test_orientation_independent(orc, dofmap):
-    """Re-orienting every element by a random cube symmetry permutes the
-    result and changes nothing else."""
+    """Re-orienting every element by a random rotation of the cube permutes
+    the result and changes nothing else."""
     ex, ey, ez, lx = 3, 2, 2, 4
     m = orc.build_mesh(ex, ey, ez, lx, amp=0.05, seed=1)
     mask = orc.mask_face_xmax(ex, ey, ez, lx)
@@ -121,3 +121,26 @@ def test_reference_pipe(orc, dofmap, pkg):
     print("reference pipe: jacobi", itj, "two-level Schwarz", its)
     assert its < 0.5 * itj
     assert np.linalg.norm(xs - xj) <= 1e-8 * np.linalg.norm(xj)
+
+
+def test_ogrid_orientation_independent(orc, dofmap):
+    """On the O-grid pipe (edges shared by three elements), re-orienting
+    every element by a random rotation permutes the result, nothing else."""
+    ev, xyz, zones = meshgen.ogrid_pipe(2, 1, 2)
+    lx = 4
+    gid = dofmap.dofmap_from_vertices(ev, lx)
+    x, y, z = meshgen.nodes_from_vertices(xyz, lx)
+    m = orc.mesh_general(x, y, z, gid, lx)
+    mask = zone_mask(lx, gid, [(e - 1, f - 1) for e, f, _, lab, *_ in zones if lab == 2])
+    rng = np.random.default_rng(11)
+    r = orc.apply_mask_zero(orc.gs_op(m, rng.standard_normal(m.n)) * m.mult, mask)
+    ref = schwarz_ref.apply_general(m, r, h1=1.0, mask=mask, coarse=True)
+    flag = np.zeros(m.n)
+    flag[mask - 1] = 1.0
+    idx = np.arange(m.n, dtype=np.float64)
+    _, (x2, y2, z2, g2, r2, f2, i2) = meshgen.reorient(lx, ev, [x, y, z, gid, r, flag, idx], rng)
+    m2 = orc.mesh_general(x2, y2, z2, g2.astype(np.int64), lx)
+    assert m2.B.min() > 0
+    mask2 = (np.nonzero(f2)[0] + 1).astype(np.int32)
+    z2v = schwarz_ref.apply_general(m2, r2, h1=1.0, mask=mask2, coarse=True)
+    assert np.allclose(z2v, ref[i2.astype(np.int64)], rtol=1e-11, atol=1e-12 * np.abs(ref).max())
