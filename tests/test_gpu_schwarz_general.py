@@ -188,3 +188,48 @@ def test_cg_mixed_on_nmsh_ogrid(pkg, orc, dev, tmp_path, coarse):
           "error", err)
     assert err <= 1e-8
     assert mon.iter < (0.35 if coarse else 0.6) * it_ref
+
+
+@pytest.mark.parametrize("kind", ["gmres", "gmres_mixed"])
+def test_gmres_with_general_schwarz(pkg, orc, dev, kind):
+    """The reference's pressure solver pairing (GMRES + the Schwarz part of
+    'hsmg') on the O-grid pipe: converges to the oracle's solution."""
+    m, _, _, zones = ogrid(orc, pkg, 6)
+    mask = outlet_mask(m, zones)
+    c = general_coef(pkg, m, dev)
+    c.set_mask(T(mask, dev, torch.int32), base=1)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    k, a, ph = orc.fourier_params(7, 8)
+    f = orc.assemble_rhs(m, orc.field_fourier(m, k, a, ph), mask)
+    x_ref, it_ref, _, _ = orc.cg(m, f, mask=mask, rtol=1e-13, max_iter=20000)
+    ksp = pkg.krylov_solver_factory(c, kind, 5000, 1e-10)
+    ksp.set_schwarz(pkg.schwarz_t(c, coarse=True))
+    x = torch.zeros(m.n, dtype=torch.float64, device=dev)
+    mon = ksp.solve(x, T(f, dev))
+    torch.cuda.synchronize()
+    assert mon.status == pkg.NTG_OK, mon
+    xn = x.cpu().numpy()
+    r = f - orc.op_apply(m, xn, mask=mask)
+    assert np.sqrt(orc.glsc3(r, r, m.mult)) <= 1.5e-10 * np.sqrt(orc.glsc3(f, f, m.mult))
+    assert np.linalg.norm(xn - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+    print(kind, "iterations", mon.iter, "(Jacobi-PCG oracle", it_ref, ")")
+    assert mon.iter < 0.5 * it_ref
+
+
+def test_dense_coarse_limit(pkg, orc, dev):
+    """The general form's dense coarse level takes at most 8192 active
+    vertices: above that the coarse level is refused with a clear error and
+    the one-level form still works."""
+    ex = ey = ez = 21  # 22^3 = 10,648 vertices
+    lx = 4
+    c = pkg.coef_t.box(ex, ey, ez, lx, amp=0.0, seed=1, device=dev)
+    c.set_coefs(h1c=1.0, ifh2=False)
+    with pytest.raises(pkg.NtgError, match="at most 8192"):
+        pkg.schwarz_t(c, coarse=True, general=True)
+    sw = pkg.schwarz_t(c, coarse=False, general=True)
+    r = torch.randn(c.n, dtype=torch.float32, device=dev)
+    pkg.gs_t(c).op(r)
+    z = torch.empty_like(r)
+    sw.apply(z, r)
+    torch.cuda.synchronize()
+    assert torch.isfinite(z).all()
