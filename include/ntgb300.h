@@ -268,6 +268,12 @@ int ntg_schwarz_create(ntg_plan* plan, int ex, int ey, int ez, const double* x_d
                        const double* z_d, ntg_schwarz** sw);
 int ntg_schwarz_create_general(ntg_plan* plan, const double* x_d, const double* y_d, const double* z_d,
                                ntg_schwarz** sw);
+/* The general form's face-neighbour table, on the host (no device needed): */
+/* gid_h the global node id of every local node (nelv * lx^3); ghost_h      */
+/* (nelv * 6 * lx^2) receives, per element face (r-, r+, s-, s+, t-, t+) and */
+/* face node (tangential indices, lower axis fastest), the 0-based local    */
+/* index one step inside the face neighbour, -1 on the boundary.            */
+int ntg_schwarz_ghost_table(int64_t nelv, int lx, const int64_t* gid_h, int32_t* ghost_h);
 /* refresh the element means of h1 / h2 after ntg_coef_set (and, with the  */
 /* coarse level on, its Dirichlet faces from the plan's mask and h1/h2)    */
 int ntg_schwarz_update(ntg_schwarz* sw);

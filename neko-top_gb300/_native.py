@@ -65,6 +65,7 @@ SIGNATURES = {
     "ntg_ksp_set_schwarz": (_i, [_vp, _vp]),
     "ntg_schwarz_create": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, C.POINTER(_vp)]),
     "ntg_schwarz_create_general": (_i, [_vp, _vp, _vp, _vp, C.POINTER(_vp)]),
+    "ntg_schwarz_ghost_table": (_i, [C.c_int64, _i, _vp, _vp]),
     "ntg_nmsh_info": (_i, [C.c_char_p, _vp, _vp, _vp, _vp]),
     "ntg_nmsh_read": (_i, [C.c_char_p, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ntg_nmsh_write": (_i, [C.c_char_p, C.c_int32, C.c_int32, _vp, _vp, _vp, C.c_int32, _vp, C.c_int32, _vp, _vp, _vp]),

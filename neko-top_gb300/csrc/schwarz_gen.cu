@@ -210,9 +210,65 @@ void gen_free(GenTopo* g) {
   delete g;
 }
 
+// The face-neighbour table of a conforming hexahedral mesh from the global
+// node of every local node (gn: nelv * lx^3 entries, any integer ids):
+// faces are keyed by their four corner nodes (sorted), pairs of equal keys
+// are neighbours, and each face node is matched to the neighbour's node with
+// the same id, so neighbours may meet in any relative orientation.
+// ghost[(e * 6 + f) * lx^2 + p]: the local index one step inside the
+// neighbour across face f from face node p, -1 on the boundary.
+int ghost_table(int64_t E, int lx, const int64_t* gn, std::vector<int32_t>& ghost) {
+  const int N = lx - 1, LX2 = lx * lx, LX3 = LX2 * lx;
+  std::vector<FaceRec> faces((size_t)E * 6);
+  for (int64_t e = 0; e < E; ++e)
+    for (int f = 0; f < 6; ++f) {
+      const int nrm = (f & 1) ? N : 0;
+      FaceRec& fr = faces[e * 6 + f];
+      for (int c = 0; c < 4; ++c) fr.key[c] = gn[e * LX3 + face_node(lx, f, (c & 1) ? N : 0, (c >> 1) ? N : 0, nrm)];
+      std::sort(fr.key.begin(), fr.key.end());
+      fr.ef = e * 6 + f;
+    }
+  std::sort(faces.begin(), faces.end());
+  ghost.assign((size_t)E * 6 * LX2, -1);
+  std::vector<std::pair<int64_t, int>> tb((size_t)LX2);
+  auto match = [&](int64_t efA, int64_t efB) {
+    const int64_t eA = efA / 6, eB = efB / 6;
+    const int fA = (int)(efA % 6), fB = (int)(efB % 6);
+    const int nA = (fA & 1) ? N : 0, nB = (fB & 1) ? N : 0, inB = (fB & 1) ? N - 1 : 1;
+    for (int t = 0; t < lx; ++t)
+      for (int s = 0; s < lx; ++s) tb[s + lx * t] = {gn[eB * LX3 + face_node(lx, fB, s, t, nB)], s + lx * t};
+    std::sort(tb.begin(), tb.end());
+    for (int t = 0; t < lx; ++t)
+      for (int s = 0; s < lx; ++s) {
+        const int64_t key = gn[eA * LX3 + face_node(lx, fA, s, t, nA)];
+        auto it = std::lower_bound(tb.begin(), tb.end(), std::make_pair(key, -1));
+        if (it == tb.end() || it->first != key) return false;
+        const int sB = it->second % lx, tB = it->second / lx;
+        ghost[efA * LX2 + s + lx * t] = (int32_t)(eB * LX3 + face_node(lx, fB, sB, tB, inB));
+      }
+    return true;
+  };
+  for (size_t a = 0; a < faces.size();) {
+    size_t b = a + 1;
+    while (b < faces.size() && faces[b].key == faces[a].key) ++b;
+    if (b - a == 2) {
+      if (!match(faces[a].ef, faces[a + 1].ef) || !match(faces[a + 1].ef, faces[a].ef)) {
+        set_error("schwarz (general mesh): elements %lld and %lld share face corners but not the face's nodes",
+                  (long long)(faces[a].ef / 6), (long long)(faces[a + 1].ef / 6));
+        return NTG_ERR_INVALID;
+      }
+    } else if (b - a > 2) {
+      set_error("schwarz (general mesh): a face is shared by %d elements (non-conforming mesh)", (int)(b - a));
+      return NTG_ERR_INVALID;
+    }
+    a = b;
+  }
+  return NTG_OK;
+}
+
 int gen_create(ntg_plan* p, GenTopo** out) {
   *out = nullptr;
-  const int lx = p->lx, N = lx - 1, LX2 = lx * lx, LX3 = LX2 * lx, LE = lx + 2, LE3 = LE * LE * LE;
+  const int lx = p->lx, LX2 = lx * lx, LX3 = LX2 * lx, LE = lx + 2, LE3 = LE * LE * LE;
   const int64_t n = p->n, E = p->nelv, nu = p->nu;
   if (E * (int64_t)LE3 >= ((int64_t)1 << 31)) {
     set_error("schwarz (general mesh): nelv * (lx+2)^3 must be below 2^31");
@@ -233,52 +289,8 @@ int gen_create(ntg_plan* p, GenTopo** out) {
   for (int64_t q = 0; q < nu; ++q)
     for (int64_t t = offs[q]; t < offs[q + 1]; ++t) g->gnum[perm[t]] = q;
   const std::vector<int64_t>& gn = g->gnum;
-  // faces keyed by their corners' global nodes; pairs are neighbours
-  std::vector<FaceRec> faces((size_t)E * 6);
-  for (int64_t e = 0; e < E; ++e)
-    for (int f = 0; f < 6; ++f) {
-      const int nrm = (f & 1) ? N : 0;
-      FaceRec& fr = faces[e * 6 + f];
-      for (int c = 0; c < 4; ++c) fr.key[c] = gn[e * LX3 + face_node(lx, f, (c & 1) ? N : 0, (c >> 1) ? N : 0, nrm)];
-      std::sort(fr.key.begin(), fr.key.end());
-      fr.ef = e * 6 + f;
-    }
-  std::sort(faces.begin(), faces.end());
-  std::vector<int32_t> ghost((size_t)E * 6 * LX2, -1);
-  std::vector<std::pair<int64_t, int>> tb((size_t)LX2);
-  int st = NTG_OK;
-  auto match = [&](int64_t efA, int64_t efB) {
-    const int64_t eA = efA / 6, eB = efB / 6;
-    const int fA = (int)(efA % 6), fB = (int)(efB % 6);
-    const int nA = (fA & 1) ? N : 0, nB = (fB & 1) ? N : 0, inB = (fB & 1) ? N - 1 : 1;
-    for (int t = 0; t < lx; ++t)
-      for (int s = 0; s < lx; ++s) tb[s + lx * t] = {gn[eB * LX3 + face_node(lx, fB, s, t, nB)], s + lx * t};
-    std::sort(tb.begin(), tb.end());
-    for (int t = 0; t < lx; ++t)
-      for (int s = 0; s < lx; ++s) {
-        const int64_t key = gn[eA * LX3 + face_node(lx, fA, s, t, nA)];
-        auto it = std::lower_bound(tb.begin(), tb.end(), std::make_pair(key, -1));
-        if (it == tb.end() || it->first != key) return false;
-        const int sB = it->second % lx, tB = it->second / lx;
-        ghost[efA * LX2 + s + lx * t] = (int32_t)(eB * LX3 + face_node(lx, fB, sB, tB, inB));
-      }
-    return true;
-  };
-  for (size_t a = 0; a < faces.size() && !st;) {
-    size_t b = a + 1;
-    while (b < faces.size() && faces[b].key == faces[a].key) ++b;
-    if (b - a == 2) {
-      if (!match(faces[a].ef, faces[a + 1].ef) || !match(faces[a + 1].ef, faces[a].ef)) {
-        set_error("schwarz (general mesh): elements %lld and %lld share face corners but not the face's nodes",
-                  (long long)(faces[a].ef / 6), (long long)(faces[a + 1].ef / 6));
-        st = NTG_ERR_INVALID;
-      }
-    } else if (b - a > 2) {
-      set_error("schwarz (general mesh): a face is shared by %d elements (non-conforming mesh)", (int)(b - a));
-      st = NTG_ERR_INVALID;
-    }
-    a = b;
-  }
+  std::vector<int32_t> ghost;
+  int st = ghost_table(E, lx, gn.data(), ghost);
   // every global node's covering list: own copies' interiors, then the ghost layers reaching it
   std::vector<int64_t> soff;
   std::vector<int32_t> src;
@@ -505,3 +517,13 @@ int gen_pull_launch(GenTopo* g, const float* ze, float* z, const float* r, const
 
 }  // namespace sw
 }  // namespace ntg
+
+extern "C" int ntg_schwarz_ghost_table(int64_t nelv, int lx, const int64_t* gid, int32_t* ghost) {
+  ntg::clear_error();
+  NTG_CHECK_ARG(nelv > 0 && lx >= 2 && lx <= NTG_LXMAX && gid && ghost, "ntg_schwarz_ghost_table: bad argument");
+  NTG_CHECK_ARG(nelv * (int64_t)lx * lx * lx < ((int64_t)1 << 31), "ntg_schwarz_ghost_table: n must be < 2^31");
+  std::vector<int32_t> tab;
+  NTG_TRY(ntg::sw::ghost_table(nelv, lx, gid, tab));
+  memcpy(ghost, tab.data(), sizeof(int32_t) * tab.size());
+  return NTG_OK;
+}
