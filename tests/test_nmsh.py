@@ -96,3 +96,28 @@ def test_bad_files(nm, tmp_path, pkg):
         nm.read(trunc)
     with pytest.raises(pkg.NtgError):
         nm.read(tmp_path / "missing.nmsh")
+
+
+def test_face_mask_covers_every_copy(nm, pkg):
+    """nmsh.face_mask: every local copy of every node on the selected zone
+    faces, 1-based, sorted (host arrays: the coefficients are not needed)."""
+    import torch
+
+    ev, xyz, zones = meshgen.ogrid_pipe(2, 1, 2)
+    lx = 4
+    gid = pkg.dofmap.dofmap_from_vertices(ev, lx)
+
+    class Stub:
+        pass
+
+    c = Stub()
+    c.lx, c.gid, c.device = lx, torch.from_numpy(gid), torch.device("cpu")
+    m = nm.nmsh_t(3, np.arange(1, len(ev) + 1, dtype=np.int32), ev.astype(np.int32), xyz, zones)
+    faces = m.zone_faces(labels=[2])
+    mask = nm.face_mask(c, faces).numpy()
+    # the nodes on those faces, by position: z = length
+    X = meshgen.nodes_from_vertices(xyz, lx)
+    on_face = np.isclose(X[2], 1.5)
+    assert np.array_equal(np.sort(mask), np.nonzero(on_face)[0] + 1)
+    assert mask.dtype == np.int32 and np.all(np.diff(mask) > 0)
+    assert len(nm.face_mask(c, [])) == 0
